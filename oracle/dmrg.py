@@ -1,0 +1,199 @@
+"""Two-site DMRG in numpy: LocalOp::product, davidson, LocalMPO environments,
+MPS::svdBond and the DMRGWorker sweep loop.
+
+Restates:
+  * LocalOp::product              itensor/mps/localop.h:324-365 (size :488-530)
+  * davidson (block size 1)       itensor/iterativesolvers.h:99-451
+  * LocalMPO position/makeL/makeR itensor/mps/localmpo.h:443-470, 542-618
+  * MPS::svdBond                  itensor/mps/mps_impl.h:21-99
+  * DMRGWorker / sweepnext        itensor/mps/dmrg.h:336-467, itensor/mps/sweeps.h:489-503
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .blocksparse import BSTensor, contract, dot
+from .decomp import denmat_decomp, svd_split
+
+
+class LocalOp:
+    def __init__(self, W1, W2, L=None, R=None):
+        self.W1, self.W2, self.L, self.R = W1, W2, L, R
+
+    def product(self, phi: BSTensor) -> BSTensor:
+        if self.L is None:
+            p = phi
+            if self.R is not None:
+                p = contract(p, self.R)
+            p = contract(p, self.W2)
+            p = contract(p, self.W1)
+        else:
+            p = contract(phi, self.L)
+            p = contract(p, self.W1)
+            p = contract(p, self.W2)
+            if self.R is not None:
+                p = contract(p, self.R)
+        return p.noprime()
+
+    def size(self, phi: BSTensor) -> int:
+        n = 1
+        for I in phi.inds:
+            n *= I.dim
+        return n
+
+
+def davidson(A: LocalOp, phi: BSTensor, maxiter=2, errgoal=1e-14, miniter=1, rng=None):
+    """Returns (energy, phi). Real arithmetic; the projected matrix is real
+    symmetric and is diagonalised as -M ascending (diagHermitian)."""
+    approx0 = 1e-12
+    nrm = phi.norm()
+    phi = phi.scale(1.0 / nrm)
+    maxsize = A.size(phi)
+    actual_maxiter = min(maxiter, maxsize - 1)
+    V = [None] * (actual_maxiter + 2)
+    AV = [None] * (actual_maxiter + 2)
+    M = np.full((actual_maxiter + 2, actual_maxiter + 2), np.nan)
+    V[0] = phi
+    AV[0] = A.product(V[0])
+    initEn = dot(V[0], AV[0])
+    last_lambda = 1000.0
+    lam = np.nan
+    U = None
+    qnorm = np.nan
+    phi_t = phi
+    for ii in range(actual_maxiter + 1):
+        ni = ii + 1
+        if ii == 0:
+            lam = initEn
+            M[0, 0] = lam
+            q = AV[0] - V[0].scale(lam)
+        else:
+            Mref = M[:ii + 1, :ii + 1]
+            # diagHermitian(-M) then negated: eigenvalues of M ascending
+            D, U = np.linalg.eigh(Mref)
+            lam = D[0]
+            phi_t = V[0].scale(U[0, 0])
+            q = AV[0].scale(U[0, 0])
+            for k in range(1, ii + 1):
+                phi_t = phi_t + V[k].scale(U[k, 0])
+                q = q + AV[k].scale(U[k, 0])
+            q = q + phi_t.scale(-lam)
+            if U[0, 0] < 0:
+                phi_t = phi_t.scale(-1.0)
+                q = q.scale(-1.0)
+        qnorm = q.norm()
+        converged = (qnorm < errgoal and abs(lam - last_lambda) < errgoal) or qnorm < max(approx0, errgoal * 1e-3)
+        last_lambda = lam
+        if qnorm < 1e-20 or (converged and ii >= miniter) or ii == actual_maxiter:
+            break
+        # Gram-Schmidt, one pass
+        npass = 1
+        pass_ = 1
+        tot_pass = 0
+        done = False
+        while pass_ <= npass:
+            tot_pass += 1
+            Vq = [dot(V[k], q) for k in range(ni)]
+            for k in range(ni):
+                q = q + V[k].scale(-Vq[k])
+            qnrm = q.norm()
+            if qnrm < 1e-10:
+                if rng is None:
+                    rng = np.random.default_rng(0)
+                q = V[ni - 1].copy()
+                for c in q.blocks:
+                    q.blocks[c] = np.asfortranarray(rng.random(q.blocks[c].shape))
+                qnrm = q.norm()
+                pass_ -= 1
+                if ni >= maxsize or tot_pass > npass * 3:
+                    done = True
+                    break
+            q = q.scale(1.0 / qnrm)
+            pass_ += 1
+        if done:
+            break
+        V[ni] = q
+        AV[ni] = A.product(V[ni])
+        for k in range(ni + 1):
+            M[k, ni] = dot(V[k], AV[ni])
+            M[ni, k] = M[k, ni]
+    if actual_maxiter == 0 or U is None:
+        return lam, (phi_t if ii > 0 else V[0])
+    return lam, phi_t
+
+
+class LocalMPO:
+    """Cached left/right environments; PH[k] for k<b holds sites 1..k, for
+    k>b+1 holds sites k..N (1-based)."""
+
+    def __init__(self, W):
+        self.W = W
+        self.N = len(W)
+        self.PH = [None] * (self.N + 2)
+        self.LHlim = 0
+        self.RHlim = self.N + 1
+
+    def makeL(self, psi, k):
+        while self.LHlim < k:
+            ll = self.LHlim
+            A = psi[ll]  # site ll+1
+            E = A if self.PH[ll] is None else contract(self.PH[ll], A)
+            E = contract(E, self.W[ll])
+            E = contract(E, A.dag().prime())
+            self.PH[ll + 1] = E
+            self.LHlim = ll + 1
+
+    def makeR(self, psi, k):
+        while self.RHlim > k:
+            rl = self.RHlim
+            A = psi[rl - 2]  # site rl-1
+            E = A if self.PH[rl] is None else contract(self.PH[rl], A)
+            E = contract(E, self.W[rl - 2])
+            E = contract(E, A.dag().prime())
+            self.PH[rl - 1] = E
+            self.RHlim = rl - 1
+
+    def position(self, b, psi):
+        self.makeL(psi, b - 1)
+        self.makeR(psi, b + 2)
+        self.LHlim = b - 1
+        self.RHlim = b + 2
+        L = self.PH[b - 1] if b - 1 >= 1 else None
+        R = self.PH[b + 2] if b + 2 <= self.N else None
+        return LocalOp(self.W[b - 1], self.W[b], L, R)
+
+
+def sweep_bonds(N):
+    """(b, half-sweep) sequence of sweepnext: b=1..N-1 then N-1..1."""
+    out = [(b, 1) for b in range(1, N)]
+    out += [(b, 2) for b in range(N - 1, 0, -1)]
+    return out
+
+
+def dmrg(W, psi, sweeps, record=None, usesvd=None):
+    """sweeps: list of dicts {maxdim, mindim, cutoff, niter}. psi: list of
+    site tensors (modified copy returned). Returns (energy, psi, records)."""
+    psi = list(psi)
+    N = len(psi)
+    PH = LocalMPO(W)
+    energy = np.nan
+    recs = []
+    for sw, s in enumerate(sweeps, start=1):
+        for b, ha in sweep_bonds(N):
+            op = PH.position(b, psi)
+            phi = contract(psi[b - 1], psi[b])
+            energy, phi = davidson(op, phi, maxiter=s["niter"])
+            svd_route = usesvd if usesvd is not None else (s["cutoff"] < 1e-12)
+            if svd_route:
+                Uinds = [I for I in psi[b - 1].inds if psi[b].find(I) < 0]
+                A, B, probs, te = svd_split(phi, Uinds, s["maxdim"], s["mindim"], s["cutoff"],
+                                            fromleft=(ha == 1))
+            else:
+                A, B, probs, te = denmat_decomp(phi, psi[b - 1], psi[b], ha == 1, s["maxdim"], s["mindim"],
+                                                s["cutoff"])
+            psi[b - 1], psi[b] = A, B
+            link = [I for I in A.inds if B.find(I) >= 0][0]
+            recs.append((sw, ha, b, energy, te, link.dim))
+            if record is not None:
+                record(sw, ha, b, energy, te, link)
+    return energy, psi, recs

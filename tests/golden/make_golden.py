@@ -1,0 +1,30 @@
+"""Regenerates the golden fixtures in this folder from the ITensor C++
+reference itself.
+
+Builds the reference library from its own sources (oracle/Makefile.ref, which
+reads them in place under REF, default /root/reference) together with the
+fixture generator oracle/ref_golden.cc, then runs it with one OpenMP thread:
+
+    python tests/golden/make_golden.py [REF]
+
+Needs g++ and the BLAS/LAPACK bundled with scipy. The generator fills every
+input from a seeded splitmix64 stream and writes inputs and reference outputs
+side by side, so the fixtures are self-contained.
+"""
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    subprocess.check_call(["make", "-f", "oracle/Makefile.ref", "-j8", "REF=" + ref], cwd=ROOT)
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    subprocess.check_call([os.path.join(ROOT, "oracle/_ref/ref_golden"), os.path.join(ROOT, "tests/golden"), "all"],
+                          cwd=ROOT, env=env)
+
+
+if __name__ == "__main__":
+    main()
