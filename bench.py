@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 device path for ITensor's two-site DMRG inner loop.
+
+Workload (one "step"): the isolated effective-Hamiltonian apply
+H_eff psi = noPrime(((psi L) W1) W2 R) of LocalOp::product
+(itensor/mps/localop.h:324-365) on a U(1) block-sparse bond of dimension
+m = 1024 split over 31 Sz sectors with Gaussian sizes (sigma = 6 sectors),
+local dimension 2, Heisenberg MPO (bond dimension 5); psi, L, R hold N(0,1)
+FP64 entries from a fixed seed (synthetic data of the stated shape).
+
+Metric: H_eff TFLOP/s = algorithmic FLOPs (sum over matched block pairs of
+2 M N K, FP64-equivalent) per second. The headline form is the split
+precision (FP64 operands as exact BF16 integer slices on the tensor pipe),
+whose result is checked against the plain FP64 path in the same run; the
+plain FP64 path and the DMRG sweep time of the N=20 Heisenberg chain
+(5 sweeps, maxdim 10..200, cutoff 1e-10, niter 2) are reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M_BOND, K_SECT, SIGMA, SEED = 1024, 15, 6.0, 20241204
+METRIC = "H_eff TFLOP/s (isolated apply, m=1024, 31 Sz sectors)"
+UNIT = "TFLOP/s"
+CONFIG = {"workload": "isolated H_eff apply: U(1) block-sparse L(m x 5 x m) W W R psi, m=1024 over 31 Sz "
+                      "sectors (Gaussian sizes, sigma=6), d=2, Heisenberg MPO k=5, FP64 N(0,1) entries",
+          "m": M_BOND, "sectors": 2 * K_SECT + 1, "d": 2, "mpo_bond_dim": 5, "seed": SEED,
+          "l2": "flushed between timed steps (256 MiB write)"}
+HEIS20_SWEEPS = [dict(maxdim=d, mindim=1, cutoff=1e-10, niter=2) for d in (10, 20, 100, 100, 200)]
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- CPU oracle (reference arm / baseline)
+def _oracle_setup():
+    import numpy as np
+    from itensor_gb300 import workloads
+    from oracle.blocksparse import BSTensor, Index, QN
+    wl = workloads.heff_workload(M_BOND, K_SECT, SIGMA, SEED)
+
+    def conv(t):
+        inds = [Index([(QN(("Sz", q, 1)), d) for q, d in zip(I["qn"], I["dims"])], dir=I["dir"], id=I["id"],
+                      plev=I["plev"]) for I in t["inds"]]
+        T = BSTensor(inds)
+        off = 0
+        for c in t["coords"]:
+            c = tuple(int(x) for x in c)
+            shp = T.block_shape(c)
+            n = int(np.prod(shp))
+            T.blocks[c] = np.reshape(t["data"][off:off + n], shp, order="F").copy(order="F")
+            off += n
+        return T
+
+    return {k: conv(wl[k]) for k in ("psi", "L", "W1", "W2", "R")}
+
+
+def _oracle_apply_loop(n_applies):
+    """Worker: n applies of the oracle's LocalOp::product; returns seconds."""
+    from oracle.dmrg import LocalOp
+    t = _oracle_setup()
+    op = LocalOp(t["W1"], t["W2"], t["L"], t["R"])
+    op.product(t["psi"])  # warm
+    t0 = time.perf_counter()
+    for _ in range(n_applies):
+        op.product(t["psi"])
+    return time.perf_counter() - t0
+
+
+def _single_thread_env():
+    env = dict(os.environ)
+    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        env[k] = "1"
+    return env
+
+
+def cpu_baseline(flops_per_apply, budget_s=15.0):
+    """Oracle apply timed on one host core in a subprocess (bounded sample)."""
+    code = ("import sys,json;sys.path.insert(0,%r);import bench;"
+            "t1=bench._oracle_apply_loop(1);n=max(1,int(%f/max(t1,1e-3)));"
+            "t=bench._oracle_apply_loop(n);print(json.dumps({'n':n,'sec':t}))" % (ROOT, budget_s / 2))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=_single_thread_env(),
+                         timeout=600)
+    if out.returncode != 0:
+        return {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": "failed: " + out.stderr[-300:]}
+    r = json.loads(out.stdout.strip().splitlines()[-1])
+    per = r["sec"] / r["n"]
+    return {"value": flops_per_apply / per / 1e12, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d applies of the numpy oracle (LocalOp::product restatement) on the same input, "
+                      "1 thread, %.1f ms/apply" % (r["n"], per * 1e3)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[k] = "1"
+    cores = os.cpu_count() or 1
+    flops = _oracle_flops()
+    ctxm = mp.get_context("spawn")
+    with ctxm.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_oracle_apply_loop, [1] * cores)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            pool.map(_oracle_apply_loop, [1] * cores)
+        el = time.perf_counter() - t0
+    # each step: `cores` independent applies in parallel
+    value = flops * cores * args.steps / el / 1e12
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": CONFIG,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "each step: %d parallel single-thread applies of the numpy oracle "
+                                       "(restatement of LocalOp::product; the reference C++ library does not "
+                                       "build on the GPU host)" % cores},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def _oracle_flops():
+    t = _oracle_setup()
+    from oracle.blocksparse import contract
+    total = 0.0
+    # algorithmic flops of the four contractions: sum over matched pairs of 2 M N K
+    p = t["psi"]
+    for B in (t["L"], t["W1"], t["W2"], t["R"]):
+        total += _pair_flops(p, B)
+        p = contract(p, B)
+    return total
+
+
+def _pair_flops(A, B):
+    import numpy as np
+    AtoB = {}
+    for i, I in enumerate(A.inds):
+        for j, J in enumerate(B.inds):
+            if I.same(J):
+                AtoB[i] = j
+                break
+    f = 0.0
+    for ca, ba in A.blocks.items():
+        for cb, bb in B.blocks.items():
+            if all(ca[i] == cb[j] for i, j in AtoB.items()):
+                K = int(np.prod([ba.shape[i] for i in AtoB])) if AtoB else 1
+                f += 2.0 * (ba.size // K) * (bb.size // K) * K
+    return f
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- device arm
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--slices", type=int, default=6)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-dmrg", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+
+    import numpy as np
+    import torch
+    import itensor_gb300 as itg
+    from itensor_gb300 import workloads
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_
+        dist_.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = dist_
+    torch.cuda.set_device(local)
+    ctx = itg.Context(local)
+    ext = torch.cuda.ExternalStream(ctx.stream)
+    wl = workloads.heff_workload(M_BOND, K_SECT, SIGMA, SEED)
+    dev = {k: workloads.to_device(ctx, wl[k]) for k in ("psi", "L", "W1", "W2", "R")}
+    L, W1, W2, R, psi = dev["L"], dev["W1"], dev["W2"], dev["R"], dev["psi"]
+
+    # correctness gate: split form vs plain FP64 on this input
+    ref64 = ctx.heff_apply(L, W1, W2, R, psi, precision=itg.PREC_F64).numpy()
+    ctx.set_precision(itg.PREC_OZAKI_BF16, args.slices)
+    oz = ctx.heff_apply(L, W1, W2, R, psi, precision=itg.PREC_OZAKI_BF16).numpy()
+    rel = float(np.max(np.abs(oz - ref64)) / np.max(np.abs(ref64)))
+
+    # algorithmic flops per apply (from the plans) and the dominant kernel
+    ctx.profile_begin()
+    ctx.heff_apply(L, W1, W2, R, psi, precision=itg.PREC_F64)
+    prof = ctx.profile_end()
+    flops_apply = sum(f for _, f, _ in prof)
+    dom = max(range(len(prof)), key=lambda i: prof[i][1])  # biggest contraction (psi * L step)
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(prec, steps, warmup, profile=False):
+        for _ in range(warmup):
+            ctx.heff_apply(L, W1, W2, R, psi, precision=prec)
+        ctx.sync()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        tot = 0.0
+        launches0 = ctx.stats()["kernel_launches"]
+        if profile:
+            ctx.profile_begin()
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            ctx.heff_apply(L, W1, W2, R, psi, precision=prec)
+            e1.record(ext)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        pr = ctx.profile_end() if profile else []
+        launches = ctx.stats()["kernel_launches"] - launches0
+        torch.cuda.synchronize()
+        if dist:
+            t = torch.tensor([tot], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t.item())
+        return tot, launches, pr
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_oz, launches, prof_oz = timed(itg.PREC_OZAKI_BF16, args.steps, args.warmup, profile=True)
+    clk = clocks.stop()
+    t_64, _, prof_64 = timed(itg.PREC_F64, max(3, args.steps // 3), 2, profile=True)
+
+    value = flops_apply * args.steps * world / (t_oz / 1e3) / 1e12
+    f64_value = flops_apply * max(3, args.steps // 3) / (t_64 / 1e3) / 1e12
+
+    # roofline of the dominant kernel (psi * L block GEMM), averaged over the timed launches
+    def dom_stats(pr):
+        per = len(prof)
+        ms = [pr[i][0] for i in range(dom, len(pr), per)]
+        return statistics.mean(ms), pr[dom][1], pr[dom][2]
+
+    peaks, peak_src = measured_peaks()
+    dm_ms, dm_flops, dm_kind = dom_stats(prof_oz)
+    achieved = dm_flops / (dm_ms / 1e3) / 1e12
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+                "kernel": "gemm_ozaki_kernel<%d> (psi*L block GEMM)" % args.slices,
+                "note": "achieved = algorithmic FP64-equivalent flops of the launch / its CUDA-event duration; "
+                        "peak = dense BF16 burst of %s; the kernel issues %d BF16 slice products per FP64 "
+                        "product" % ("MEASURED_PEAKS.json" if peak_src == "measured" else "the fallback",
+                                     args.slices * (args.slices + 1) // 2),
+                "slice_tflops": achieved * args.slices * (args.slices + 1) / 2}
+    d64_ms, d64_flops, _ = dom_stats(prof_64)
+
+    # end-to-end through the public API: host psi -> device, apply, result -> host
+    psi_host = np.ascontiguousarray(wl["psi"]["data"])
+    inds = psi.inds
+    coords = wl["psi"]["coords"].reshape(-1)
+    out_n = len(oz)
+    e2e_t = 0.0
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p = ctx.tensor(inds, coords, psi_host)
+        o = ctx.heff_apply(L, W1, W2, R, p, precision=itg.PREC_OZAKI_BF16).numpy()
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_t += dt
+    e2e = {"value": flops_apply * args.steps / e2e_t / 1e12, "unit": UNIT,
+           "h2d_bytes_per_step": int(8 * psi_host.size), "d2h_bytes_per_step": int(8 * out_n),
+           "ms_per_step": e2e_t / args.steps * 1e3, "api": "itg_tensor_create(host data) + itg_heff_apply + "
+                                                             "itg_tensor_read"}
+
+    # DMRG sweep time: N=20 Heisenberg chain (5 sweeps), plain FP64 and split form
+    dmrg = None
+    if not args.no_dmrg and rank == 0:
+        ref_e = None
+        try:
+            with open(os.path.join(ROOT, "tests", "golden", "dmrg.json")) as f:
+                ref_e = [c for c in json.load(f)["cases"] if c["name"] == "heis20"][0]["energy"]
+        except OSError:
+            pass
+        dmrg = {"model": "S=1/2 Heisenberg N=20, Sz QN, Neel start, 5 sweeps maxdim 10,20,100,100,200, "
+                         "cutoff 1e-10, niter 2", "reference_energy": ref_e}
+        for name, prec in (("f64", itg.PREC_F64), ("split", itg.PREC_OZAKI_BF16)):
+            ctx.dmrg(dict(type=0, N=20), HEIS20_SWEEPS, precision=prec)  # warm (plans, pool)
+            t0 = time.perf_counter()
+            r = ctx.dmrg(dict(type=0, N=20), HEIS20_SWEEPS, precision=prec)
+            el = time.perf_counter() - t0
+            dmrg[name] = {"seconds": el, "sweep_seconds": r.sweep_seconds, "energy": r.energy,
+                          "dE": None if ref_e is None else r.energy - ref_e, "heff_applies": r.heff_applies}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(flops_apply)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_oz / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64 (FP64 operands as %d exact BF16 slices, FP32-exact accumulation)" % args.slices,
+                "data": "synthetic (seeded N(0,1) blocks of the stated shape)", "config": CONFIG,
+                "algorithmic_gflop_per_apply": flops_apply / 1e9,
+                "split_vs_f64_max_rel_err": rel,
+                "f64_path": {"value": f64_value, "unit": UNIT, "ms_per_step": t_64 / max(3, args.steps // 3),
+                             "dominant_kernel_ms": d64_ms,
+                             "dominant_kernel_tflops": d64_flops / (d64_ms / 1e3) / 1e12},
+                "speedup_split_over_f64": value / f64_value,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk, "dmrg_heis20": dmrg}
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

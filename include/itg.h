@@ -1,0 +1,192 @@
+/*
+ * itg.h -- C-ABI of the GB300 (sm_103a) device path for ITensor's two-site DMRG
+ * inner loop: block-sparse QN contraction, effective-Hamiltonian apply,
+ * Davidson, density-matrix bond split and the DMRG sweep driver.
+ *
+ * Conventions (shared with ITensor's QDense storage, itensor/itdata/qdense.h:34-187):
+ *   - a block is named by one sector number per index (0-based); blocks are
+ *     dense, column-major (first index fastest), ordered by reversed-
+ *     lexicographic coordinates and packed back to back;
+ *   - an index is (id, prime level, arrow, QN sectors); two indices contract
+ *     when id and prime level agree;
+ *   - a QN holds 4 integer slots; slot k is reduced modulo qn_mod[k] when
+ *     |qn_mod[k]| > 1 (Z_n), is a plain integer when |qn_mod[k]| == 1, and is
+ *     unused when qn_mod[k] == 0. Negative moduli mark fermionic U(1) numbers
+ *     (bookkeeping only, as in itensor/qn.h:36-60).
+ *
+ * Every function returns an int status (ITG_OK = 0); no C++ exception crosses
+ * the boundary. itg_last_error() gives the message of the last failure on a
+ * context. A context owns one CUDA stream; calls on one context must not be
+ * made from two host threads at once. Device pointers passed in are never
+ * freed by the library.
+ */
+#ifndef ITG_H
+#define ITG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    ITG_OK = 0,
+    ITG_ERR_ARG = 1,       /* malformed arguments or block metadata */
+    ITG_ERR_CUDA = 2,      /* CUDA runtime error */
+    ITG_ERR_OOM = 3,       /* device allocation failed */
+    ITG_ERR_NOCONV = 4,    /* eigensolver hit its sweep cap */
+    ITG_ERR_TIMEOUT = 5,   /* a bounded device-side wait gave up */
+    ITG_ERR_INTERNAL = 6,
+    ITG_ERR_RANGE = 7      /* size beyond a stated maximum */
+};
+
+enum {
+    ITG_PREC_F64 = 0,        /* plain FP64 -- the drop-in path */
+    ITG_PREC_OZAKI_BF16 = 1  /* FP64 operands as exact BF16 integer slices, FP32-exact accumulation */
+};
+
+typedef struct itg_ctx itg_ctx;
+typedef struct itg_tensor itg_tensor;
+typedef struct itg_plan itg_plan;
+typedef struct itg_dmrg_result itg_dmrg_result;
+
+typedef struct {
+    uint64_t id;
+    int32_t plev;
+    int32_t dir;            /* +1 Out, -1 In */
+    int32_t nsect;
+    const int32_t* qn;      /* nsect * 4 values */
+    const int32_t* qn_mod;  /* 4 moduli */
+    const int32_t* dims;    /* nsect sector sizes */
+} itg_index_desc;
+
+/* ---------------------------------------------------------------- context */
+int itg_create(int device, itg_ctx** out);
+void itg_destroy(itg_ctx* ctx);
+const char* itg_last_error(itg_ctx* ctx);
+int itg_synchronize(itg_ctx* ctx);
+/* Default arithmetic of the block GEMMs; ozaki_slices in 3..6. */
+int itg_set_precision(itg_ctx* ctx, int mode, int ozaki_slices);
+int itg_stats(itg_ctx* ctx, uint64_t* kernel_launches, double* gemm_flops, uint64_t* plans_built,
+              uint64_t* plan_hits);
+int itg_reset_stats(itg_ctx* ctx);
+/* The CUDA stream (cudaStream_t) all work of this context is ordered on. */
+void* itg_stream(itg_ctx* ctx);
+/* Per-launch timing of the block-GEMM launches (CUDA events on the context
+ * stream) between begin and end: n launches (capacity *n on input), their
+ * durations in ms, algorithmic flops (sum of 2MNK) and arithmetic kind
+ * (0 FP64, 1 Ozaki BF16). */
+int itg_profile_begin(itg_ctx* ctx);
+int itg_profile_end(itg_ctx* ctx, int32_t* n, float* ms, double* flops, int32_t* kind);
+
+/* ---------------------------------------------------------------- tensors
+ * Replaces QDense<Real> storage (itensor/itdata/qdense.h:34-60): `coords` are
+ * the blocks in storage order (nblocks x rank), data packed in that order.
+ * data_is_device != 0: `data` is a device pointer (copied on the context stream). */
+int itg_tensor_create(itg_ctx* ctx, int32_t rank, const itg_index_desc* inds, int32_t nblocks, const int32_t* coords,
+                      const double* data, int data_is_device, itg_tensor** out);
+void itg_tensor_free(itg_tensor* t);
+int itg_tensor_layout(const itg_tensor* t, int32_t* rank, int32_t* nblocks, int64_t* size);
+/* Index k: nsect first (call with qn/dims NULL), then the sector data. */
+int itg_tensor_index(const itg_tensor* t, int32_t k, uint64_t* id, int32_t* plev, int32_t* dir, int32_t* nsect,
+                     int32_t* qn, int32_t* qn_mod, int32_t* dims);
+int itg_tensor_blocks(const itg_tensor* t, int32_t* coords, int64_t* offsets);
+int itg_tensor_read(itg_ctx* ctx, const itg_tensor* t, double* host);
+double* itg_tensor_device_ptr(const itg_tensor* t);
+/* Value of a rank-0 tensor (a full contraction). */
+int itg_tensor_scalar(const itg_tensor* t, double* value);
+
+/* ---------------------------------------------------------------- contraction
+ * ITensor operator* for QN tensors: doTask(Contract,QDense,QDense),
+ * itensor/itdata/qdense.cc:671-743 (block matching getContractedOffsets,
+ * itensor/itdata/qutil.h:93-242). Output indices: A's uncontracted then B's
+ * (contractIS, itensor/indexset_impl.h:77-127); output blocks: exactly those
+ * produced by a matching block pair, sorted, packed. */
+int itg_contract(itg_ctx* ctx, const itg_tensor* A, const itg_tensor* B, int precision, itg_tensor** C);
+
+/* Raw boundary for a QDense caller that keeps its own storage: layouts as
+ * sector sizes + block coordinates, contraction labels in the reference's
+ * Lind/Rind convention (negative = contracted, equal negative labels pair up;
+ * computeLabels itensor/tensor/contract.h:155-216). Data pointers are device
+ * memory laid out as the layouts say. */
+typedef struct {
+    int32_t rank;
+    const int32_t* nsect;      /* rank */
+    const int32_t* sect_dims;  /* sum(nsect) sector sizes, index by index */
+    int32_t nblocks;
+    const int32_t* coords;     /* nblocks x rank, storage order */
+} itg_layout_desc;
+int itg_contract_plan(itg_ctx* ctx, const itg_layout_desc* A, const int32_t* labelsA, const itg_layout_desc* B,
+                      const int32_t* labelsB, itg_plan** plan);
+int itg_plan_output(const itg_plan* plan, int32_t* rank, int32_t* nblocks, int64_t* size);
+int itg_plan_output_blocks(const itg_plan* plan, int32_t* coords, int64_t* offsets);
+int itg_plan_flops(const itg_plan* plan, double* flops);
+int itg_contract_exec(itg_ctx* ctx, const itg_plan* plan, const double* A, const double* B, double* C, int precision);
+void itg_plan_free(itg_plan* plan);
+
+/* ---------------------------------------------------------------- H_eff
+ * LocalOp::product, itensor/mps/localop.h:324-365: out = noPrime(((phi*L)*W1)*W2*R)
+ * (L or R may be NULL at the chain ends). The output has the block structure
+ * the reference produces. */
+int itg_heff_apply(itg_ctx* ctx, const itg_tensor* L, const itg_tensor* W1, const itg_tensor* W2, const itg_tensor* R,
+                   const itg_tensor* phi, int precision, itg_tensor** out);
+
+/* davidson (block size 1), itensor/iterativesolvers.h:99-451. Returns the
+ * lowest Ritz value and the normalised Ritz vector (on every block of phi's
+ * divergence). */
+int itg_davidson(itg_ctx* ctx, const itg_tensor* L, const itg_tensor* W1, const itg_tensor* W2, const itg_tensor* R,
+                 const itg_tensor* phi, int32_t maxiter, double errgoal, int precision, double* energy,
+                 itg_tensor** phi_out);
+
+/* ---------------------------------------------------------------- bond split
+ * denmatDecomp, itensor/decomp.h:316-418, with diag_hermitian's QN branch
+ * (itensor/hermitian.cc:180-426) and truncate (itensor/decomp.cc:305-463).
+ * A and B give the index split (their data is not read). eigs receives the
+ * kept density-matrix eigenvalues (capacity *neigs on input, count on output). */
+int itg_denmat_decomp(itg_ctx* ctx, const itg_tensor* AA, const itg_tensor* A, const itg_tensor* B, int fromleft,
+                      double cutoff, int32_t maxdim, int32_t mindim, int respect_degenerate, int normalize,
+                      int precision, itg_tensor** A_out, itg_tensor** B_out, double* truncerr, double* eigs,
+                      int32_t* neigs);
+
+/* truncate, itensor/decomp.cc:305-463 (host function, same decisions and
+ * values as the reference). P sorted descending; Pout capacity n. */
+int itg_truncate(const double* P, int32_t n, int32_t maxdim, int32_t mindim, double cutoff, int absolute_cutoff,
+                 int rel_cutoff, int respect_degenerate, double* Pout, int32_t* m, double* truncerr,
+                 double* docut_lower, double* docut_upper, int32_t* ndegen);
+
+/* ---------------------------------------------------------------- DMRG driver
+ * dmrg(H, psi0, sweeps) with DMRGWorker (itensor/mps/dmrg.h:336-467). The MPO
+ * and the initial product state are built from the model description:
+ * type 0: S=1/2 chain, H = sum Jz SzSz + J/2 (S+S- + S-S+) (+ J2 on next neighbours), Sz QN, Neel start;
+ * type 1: transverse-field Ising, H = -sum SxSx - h sum Sz, parity QN, all-up start;
+ * type 2: Hubbard on an Lx x Ly square lattice snaked column by column,
+ *         H = -t sum hops + U sum n_up n_dn, (Nf, Sz) QN, Neel start at half filling. */
+typedef struct {
+    int32_t type;
+    int32_t N;
+    double J, Jz, J2, h, t, U;
+    int32_t Lx, Ly, yperiodic;
+} itg_model_desc;
+
+typedef struct {
+    int32_t maxdim, mindim;
+    double cutoff;
+    int32_t niter;
+    double noise; /* must be 0 */
+} itg_sweep_desc;
+
+int itg_dmrg_run(itg_ctx* ctx, const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps,
+                 int precision, itg_dmrg_result** out);
+int itg_dmrg_energy(const itg_dmrg_result* r, double* energy);
+int itg_dmrg_nbonds(const itg_dmrg_result* r, int32_t* nbonds);
+int itg_dmrg_bonds(const itg_dmrg_result* r, int32_t* sweep, int32_t* halfsweep, int32_t* bond, double* energy,
+                   double* truncerr, int32_t* dim);
+/* Final link index b (1..N-1): sectors (4 QN values each) and sizes. */
+int itg_dmrg_link(const itg_dmrg_result* r, int32_t b, int32_t* dir, int32_t* nsect, int32_t* qn, int32_t* dims);
+int itg_dmrg_timing(const itg_dmrg_result* r, int32_t* nsweeps, double* sweep_seconds, int32_t* heff_applies);
+void itg_dmrg_free(itg_dmrg_result* r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

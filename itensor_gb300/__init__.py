@@ -1,0 +1,436 @@
+"""GB300 (sm_103a) device path for ITensor's two-site DMRG inner loop.
+
+Python mirror of the C-ABI in include/itg.h, loaded from the in-tree
+libitg.so (built by itensor_gb300.build). The names follow ITensor's
+interface: contraction (``A * B``), ``heff_apply`` (LocalOp::product),
+``davidson``, ``denmat_decomp``, ``truncate`` and ``dmrg``.
+
+There is no CPU fallback: importing works without a GPU, but creating a
+Context needs the built library and a CUDA device, and fails loudly otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libitg.so")
+
+PREC_F64 = 0
+PREC_OZAKI_BF16 = 1
+
+_i32p = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+_f64p = C.POINTER(C.c_double)
+_u64p = C.POINTER(C.c_uint64)
+
+
+class IndexDesc(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("plev", C.c_int32), ("dir", C.c_int32), ("nsect", C.c_int32),
+                ("qn", _i32p), ("qn_mod", _i32p), ("dims", _i32p)]
+
+
+class LayoutDesc(C.Structure):
+    _fields_ = [("rank", C.c_int32), ("nsect", _i32p), ("sect_dims", _i32p), ("nblocks", C.c_int32),
+                ("coords", _i32p)]
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("N", C.c_int32), ("J", C.c_double), ("Jz", C.c_double), ("J2", C.c_double),
+                ("h", C.c_double), ("t", C.c_double), ("U", C.c_double), ("Lx", C.c_int32), ("Ly", C.c_int32),
+                ("yperiodic", C.c_int32)]
+
+
+class SweepDesc(C.Structure):
+    _fields_ = [("maxdim", C.c_int32), ("mindim", C.c_int32), ("cutoff", C.c_double), ("niter", C.c_int32),
+                ("noise", C.c_double)]
+
+
+# every exported symbol with its C signature (restype, argtypes)
+SIGNATURES = {
+    "itg_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "itg_destroy": (None, [C.c_void_p]),
+    "itg_last_error": (C.c_char_p, [C.c_void_p]),
+    "itg_synchronize": (C.c_int, [C.c_void_p]),
+    "itg_set_precision": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "itg_stats": (C.c_int, [C.c_void_p, _u64p, _f64p, _u64p, _u64p]),
+    "itg_reset_stats": (C.c_int, [C.c_void_p]),
+    "itg_stream": (C.c_void_p, [C.c_void_p]),
+    "itg_profile_begin": (C.c_int, [C.c_void_p]),
+    "itg_profile_end": (C.c_int, [C.c_void_p, _i32p, C.POINTER(C.c_float), _f64p, _i32p]),
+    "itg_tensor_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(IndexDesc), C.c_int32, _i32p, C.c_void_p,
+                                    C.c_int, C.POINTER(C.c_void_p)]),
+    "itg_tensor_free": (None, [C.c_void_p]),
+    "itg_tensor_layout": (C.c_int, [C.c_void_p, _i32p, _i32p, _i64p]),
+    "itg_tensor_index": (C.c_int, [C.c_void_p, C.c_int32, _u64p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p]),
+    "itg_tensor_blocks": (C.c_int, [C.c_void_p, _i32p, _i64p]),
+    "itg_tensor_read": (C.c_int, [C.c_void_p, C.c_void_p, _f64p]),
+    "itg_tensor_device_ptr": (C.c_void_p, [C.c_void_p]),
+    "itg_tensor_scalar": (C.c_int, [C.c_void_p, _f64p]),
+    "itg_contract": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "itg_contract_plan": (C.c_int, [C.c_void_p, C.POINTER(LayoutDesc), _i32p, C.POINTER(LayoutDesc), _i32p,
+                                    C.POINTER(C.c_void_p)]),
+    "itg_plan_output": (C.c_int, [C.c_void_p, _i32p, _i32p, _i64p]),
+    "itg_plan_output_blocks": (C.c_int, [C.c_void_p, _i32p, _i64p]),
+    "itg_plan_flops": (C.c_int, [C.c_void_p, _f64p]),
+    "itg_contract_exec": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "itg_plan_free": (None, [C.c_void_p]),
+    "itg_heff_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                 C.POINTER(C.c_void_p)]),
+    "itg_davidson": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                               C.c_double, C.c_int, _f64p, C.POINTER(C.c_void_p)]),
+    "itg_denmat_decomp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int32,
+                                    C.c_int32, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p),
+                                    C.POINTER(C.c_void_p), _f64p, _f64p, _i32p]),
+    "itg_truncate": (C.c_int, [_f64p, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int, C.c_int, C.c_int, _f64p,
+                               _i32p, _f64p, _f64p, _f64p, _i32p]),
+    "itg_dmrg_run": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.POINTER(SweepDesc), C.c_int32, C.c_int,
+                               C.POINTER(C.c_void_p)]),
+    "itg_dmrg_energy": (C.c_int, [C.c_void_p, _f64p]),
+    "itg_dmrg_nbonds": (C.c_int, [C.c_void_p, _i32p]),
+    "itg_dmrg_bonds": (C.c_int, [C.c_void_p, _i32p, _i32p, _i32p, _f64p, _f64p, _i32p]),
+    "itg_dmrg_link": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p, _i32p, _i32p]),
+    "itg_dmrg_timing": (C.c_int, [C.c_void_p, _i32p, _f64p, _i32p]),
+    "itg_dmrg_free": (None, [C.c_void_p]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded C-ABI library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("itensor_gb300: %s is missing; run itensor_gb300.build.build() first" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class ITGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("itg error %d: %s" % (code, msg))
+        self.code = code
+
+
+def _p(arr, typ):
+    return arr.ctypes.data_as(C.POINTER(typ))
+
+
+class Index:
+    """QN index: id, prime level, arrow (+1 Out, -1 In), sectors with 4-slot QNs."""
+
+    def __init__(self, id, plev, dir, qns, dims, mods):
+        self.id = int(id)
+        self.plev = int(plev)
+        self.dir = int(dir)
+        self.qns = np.ascontiguousarray(np.asarray(qns, dtype=np.int32).reshape(-1, 4))
+        self.dims = np.ascontiguousarray(np.asarray(dims, dtype=np.int32))
+        self.mods = np.ascontiguousarray(np.asarray(mods, dtype=np.int32).reshape(4))
+
+    def desc(self):
+        return IndexDesc(self.id, self.plev, self.dir, len(self.dims), _p(self.qns, C.c_int32),
+                         _p(self.mods, C.c_int32), _p(self.dims, C.c_int32))
+
+    def same(self, o):
+        return self.id == o.id and self.plev == o.plev
+
+    def prime(self, inc=1):
+        return Index(self.id, self.plev + inc, self.dir, self.qns, self.dims, self.mods)
+
+    def dag(self):
+        return Index(self.id, self.plev, -self.dir, self.qns, self.dims, self.mods)
+
+    @property
+    def dim(self):
+        return int(self.dims.sum())
+
+
+class Tensor:
+    """Handle to a block-sparse tensor whose blocks live in device memory."""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.h = C.c_void_p(handle) if not isinstance(handle, C.c_void_p) else handle
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.itg_tensor_free(self.h)
+            self.h = C.c_void_p(None)
+
+    def __mul__(self, other):
+        return self.ctx.contract(self, other)
+
+    def layout(self):
+        r, nb, sz = C.c_int32(), C.c_int32(), C.c_int64()
+        self.ctx._ok(lib().itg_tensor_layout(self.h, C.byref(r), C.byref(nb), C.byref(sz)), self.ctx.h)
+        return r.value, nb.value, sz.value
+
+    @property
+    def inds(self):
+        r, _, _ = self.layout()
+        out = []
+        for k in range(r):
+            id_, pl, dr, ns = C.c_uint64(), C.c_int32(), C.c_int32(), C.c_int32()
+            self.ctx._ok(lib().itg_tensor_index(self.h, k, C.byref(id_), C.byref(pl), C.byref(dr), C.byref(ns),
+                                                None, None, None), None)
+            qn = np.zeros(ns.value * 4, np.int32)
+            dims = np.zeros(ns.value, np.int32)
+            mods = np.zeros(4, np.int32)
+            self.ctx._ok(lib().itg_tensor_index(self.h, k, None, None, None, None, _p(qn, C.c_int32),
+                                                _p(mods, C.c_int32), _p(dims, C.c_int32)), None)
+            out.append(Index(id_.value, pl.value, dr.value, qn, dims, mods))
+        return out
+
+    def blocks(self):
+        r, nb, _ = self.layout()
+        coords = np.zeros(max(1, nb * r), np.int32)
+        offs = np.zeros(max(1, nb), np.int64)
+        self.ctx._ok(lib().itg_tensor_blocks(self.h, _p(coords, C.c_int32), _p(offs, C.c_int64)), None)
+        return coords[:nb * r].reshape(nb, r), offs[:nb]
+
+    def numpy(self):
+        _, _, sz = self.layout()
+        out = np.zeros(max(sz, 1))
+        self.ctx._ok(lib().itg_tensor_read(self.ctx.h, self.h, _p(out, C.c_double)), self.ctx.h)
+        return out[:sz]
+
+    def scalar(self):
+        v = C.c_double()
+        self.ctx._ok(lib().itg_tensor_scalar(self.h, C.byref(v)), None)
+        return v.value
+
+    def device_ptr(self):
+        return lib().itg_tensor_device_ptr(self.h)
+
+
+class Plan:
+    def __init__(self, ctx, handle):
+        self.ctx, self.h = ctx, handle
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.itg_plan_free(self.h)
+            self.h = C.c_void_p(None)
+
+    def output(self):
+        r, nb, sz = C.c_int32(), C.c_int32(), C.c_int64()
+        self.ctx._ok(lib().itg_plan_output(self.h, C.byref(r), C.byref(nb), C.byref(sz)), None)
+        coords = np.zeros(max(1, r.value * nb.value), np.int32)
+        offs = np.zeros(max(1, nb.value), np.int64)
+        self.ctx._ok(lib().itg_plan_output_blocks(self.h, _p(coords, C.c_int32), _p(offs, C.c_int64)), None)
+        return coords[:r.value * nb.value].reshape(nb.value, r.value), offs[:nb.value], sz.value
+
+    def flops(self):
+        f = C.c_double()
+        self.ctx._ok(lib().itg_plan_flops(self.h, C.byref(f)), None)
+        return f.value
+
+
+class DmrgResult:
+    def __init__(self, energy, bonds, links, sweep_seconds, heff_applies):
+        self.energy = energy
+        self.bonds = bonds            # list of (sweep, halfsweep, bond, energy, truncerr, dim)
+        self.links = links            # list of (dir, qns (nsect x 4), dims)
+        self.sweep_seconds = sweep_seconds
+        self.heff_applies = heff_applies
+
+
+class Context:
+    """One GPU, one CUDA stream, a plan cache and a memory pool."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        rc = lib().itg_create(device, C.byref(h))
+        if rc != 0:
+            raise ITGError(rc, lib().itg_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().itg_destroy(self.h)
+            self.h = C.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc, hctx):
+        if rc != 0:
+            msg = lib().itg_last_error(hctx if hctx is not None else None)
+            raise ITGError(rc, msg.decode() if msg else "")
+
+    @property
+    def stream(self):
+        return lib().itg_stream(self.h)
+
+    def sync(self):
+        self._ok(lib().itg_synchronize(self.h), self.h)
+
+    def set_precision(self, mode, slices=6):
+        self._ok(lib().itg_set_precision(self.h, mode, slices), self.h)
+
+    def stats(self):
+        a, f, b, c = C.c_uint64(), C.c_double(), C.c_uint64(), C.c_uint64()
+        self._ok(lib().itg_stats(self.h, C.byref(a), C.byref(f), C.byref(b), C.byref(c)), self.h)
+        return {"kernel_launches": a.value, "gemm_flops": f.value, "plans_built": b.value, "plan_hits": c.value}
+
+    def profile_begin(self):
+        self._ok(lib().itg_profile_begin(self.h), self.h)
+
+    def profile_end(self, cap=4096):
+        """[(ms, flops, kind)] of every block-GEMM launch since profile_begin."""
+        n = C.c_int32(cap)
+        ms = np.zeros(cap, np.float32)
+        fl = np.zeros(cap)
+        kd = np.zeros(cap, np.int32)
+        self._ok(lib().itg_profile_end(self.h, C.byref(n), _p(ms, C.c_float), _p(fl, C.c_double),
+                                       _p(kd, C.c_int32)), self.h)
+        k = min(n.value, cap)
+        return [(float(ms[i]), float(fl[i]), int(kd[i])) for i in range(k)]
+
+    def reset_stats(self):
+        self._ok(lib().itg_reset_stats(self.h), self.h)
+
+    # ---- tensors
+    def tensor(self, inds, coords, data=None, device_ptr=None):
+        """Block-sparse tensor from indices, block coordinates (storage order)
+        and packed data (host numpy array, or a device pointer)."""
+        descs = (IndexDesc * max(1, len(inds)))(*[I.desc() for I in inds])
+        coords = np.ascontiguousarray(np.asarray(coords, dtype=np.int32).reshape(-1))
+        nb = (len(coords) // len(inds)) if inds else 1
+        out = C.c_void_p()
+        if device_ptr is not None:
+            ptr, is_dev = C.c_void_p(device_ptr), 1
+        elif data is not None:
+            data = np.ascontiguousarray(np.asarray(data, dtype=np.float64))
+            ptr, is_dev = data.ctypes.data_as(C.c_void_p), 0
+        else:
+            ptr, is_dev = None, 0
+        self._ok(lib().itg_tensor_create(self.h, len(inds), descs, nb, _p(coords, C.c_int32) if len(coords) else None,
+                                         ptr, is_dev, C.byref(out)), self.h)
+        return Tensor(self, out)
+
+    # ---- contraction
+    def contract(self, A, B, precision=-1):
+        out = C.c_void_p()
+        self._ok(lib().itg_contract(self.h, A.h, B.h, precision, C.byref(out)), self.h)
+        return Tensor(self, out)
+
+    def plan(self, A_layout, labelsA, B_layout, labelsB):
+        """A_layout/B_layout: (sector dims per index list, coords (nblocks x rank))."""
+        keep = []
+
+        def desc(lay):
+            dims, coords = lay
+            ns = np.array([len(d) for d in dims], np.int32)
+            sd = np.array([x for d in dims for x in d], np.int32)
+            cc = np.ascontiguousarray(np.asarray(coords, np.int32).reshape(-1))
+            keep.extend([ns, sd, cc])
+            return LayoutDesc(len(dims), _p(ns, C.c_int32), _p(sd, C.c_int32), len(cc) // max(1, len(dims)),
+                              _p(cc, C.c_int32))
+
+        la, lb = desc(A_layout), desc(B_layout)
+        LA = np.ascontiguousarray(np.asarray(labelsA, np.int32))
+        LB = np.ascontiguousarray(np.asarray(labelsB, np.int32))
+        out = C.c_void_p()
+        self._ok(lib().itg_contract_plan(self.h, C.byref(la), _p(LA, C.c_int32), C.byref(lb), _p(LB, C.c_int32),
+                                         C.byref(out)), self.h)
+        return Plan(self, out)
+
+    def contract_exec(self, plan, a_ptr, b_ptr, c_ptr, precision=-1):
+        self._ok(lib().itg_contract_exec(self.h, plan.h, C.c_void_p(a_ptr), C.c_void_p(b_ptr), C.c_void_p(c_ptr),
+                                         precision), self.h)
+
+    # ---- DMRG pieces
+    def heff_apply(self, L, W1, W2, R, phi, precision=-1):
+        out = C.c_void_p()
+        self._ok(lib().itg_heff_apply(self.h, L.h if L is not None else None, W1.h, W2.h,
+                                      R.h if R is not None else None, phi.h, precision, C.byref(out)), self.h)
+        return Tensor(self, out)
+
+    def davidson(self, L, W1, W2, R, phi, maxiter=2, errgoal=1e-14, precision=-1):
+        out = C.c_void_p()
+        e = C.c_double()
+        self._ok(lib().itg_davidson(self.h, L.h if L is not None else None, W1.h, W2.h,
+                                    R.h if R is not None else None, phi.h, maxiter, errgoal, precision,
+                                    C.byref(e), C.byref(out)), self.h)
+        return e.value, Tensor(self, out)
+
+    def denmat_decomp(self, AA, A, B, fromleft, cutoff, maxdim, mindim=1, respect_degenerate=True, normalize=True,
+                      precision=-1):
+        ao, bo = C.c_void_p(), C.c_void_p()
+        te = C.c_double()
+        cap = 1 << 16
+        eigs = np.zeros(cap)
+        n = C.c_int32(cap)
+        self._ok(lib().itg_denmat_decomp(self.h, AA.h, A.h, B.h, int(fromleft), cutoff, maxdim, mindim,
+                                         int(respect_degenerate), int(normalize), precision, C.byref(ao),
+                                         C.byref(bo), C.byref(te), _p(eigs, C.c_double), C.byref(n)), self.h)
+        return Tensor(self, ao), Tensor(self, bo), eigs[:n.value].copy(), te.value
+
+    def dmrg(self, model, sweeps, precision=-1):
+        """model: dict(type, N, J, Jz, J2, h, t, U, Lx, Ly, yperiodic); sweeps: list of
+        dict(maxdim, mindim, cutoff, niter)."""
+        md = ModelDesc(int(model.get("type", 0)), int(model.get("N", 0)), float(model.get("J", 1.0)),
+                       float(model.get("Jz", model.get("J", 1.0))), float(model.get("J2", 0.0)),
+                       float(model.get("h", 0.0)), float(model.get("t", 1.0)), float(model.get("U", 0.0)),
+                       int(model.get("Lx", 0)), int(model.get("Ly", 1)), int(model.get("yperiodic", 0)))
+        sw = (SweepDesc * len(sweeps))(*[SweepDesc(int(s["maxdim"]), int(s.get("mindim", 1)), float(s["cutoff"]),
+                                                   int(s.get("niter", 2)), float(s.get("noise", 0.0)))
+                                         for s in sweeps])
+        out = C.c_void_p()
+        self._ok(lib().itg_dmrg_run(self.h, C.byref(md), sw, len(sweeps), precision, C.byref(out)), self.h)
+        try:
+            L = lib()
+            e = C.c_double()
+            L.itg_dmrg_energy(out, C.byref(e))
+            nb = C.c_int32()
+            L.itg_dmrg_nbonds(out, C.byref(nb))
+            n = nb.value
+            sw_, ha, bb, te, dm = (np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32),
+                                   np.zeros(n), np.zeros(n, np.int32))
+            en = np.zeros(n)
+            L.itg_dmrg_bonds(out, _p(sw_, C.c_int32), _p(ha, C.c_int32), _p(bb, C.c_int32), _p(en, C.c_double),
+                             _p(te, C.c_double), _p(dm, C.c_int32))
+            bonds = [(int(sw_[i]), int(ha[i]), int(bb[i]), float(en[i]), float(te[i]), int(dm[i])) for i in range(n)]
+            N = max(b[2] for b in bonds) + 1 if bonds else 0
+            links = []
+            for b in range(1, N):
+                d, ns = C.c_int32(), C.c_int32()
+                L.itg_dmrg_link(out, b, C.byref(d), C.byref(ns), None, None)
+                qn = np.zeros(ns.value * 4, np.int32)
+                dims = np.zeros(ns.value, np.int32)
+                L.itg_dmrg_link(out, b, None, None, _p(qn, C.c_int32), _p(dims, C.c_int32))
+                links.append((d.value, qn.reshape(-1, 4), dims))
+            nsw = C.c_int32()
+            L.itg_dmrg_timing(out, C.byref(nsw), None, None)
+            secs = np.zeros(max(1, nsw.value))
+            ap = C.c_int32()
+            L.itg_dmrg_timing(out, None, _p(secs, C.c_double), C.byref(ap))
+            return DmrgResult(e.value, bonds, links, secs[:nsw.value].tolist(), ap.value)
+        finally:
+            lib().itg_dmrg_free(out)
+
+
+def truncate(P, maxdim, mindim, cutoff, absolute_cutoff=False, rel_cutoff=True, respect_degenerate=False):
+    """truncate (itensor/decomp.cc:305-463): returns (P_kept, truncerr, docut_lower, docut_upper, ndegen)."""
+    P = np.ascontiguousarray(np.asarray(P, np.float64))
+    out = np.zeros(len(P))
+    m, nd = C.c_int32(), C.c_int32()
+    te, lo, up = C.c_double(), C.c_double(), C.c_double()
+    rc = lib().itg_truncate(_p(P, C.c_double), len(P), maxdim, mindim, cutoff, int(absolute_cutoff),
+                            int(rel_cutoff), int(respect_degenerate), _p(out, C.c_double), C.byref(m), C.byref(te),
+                            C.byref(lo), C.byref(up), C.byref(nd))
+    if rc != 0:
+        raise ITGError(rc, lib().itg_last_error(None).decode())
+    return out[:m.value].copy(), te.value, lo.value, up.value, nd.value

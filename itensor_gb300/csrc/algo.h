@@ -1,0 +1,130 @@
+// Host-side algorithms of the two-site DMRG inner loop, driving the device
+// kernels. Each function follows the reference routine named beside it.
+#pragma once
+#include "ops.h"
+#include <map>
+
+namespace itg {
+
+// ---------------------------------------------------------------- tensors
+Tensor upload_tensor(Ctx& ctx, std::shared_ptr<Layout> lay, double const* host);
+std::vector<double> download(Ctx& ctx, Tensor const& t);
+QN tensor_div(Tensor const& t);
+std::vector<Index> prime_all(std::vector<Index> inds, int inc = 1);
+std::vector<Index> dag_all(std::vector<Index> inds);
+std::vector<Index> noprime_all(std::vector<Index> inds);
+Tensor copy_tensor(Ctx& ctx, Tensor const& t);
+double tensor_norm(Ctx& ctx, Tensor const& t);
+
+// ---------------------------------------------------------------- truncate
+// itensor/decomp.cc:305-463 (bit-for-bit the same decisions and values)
+struct TruncResult {
+    std::vector<double> P;
+    double truncerr = 0, docut_lower = 0, docut_upper = 0;
+    int ndegen = 0;
+};
+TruncResult truncate(std::vector<double> P, long maxdim, long mindim, double cutoff, bool absoluteCutoff,
+                     bool doRelCutoff, bool respectDegenerate);
+
+// ---------------------------------------------------------------- combiner
+// combiner / QCombiner (itensor/itensor.cc:1469-1560, itensor/itdata/qcombiner.cc:125-300)
+struct Combiner {
+    std::vector<Index> inds;
+    Index ci;
+    // sector tuple (one per fused index) -> (sector of ci, start, extent)
+    std::map<std::vector<int32_t>, std::array<int32_t, 3>> ranges;
+};
+Combiner make_combiner(std::vector<Index> const& inds);
+Tensor combine(Ctx& ctx, Tensor const& T, Combiner const& C);     // inds: [ci] + rest
+Tensor uncombine(Ctx& ctx, Tensor const& T, Combiner const& C);   // ci replaced in place
+
+// ---------------------------------------------------------------- H_eff and Davidson
+// LocalOp::product (itensor/mps/localop.h:324-365); L or R may be null.
+struct LocalOp {
+    Tensor const* L = nullptr;
+    Tensor const* W1 = nullptr;
+    Tensor const* W2 = nullptr;
+    Tensor const* R = nullptr;
+};
+// H_eff * phi written in phi's layout (phi must hold every block of its divergence).
+// into_phi_layout=false returns the reference's own output structure instead.
+Tensor heff_product(Ctx& ctx, LocalOp const& op, Tensor const& phi, int prec, bool into_phi_layout = true);
+// davidson, block size 1 (itensor/iterativesolvers.h:99-451); phi is replaced by the
+// normalised lowest Ritz vector; returns the Ritz value.
+double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double errgoal, int miniter, int prec,
+                int* applies = nullptr);
+
+// ---------------------------------------------------------------- bond split
+struct SplitArgs {
+    double cutoff = 0;
+    long maxdim = 0, mindim = 1;
+    bool respect_degenerate = true;
+    bool normalize = true;
+};
+struct SplitResult {
+    Tensor A, B;
+    std::vector<double> probs;
+    double truncerr = 0;
+    Index link;
+};
+// denmatDecomp (itensor/decomp.h:316-418) with diag_hermitian's QN branch
+// (itensor/hermitian.cc:180-426) and the DoNormalize step of MPS::svdBond.
+SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor const& B, bool fromleft,
+                          SplitArgs const& args, int prec);
+
+// ---------------------------------------------------------------- models / MPO / MPS
+struct SiteType {
+    std::string name;
+    std::vector<QN> qn;                                   // per basis state
+    std::map<std::string, std::vector<double>> ops;       // d x d, element (i,j) = <i|O|j> at i + d j
+    std::vector<std::string> fermionic;                   // left operators of a hop that carry the string
+    std::vector<std::string> labels;
+    int d() const { return (int)qn.size(); }
+};
+SiteType spin_half(int conserve);   // 0 none, 1 Sz, 2 parity
+SiteType electron();
+
+struct Term2 { double c; std::string a; int i; std::string b; int j; };
+struct Term1 { double c; std::string op; int i; };
+struct Hamiltonian {
+    SiteType st;
+    int N = 0;
+    std::vector<Term1> one;
+    std::vector<Term2> two;
+};
+// model: 0 Heisenberg/XXZ/J1-J2 (J, Jz, J2), 1 transverse-field Ising (h),
+// 2 Hubbard on an Lx x Ly square lattice snaked column by column (t, U, yperiodic)
+struct ModelSpec {
+    int type = 0;
+    int N = 0;
+    double J = 1, Jz = 1, J2 = 0, h = 0, t = 1, U = 0;
+    int Lx = 0, Ly = 1;
+    int yperiodic = 0;
+};
+Hamiltonian make_hamiltonian(ModelSpec const& m);
+
+struct MPO {
+    std::vector<Index> sites;
+    std::vector<Tensor> W;      // W_n: (dag(s_n), s_n', dag(link_{n-1}), link_n), ends projected
+    int bond_dim = 0;
+};
+MPO build_mpo(Ctx& ctx, Hamiltonian const& H);
+// Product state with the link QNs of MPS(InitState) (itensor/mps/mps.cc:558-585).
+std::vector<Tensor> product_mps(Ctx& ctx, MPO const& H, SiteType const& st, std::vector<int> const& states);
+std::vector<int> default_state(ModelSpec const& m);
+
+// ---------------------------------------------------------------- DMRG
+struct SweepSpec { long maxdim = 0, mindim = 1; double cutoff = 0; int niter = 2; double noise = 0; };
+struct BondRecord { int sweep, halfsweep, bond; double energy, truncerr; long dim; };
+struct DmrgResult {
+    double energy = 0;
+    std::vector<BondRecord> bonds;
+    std::vector<Index> links;
+    std::vector<double> sweep_seconds;
+    int heff_applies = 0;
+};
+// DMRGWorker (itensor/mps/dmrg.h:336-467) with LocalMPO environments
+// (itensor/mps/localmpo.h:443-618).
+DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<SweepSpec> const& sweeps, int prec);
+
+}  // namespace itg

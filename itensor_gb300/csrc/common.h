@@ -1,0 +1,74 @@
+// Shared host-side plumbing for the GB300 DMRG hot path: error handling,
+// stream-ordered device buffers, and the per-context state.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace itg {
+
+// Status codes returned through the C-ABI (include/itg.h).
+enum Status : int {
+    OK = 0,
+    ERR_ARG = 1,        // malformed arguments / block metadata
+    ERR_CUDA = 2,       // CUDA runtime error
+    ERR_OOM = 3,        // device allocation failed
+    ERR_NOCONV = 4,     // eigensolver did not converge within its sweep cap
+    ERR_TIMEOUT = 5,    // device-side bounded wait gave up
+    ERR_INTERNAL = 6,
+    ERR_RANGE = 7,      // size beyond a stated maximum
+};
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, std::string const& m) : std::runtime_error(m), code(c) {}
+};
+
+#define ITG_CHECK_CUDA(expr)                                                                      \
+    do {                                                                                          \
+        cudaError_t e_ = (expr);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            throw ::itg::Error(e_ == cudaErrorMemoryAllocation ? ::itg::ERR_OOM : ::itg::ERR_CUDA, \
+                               std::string(#expr) + ": " + cudaGetErrorString(e_));               \
+        }                                                                                         \
+    } while (0)
+
+#define ITG_REQUIRE(cond, msg)                                  \
+    do {                                                        \
+        if (!(cond)) throw ::itg::Error(::itg::ERR_ARG, (msg)); \
+    } while (0)
+
+// Device buffer from the stream-ordered pool (cudaMallocAsync). Freed on the
+// stream it was allocated on, so reuse is ordered after every prior use.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf() = default;
+    DevBuf(size_t n, cudaStream_t s) : bytes(n), stream(s) {
+        if (n) ITG_CHECK_CUDA(cudaMallocAsync(&p, n, s));
+    }
+    ~DevBuf() {
+        if (p) cudaFreeAsync(p, stream);
+    }
+    DevBuf(DevBuf const&) = delete;
+    DevBuf& operator=(DevBuf const&) = delete;
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+using DevBufPtr = std::shared_ptr<DevBuf>;
+
+inline DevBufPtr dev_alloc(size_t bytes, cudaStream_t s) { return std::make_shared<DevBuf>(bytes, s); }
+
+// Arithmetic used by the block GEMMs.
+enum Precision : int {
+    PREC_F64 = 0,        // plain FP64 (FFMA) -- the drop-in path
+    PREC_OZAKI_BF16 = 1, // FP64 operands split into exact BF16 integer slices, FP32-exact accumulation
+    PREC_TF32X3 = 2,     // 3xTF32 split, FP32 accumulate (FP32-level accuracy)
+};
+
+}  // namespace itg

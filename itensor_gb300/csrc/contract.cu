@@ -1,0 +1,916 @@
+// Block-sparse contraction on sm_103a: device planner + grouped block GEMMs.
+//
+// Planner (one CTA): reproduces getContractedOffsets (itensor/itdata/qutil.h:93-242)
+// bit-exactly. A blocks are ranked by their uncontracted coordinates, B blocks by
+// theirs; candidate pairs are enumerated in (B-group, A, B) order, which is already
+// the reversed-lexicographic order of the output block, so matching, compaction,
+// deduplication and the offset prefix sum are three block-wide scans -- no sort
+// of the pair list is needed.
+//
+// GEMMs: every output tile walks the pairs feeding its block. Operands are read
+// through per-block offset tables (offset(m,k) = T_m[m] + T_k[k]), so arbitrary
+// index permutations cost nothing extra and no permuted copy is ever formed.
+#include "engine.h"
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+namespace itg {
+
+// ------------------------------------------------------------------ block scan
+__device__ __forceinline__ int block_excl_scan(int v, int* total, int* sh_warp) {
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh_warp[warp] = x;
+    __syncthreads();
+    int nw = blockDim.x >> 5;
+    if (warp == 0) {
+        int w = lane < nw ? sh_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) sh_warp[lane] = w;  // inclusive warp prefix
+    }
+    __syncthreads();
+    int before = warp ? sh_warp[warp - 1] : 0;
+    *total = sh_warp[nw - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+struct PlanArgs {
+    int nA, nB, rA, rB, ncon, nau, nbu;
+    const int32_t* Acoords;
+    const int32_t* Bcoords;
+    const int32_t* pos;     // [acon(ncon) | bcon(ncon) | aunc(nau) | bunc(nbu)]
+    const int32_t* bits;    // bit widths: [con(ncon) | aunc(nau) | bunc(nbu)]
+    const int32_t* cdims;   // C natural-order sector dims, concatenated
+    const int32_t* cdstart; // start of each C index in cdims
+    // scratch (device)
+    uint64_t* keyA; uint64_t* keyB; uint64_t* conA; uint64_t* conB;
+    int32_t* sortA; int32_t* sortB; int32_t* gstart; uint64_t* pkey;
+    // outputs (host-mapped)
+    int32_t* out_counts;    // [npairs, nC, overflow]
+    int32_t* pair_a; int32_t* pair_b; int32_t* pair_c;
+    int32_t* c_coords;      // nC * (nau+nbu)
+    int64_t* c_off;         // nC + 1 (last = total size)
+    int cap_pairs, cap_c;
+};
+
+__device__ uint64_t pack_key(const int32_t* c, const int32_t* pos, const int32_t* bits, int n) {
+    uint64_t k = 0;
+    int sh = 0;
+    for (int i = 0; i < n; ++i) {
+        k |= (uint64_t)(uint32_t)c[pos[i]] << sh;
+        sh += bits[i];
+    }
+    return k;
+}
+
+__global__ void __launch_bounds__(1024) plan_kernel(PlanArgs a) {
+    __shared__ int sh_warp[32];
+    __shared__ int sh_ngroups;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int32_t* acon = a.pos;
+    const int32_t* bcon = a.pos + a.ncon;
+    const int32_t* aunc = a.pos + 2 * a.ncon;
+    const int32_t* bunc = aunc + a.nau;
+    const int32_t* bcon_bits = a.bits;
+    const int32_t* aunc_bits = a.bits + a.ncon;
+    const int32_t* bunc_bits = aunc_bits + a.nau;
+    int bitsA = 0;
+    for (int i = 0; i < a.nau; ++i) bitsA += aunc_bits[i];
+    // 1. keys
+    for (int i = tid; i < a.nA; i += nt) {
+        const int32_t* c = a.Acoords + (size_t)i * a.rA;
+        a.keyA[i] = pack_key(c, aunc, aunc_bits, a.nau);
+        a.conA[i] = pack_key(c, acon, bcon_bits, a.ncon);
+    }
+    for (int j = tid; j < a.nB; j += nt) {
+        const int32_t* c = a.Bcoords + (size_t)j * a.rB;
+        a.keyB[j] = pack_key(c, bunc, bunc_bits, a.nbu);
+        a.conB[j] = pack_key(c, bcon, bcon_bits, a.ncon);
+    }
+    __syncthreads();
+    // 2. rank sorts (stable by original position)
+    for (int i = tid; i < a.nA; i += nt) {
+        uint64_t k = a.keyA[i];
+        int r = 0;
+        for (int j = 0; j < a.nA; ++j) {
+            uint64_t kj = a.keyA[j];
+            r += (kj < k) || (kj == k && j < i);
+        }
+        a.sortA[r] = i;
+    }
+    for (int i = tid; i < a.nB; i += nt) {
+        uint64_t k = a.keyB[i];
+        int r = 0;
+        for (int j = 0; j < a.nB; ++j) {
+            uint64_t kj = a.keyB[j];
+            r += (kj < k) || (kj == k && j < i);
+        }
+        a.sortB[r] = i;
+    }
+    __syncthreads();
+    // 3. groups of equal B keys among sorted B
+    int base = 0;
+    for (int s0 = 0; s0 < a.nB; s0 += nt) {
+        int s = s0 + tid;
+        int f = 0;
+        if (s < a.nB) f = (s == 0) || (a.keyB[a.sortB[s]] != a.keyB[a.sortB[s - 1]]);
+        int tot;
+        int ex = block_excl_scan(f, &tot, sh_warp);
+        if (f) a.gstart[base + ex] = s;
+        base += tot;
+    }
+    if (tid == 0) { a.gstart[base] = a.nB; sh_ngroups = base; }
+    __syncthreads();
+    const int ng = sh_ngroups;
+    // 4. candidates in (group, sorted A, B in group) order; compact the matches
+    const long long total = (long long)a.nA * a.nB;
+    int np = 0;
+    bool overflow = false;
+    for (long long t0 = 0; t0 < total; t0 += nt) {
+        long long t = t0 + tid;
+        int f = 0, ia = -1, jb = -1;
+        if (t < total) {
+            int lo = 0, hi = ng - 1;  // last group g with nA*gstart[g] <= t
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if ((long long)a.nA * a.gstart[mid] <= t) lo = mid;
+                else hi = mid - 1;
+            }
+            int g = lo;
+            int gs = a.gstart[g], sz = a.gstart[g + 1] - gs;
+            long long local = t - (long long)a.nA * gs;
+            ia = a.sortA[local / sz];
+            jb = a.sortB[gs + (int)(local % sz)];
+            f = a.conA[ia] == a.conB[jb];
+        }
+        int tot;
+        int ex = block_excl_scan(f, &tot, sh_warp);
+        if (f) {
+            int p = np + ex;
+            if (p < a.cap_pairs) {
+                a.pair_a[p] = ia;
+                a.pair_b[p] = jb;
+                a.pkey[p] = a.keyA[ia] | (a.keyB[jb] << bitsA);
+            }
+        }
+        np += tot;
+    }
+    if (np > a.cap_pairs) overflow = true;
+    __syncthreads();
+    // 5. output blocks: boundaries of equal keys, coordinates and sizes
+    int nc = 0;
+    const int rC = a.nau + a.nbu;
+    if (!overflow) {
+        for (int p0 = 0; p0 < np; p0 += nt) {
+            int p = p0 + tid;
+            int f = 0;
+            if (p < np) f = (p == 0) || (a.pkey[p] != a.pkey[p - 1]);
+            int tot;
+            int ex = block_excl_scan(f, &tot, sh_warp);
+            __syncthreads();
+            if (p < np) {
+                // C index of this pair: blocks before it = nc + (inclusive count) - 1
+                a.pair_c[p] = nc + ex + f - 1;
+            }
+            if (f && nc + ex < a.cap_c) {
+                int c = nc + ex;
+                const int32_t* ca = a.Acoords + (size_t)a.pair_a[p] * a.rA;
+                const int32_t* cb = a.Bcoords + (size_t)a.pair_b[p] * a.rB;
+                int64_t size = 1;
+                for (int i = 0; i < a.nau; ++i) {
+                    int s = ca[aunc[i]];
+                    a.c_coords[(size_t)c * rC + i] = s;
+                    size *= a.cdims[a.cdstart[i] + s];
+                }
+                for (int i = 0; i < a.nbu; ++i) {
+                    int s = cb[bunc[i]];
+                    a.c_coords[(size_t)c * rC + a.nau + i] = s;
+                    size *= a.cdims[a.cdstart[a.nau + i] + s];
+                }
+                a.c_off[c] = size;
+            }
+            nc += tot;
+        }
+        // fix pair_c of pairs whose block started in an earlier chunk: pair_c from
+        // the scan above is exact because nc carries across chunks.
+    }
+    if (nc > a.cap_c) overflow = true;
+    __syncthreads();
+    // 6. offsets = exclusive prefix sum of block sizes (serial over chunks, 64-bit)
+    if (!overflow) {
+        __shared__ long long sh_carry;
+        if (tid == 0) sh_carry = 0;
+        __syncthreads();
+        for (int c0 = 0; c0 < nc; c0 += nt) {
+            int c = c0 + tid;
+            long long v = (c < nc) ? a.c_off[c] : 0;
+            // 64-bit inclusive scan via warp shuffles + shared warp sums
+            long long x = v;
+            int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                long long y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            __shared__ long long sw[32];
+            if (lane == 31) sw[warp] = x;
+            __syncthreads();
+            if (warp == 0) {
+                long long w = lane < (nt >> 5) ? sw[lane] : 0;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    long long y = __shfl_up_sync(0xffffffffu, w, o);
+                    if (lane >= o) w += y;
+                }
+                sw[lane] = w;
+            }
+            __syncthreads();
+            long long incl = x + (warp ? sw[warp - 1] : 0);
+            long long carry = sh_carry;
+            __syncthreads();
+            if (c < nc) a.c_off[c] = carry + incl - v;
+            if (tid == nt - 1) sh_carry = carry + incl;
+            __syncthreads();
+        }
+        if (tid == 0) a.c_off[nc] = sh_carry;
+    }
+    if (tid == 0) {
+        a.out_counts[0] = np;
+        a.out_counts[1] = nc;
+        a.out_counts[2] = overflow ? 1 : 0;
+    }
+}
+
+// ------------------------------------------------------------------ FP64 block GEMM
+// One CTA per 32x32 output tile; 256 threads, 2x2 outputs each. Warps own
+// output columns, so warps whose columns lie outside a narrow block skip the
+// FMA loop entirely (FP64 issue slots are the bound on this part).
+__global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict__ items,
+                                                       const PairRec* __restrict__ pairs,
+                                                       const CBlockRec* __restrict__ cblk,
+                                                       const int32_t* __restrict__ tab,
+                                                       const double* __restrict__ A,
+                                                       const double* __restrict__ B,
+                                                       double* __restrict__ C) {
+    constexpr int T = GEMM_TILE, TK = 16;
+    __shared__ double As[TK][T + 1];
+    __shared__ double Bs[TK][T + 1];
+    const ItemRec it = items[blockIdx.x];
+    const CBlockRec cb = cblk[it.c];
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;     // rows tx*2+{0,1}, cols ty*2+{0,1}
+    const int warp_col0 = (tid >> 5) * 4;       // first column touched by this warp
+    const bool warp_active = it.n0 + warp_col0 < cb.N;
+    double acc00 = 0, acc01 = 0, acc10 = 0, acc11 = 0;
+    for (int p = it.p0; p < it.p1; ++p) {
+        const PairRec pr = pairs[p];
+        for (int k0 = 0; k0 < pr.K; k0 += TK) {
+            for (int e = tid; e < TK * T; e += 256) {
+                int i = e % T, kk = e / T;
+                int m = it.m0 + i, k = k0 + kk;
+                As[kk][i] = (m < cb.M && k < pr.K) ? A[pr.aoff + tab[pr.tam + m] + tab[pr.tak + k]] : 0.0;
+                int n = it.n0 + i;
+                Bs[kk][i] = (n < cb.N && k < pr.K) ? B[pr.boff + tab[pr.tbk + k] + tab[pr.tbn + n]] : 0.0;
+            }
+            __syncthreads();
+            if (warp_active) {
+                const int kmax = min(TK, pr.K - k0);
+                for (int kk = 0; kk < kmax; ++kk) {
+                    double a0 = As[kk][tx * 2], a1 = As[kk][tx * 2 + 1];
+                    double b0 = Bs[kk][ty * 2], b1 = Bs[kk][ty * 2 + 1];
+                    acc00 = fma(a0, b0, acc00);
+                    acc01 = fma(a0, b1, acc01);
+                    acc10 = fma(a1, b0, acc10);
+                    acc11 = fma(a1, b1, acc11);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    const int m = it.m0 + tx * 2, n = it.n0 + ty * 2;
+    double accs[2][2] = {{acc00, acc01}, {acc10, acc11}};
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+            if (m + r < cb.M && n + s < cb.N) C[cb.coff + tab[cb.tcm + m + r] + tab[cb.tcn + n + s]] = accs[r][s];
+}
+
+// ------------------------------------------------------------------ Ozaki BF16 block GEMM
+// FP64 operands become fixed-point integers relative to a power-of-two scale
+// per tile row (A) / tile column (B): X = floor(|x| 2^(7S - e)), |x| < 2^e,
+// cut into S digits of 7 bits (sign applied), each exact in BF16. Digit
+// products are exact in FP32 and so are their sums while |sum| < 2^24. Digit
+// pairs (s,t) with s+t < S are accumulated per diagonal D = s+t on the BF16
+// tensor pipe (mma.sync m16n8k16, FP32 accumulate); every 256 k the diagonals
+// are converted to integers and folded into one int64 accumulator
+// sum_D acc_D 2^(7(S-1-D)). One FP64 conversion per output at the end.
+// The slicing and folding use integer instructions only (FP64 issue slots on
+// this part are ~1/60 of FP32). Accuracy ~2^(-7S) of row/column maxima.
+__device__ __forceinline__ int exp_field(double x) {
+    return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+template <int S>
+__device__ __forceinline__ void ozaki_digits(double x, int e, __nv_bfloat16* dst, int stride) {
+    long long bits = __double_as_longlong(x);
+    int ef = (int)((bits >> 52) & 0x7FF);
+    unsigned long long X = 0;
+    if (ef != 0) {
+        unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+        int sh = ef - 1075 + 7 * S - e;  // |x| = mant 2^(ef-1075)
+        if (sh >= 0) X = mant << sh;
+        else if (sh > -64) X = mant >> (-sh);
+    }
+    const bool neg = bits < 0;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        int d = (int)((X >> (7 * (S - 1 - s))) & 127ull);
+        dst[s * stride] = __float2bfloat16_rn((float)(neg ? -d : d));
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(128) gemm_ozaki_kernel(const ItemRec* __restrict__ items,
+                                                         const PairRec* __restrict__ pairs,
+                                                         const CBlockRec* __restrict__ cblk,
+                                                         const int32_t* __restrict__ tab,
+                                                         const double* __restrict__ A,
+                                                         const double* __restrict__ B,
+                                                         double* __restrict__ C) {
+    constexpr int T = GEMM_TILE, TK = 16, KCHUNK = 256, LD = TK + 8;
+    __shared__ __align__(16) __nv_bfloat16 As[S][T][LD];
+    __shared__ __align__(16) __nv_bfloat16 Bs[S][T][LD];
+    __shared__ int rowexp[T], colexp[T];
+    const ItemRec it = items[blockIdx.x];
+    const CBlockRec cb = cblk[it.c];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = (warp & 1) * 16, wn = (warp >> 1) * 16;  // warp tile 16x16 = 2 mma n-tiles
+    const int g = lane >> 2, tg = lane & 3;
+    // pass 1: exponent scale per tile row / column over every pair of the tile
+    if (tid < 2 * T) {
+        const bool isrow = tid < T;
+        const int i = isrow ? tid : tid - T;
+        const int mn = isrow ? it.m0 + i : it.n0 + i;
+        int emax = 0;
+        if (mn < (isrow ? cb.M : cb.N)) {
+            for (int p = it.p0; p < it.p1; ++p) {
+                const PairRec pr = pairs[p];
+                if (isrow) {
+                    const double* a = A + pr.aoff + tab[pr.tam + mn];
+                    for (int k = 0; k < pr.K; ++k) emax = max(emax, exp_field(a[tab[pr.tak + k]]));
+                } else {
+                    const double* b = B + pr.boff + tab[pr.tbn + mn];
+                    for (int k = 0; k < pr.K; ++k) emax = max(emax, exp_field(b[tab[pr.tbk + k]]));
+                }
+            }
+        }
+        // |x| < 2^(emax - 1022) for every x in this row / column
+        if (isrow) rowexp[i] = emax - 1022;
+        else colexp[i] = emax - 1022;
+    }
+    __syncthreads();
+    long long tot[2][4];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tot[j][q] = 0;
+    float acc[S][2][4];
+#pragma unroll
+    for (int d = 0; d < S; ++d)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[d][j][q] = 0.f;
+    int kacc = 0;  // k accumulated in acc since the last fold
+    auto fold = [&]() {
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                long long v = 0;
+#pragma unroll
+                for (int d = 0; d < S; ++d) {
+                    v += (long long)__float2ll_rn(acc[d][j][q]) << (7 * (S - 1 - d));
+                    acc[d][j][q] = 0.f;
+                }
+                tot[j][q] += v;
+            }
+    };
+    for (int p = it.p0; p < it.p1; ++p) {
+        const PairRec pr = pairs[p];
+        for (int k0 = 0; k0 < pr.K; k0 += TK) {
+            for (int e = tid; e < T * TK; e += 128) {
+                const int i = e % T, kk = e / T, k = k0 + kk;
+                const int m = it.m0 + i, n = it.n0 + i;
+                double x = (m < cb.M && k < pr.K) ? A[pr.aoff + tab[pr.tam + m] + tab[pr.tak + k]] : 0.0;
+                double y = (n < cb.N && k < pr.K) ? B[pr.boff + tab[pr.tbk + k] + tab[pr.tbn + n]] : 0.0;
+                ozaki_digits<S>(x, rowexp[i], &As[0][i][kk], T * LD);
+                ozaki_digits<S>(y, colexp[i], &Bs[0][i][kk], T * LD);
+            }
+            __syncthreads();
+            uint32_t af[S][4], bfr[S][2][2];
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                af[s][0] = *reinterpret_cast<const uint32_t*>(&As[s][wm + g][tg * 2]);
+                af[s][1] = *reinterpret_cast<const uint32_t*>(&As[s][wm + g + 8][tg * 2]);
+                af[s][2] = *reinterpret_cast<const uint32_t*>(&As[s][wm + g][tg * 2 + 8]);
+                af[s][3] = *reinterpret_cast<const uint32_t*>(&As[s][wm + g + 8][tg * 2 + 8]);
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    bfr[s][j][0] = *reinterpret_cast<const uint32_t*>(&Bs[s][wn + j * 8 + g][tg * 2]);
+                    bfr[s][j][1] = *reinterpret_cast<const uint32_t*>(&Bs[s][wn + j * 8 + g][tg * 2 + 8]);
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+#pragma unroll
+                for (int t = 0; t + s < S; ++t)
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        float* c = acc[s + t][j];
+                        asm volatile(
+                            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                            "{%8,%9}, {%0,%1,%2,%3};\n"
+                            : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                            : "r"(af[s][0]), "r"(af[s][1]), "r"(af[s][2]), "r"(af[s][3]), "r"(bfr[t][j][0]),
+                              "r"(bfr[t][j][1]));
+                    }
+            __syncthreads();
+            kacc += TK;
+            if (kacc >= KCHUNK) { fold(); kacc = 0; }
+        }
+    }
+    fold();
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int r = wm + g + (q >= 2 ? 8 : 0);
+            const int cc = wn + j * 8 + tg * 2 + (q & 1);
+            const int m = it.m0 + r, n = it.n0 + cc;
+            if (m < cb.M && n < cb.N) {
+                // value = tot * 2^(e_row + e_col - 7 S - 7)
+                C[cb.coff + tab[cb.tcm + m] + tab[cb.tcn + n]] = ldexp((double)tot[j][q], rowexp[r] + colexp[cc] - 7 * S - 7);
+            }
+        }
+}
+
+// ------------------------------------------------------------------ host side
+Ctx::Ctx(int dev) : device(dev) {
+    ITG_CHECK_CUDA(cudaSetDevice(dev));
+    ITG_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    int sms = 0;
+    ITG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    sm_count = sms;
+    cudaMemPool_t pool;
+    ITG_CHECK_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
+    ITG_CHECK_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+}
+
+Ctx::~Ctx() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (auto& r : prof) { cudaEventDestroy(r.start); cudaEventDestroy(r.stop); }
+    plans.clear();
+    if (pin) cudaFreeHost(pin);
+    if (stage) cudaFreeHost(stage);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void Ctx::ensure_pin(size_t bytes) {
+    if (pin_bytes >= bytes) return;
+    sync();
+    if (pin) cudaFreeHost(pin);
+    pin = nullptr;
+    size_t nb = std::max<size_t>(bytes, 1 << 20);
+    ITG_CHECK_CUDA(cudaHostAlloc(&pin, nb, cudaHostAllocMapped));
+    ITG_CHECK_CUDA(cudaHostGetDevicePointer(&pin_dev, pin, 0));
+    pin_bytes = nb;
+}
+
+void Ctx::ensure_stage(size_t bytes) {
+    if (stage_bytes >= bytes) return;
+    sync();
+    if (stage) cudaFreeHost(stage);
+    stage = nullptr;
+    size_t nb = std::max<size_t>(bytes, 1 << 20);
+    ITG_CHECK_CUDA(cudaHostAlloc(&stage, nb, cudaHostAllocDefault));
+    stage_bytes = nb;
+}
+
+Match match_indices(std::vector<Index> const& A, std::vector<Index> const& B) {
+    Match m;
+    std::vector<char> bused(B.size(), 0);
+    std::vector<char> acon(A.size(), 0);
+    for (size_t i = 0; i < A.size(); ++i)
+        for (size_t j = 0; j < B.size(); ++j)
+            if (!bused[j] && A[i].same(B[j])) {
+                m.a_con.push_back((int)i);
+                m.b_con.push_back((int)j);
+                bused[j] = 1;
+                acon[i] = 1;
+                break;
+            }
+    for (size_t i = 0; i < A.size(); ++i) if (!acon[i]) m.a_unc.push_back((int)i);
+    for (size_t j = 0; j < B.size(); ++j) if (!bused[j]) m.b_unc.push_back((int)j);
+    return m;
+}
+
+namespace {
+
+template <typename T> void put(std::string& s, T const& v) { s.append(reinterpret_cast<char const*>(&v), sizeof(T)); }
+template <typename T> void putv(std::string& s, std::vector<T> const& v) {
+    put(s, (uint64_t)v.size());
+    if (!v.empty()) s.append(reinterpret_cast<char const*>(v.data()), v.size() * sizeof(T));
+}
+void put_layout_structure(std::string& s, Layout const& L) {
+    put(s, (int32_t)L.rank());
+    for (auto const& I : L.inds) putv(s, I.sec->dim);
+    putv(s, L.coords);
+}
+
+int bits_for(int n) {
+    int b = 0;
+    while ((1 << b) < n) ++b;
+    return b;
+}
+
+void enum_offsets(std::vector<int32_t>& tab, std::vector<int> const& dims, std::vector<int64_t> const& strides) {
+    int n = (int)dims.size();
+    int64_t total = 1;
+    for (int d : dims) total *= d;
+    std::vector<int> dig(n, 0);
+    int64_t off = 0;
+    for (int64_t t = 0; t < total; ++t) {
+        tab.push_back((int32_t)off);
+        for (int k = 0; k < n; ++k) {
+            off += strides[k];
+            if (++dig[k] < dims[k]) break;
+            off -= strides[k] * dims[k];
+            dig[k] = 0;
+        }
+    }
+}
+
+std::vector<int64_t> block_strides(Layout const& L, int b) {
+    std::vector<int64_t> st(L.rank());
+    int64_t s = 1;
+    for (int k = 0; k < L.rank(); ++k) { st[k] = s; s *= L.inds[k].bdim(L.block(b)[k]); }
+    return st;
+}
+
+size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+}  // namespace
+
+std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match const& mt,
+                               std::shared_ptr<Layout> target) {
+    const int nau = (int)mt.a_unc.size(), nbu = (int)mt.b_unc.size(), ncon = (int)mt.a_con.size();
+    const int rC = nau + nbu;
+    // natural output index order: A's uncontracted, then B's (contractIS)
+    std::vector<Index> cinds;
+    for (int i : mt.a_unc) cinds.push_back(A.inds[i]);
+    for (int j : mt.b_unc) cinds.push_back(B.inds[j]);
+    std::vector<int> perm(rC);  // natural C position -> target position
+    if (target) {
+        ITG_REQUIRE(target->rank() == rC, "contract: target layout has rank " + std::to_string(target->rank()) +
+                                              ", the product has rank " + std::to_string(rC));
+        for (int k = 0; k < rC; ++k) {
+            perm[k] = target->find_index(cinds[k]);
+            ITG_REQUIRE(perm[k] >= 0, "contract: target layout lacks an output index");
+        }
+    } else {
+        std::iota(perm.begin(), perm.end(), 0);
+    }
+    std::string key;
+    key.reserve(256 + 4 * (A.coords.size() + B.coords.size()));
+    put_layout_structure(key, A);
+    put_layout_structure(key, B);
+    putv(key, mt.a_con); putv(key, mt.b_con); putv(key, mt.a_unc); putv(key, mt.b_unc);
+    put(key, (int32_t)(target ? 1 : 0));
+    if (target) { put_layout_structure(key, *target); putv(key, perm); }
+    auto hit = ctx.plans.find(key);
+    if (hit != ctx.plans.end()) { ctx.plan_hits++; return hit->second; }
+
+    const int nA = A.nblocks(), nB = B.nblocks(), rA = A.rank(), rB = B.rank();
+    // ---- device planner inputs
+    std::vector<int32_t> pos, bits, cdims, cdstart;
+    for (int i : mt.a_con) pos.push_back(i);
+    for (int j : mt.b_con) pos.push_back(j);
+    for (int i : mt.a_unc) pos.push_back(i);
+    for (int j : mt.b_unc) pos.push_back(j);
+    int bcon = 0, bunc = 0;
+    for (int q = 0; q < ncon; ++q) { int b = bits_for(A.inds[mt.a_con[q]].nblock()); bits.push_back(b); bcon += b; }
+    for (int i : mt.a_unc) { int b = bits_for(A.inds[i].nblock()); bits.push_back(b); bunc += b; }
+    for (int j : mt.b_unc) { int b = bits_for(B.inds[j].nblock()); bits.push_back(b); bunc += b; }
+    if (bcon > 64 || bunc > 64) throw Error(ERR_RANGE, "contract: block coordinates need more than 64 key bits");
+    for (auto const& I : cinds) {
+        cdstart.push_back((int32_t)cdims.size());
+        for (int d : I.sec->dim) cdims.push_back(d);
+    }
+    const long long cap_ll = std::max<long long>(1, (long long)nA * nB);
+    if (cap_ll > (1ll << 26)) throw Error(ERR_RANGE, "contract: too many candidate block pairs");
+    const int cap = (int)cap_ll;
+
+    auto plan = std::make_shared<Plan>();
+    if (nA > 0 && nB > 0) {
+        // inputs -> device (one staged copy)
+        size_t o_ac = 0, o_bc = align16(o_ac + sizeof(int32_t) * std::max<size_t>(1, A.coords.size()));
+        size_t o_pos = align16(o_bc + sizeof(int32_t) * std::max<size_t>(1, B.coords.size()));
+        size_t o_bits = align16(o_pos + sizeof(int32_t) * std::max<size_t>(1, pos.size()));
+        size_t o_cd = align16(o_bits + sizeof(int32_t) * std::max<size_t>(1, bits.size()));
+        size_t o_cs = align16(o_cd + sizeof(int32_t) * std::max<size_t>(1, cdims.size()));
+        size_t in_bytes = align16(o_cs + sizeof(int32_t) * std::max<size_t>(1, cdstart.size()));
+        ctx.ensure_stage(in_bytes);
+        char* st = static_cast<char*>(ctx.stage);
+        auto cp = [&](size_t o, auto const& v) { if (!v.empty()) std::memcpy(st + o, v.data(), v.size() * sizeof(v[0])); };
+        cp(o_ac, A.coords); cp(o_bc, B.coords); cp(o_pos, pos); cp(o_bits, bits); cp(o_cd, cdims); cp(o_cs, cdstart);
+        size_t o_keyA = align16(in_bytes), o_keyB = align16(o_keyA + 8 * (size_t)nA);
+        size_t o_conA = align16(o_keyB + 8 * (size_t)nB), o_conB = align16(o_conA + 8 * (size_t)nA);
+        size_t o_sA = align16(o_conB + 8 * (size_t)nB), o_sB = align16(o_sA + 4 * (size_t)nA);
+        size_t o_gs = align16(o_sB + 4 * (size_t)nB), o_pk = align16(o_gs + 4 * (size_t)(nB + 1));
+        size_t dev_bytes = align16(o_pk + 8 * (size_t)cap);
+        DevBuf scratch(dev_bytes, ctx.stream);
+        char* dv = scratch.as<char>();
+        ITG_CHECK_CUDA(cudaMemcpyAsync(dv, st, in_bytes, cudaMemcpyHostToDevice, ctx.stream));
+        // outputs in host-mapped memory
+        size_t p_cnt = 0, p_pa = 16, p_pb = align16(p_pa + 4 * (size_t)cap), p_pc = align16(p_pb + 4 * (size_t)cap);
+        size_t p_cc = align16(p_pc + 4 * (size_t)cap), p_co = align16(p_cc + 4 * (size_t)cap * std::max(rC, 1));
+        size_t out_bytes = align16(p_co + 8 * ((size_t)cap + 1));
+        ctx.ensure_pin(out_bytes);
+        char* hp = static_cast<char*>(ctx.pin);
+        char* dp = static_cast<char*>(ctx.pin_dev);
+        PlanArgs a;
+        a.nA = nA; a.nB = nB; a.rA = rA; a.rB = rB; a.ncon = ncon; a.nau = nau; a.nbu = nbu;
+        a.Acoords = reinterpret_cast<const int32_t*>(dv + o_ac);
+        a.Bcoords = reinterpret_cast<const int32_t*>(dv + o_bc);
+        a.pos = reinterpret_cast<const int32_t*>(dv + o_pos);
+        a.bits = reinterpret_cast<const int32_t*>(dv + o_bits);
+        a.cdims = reinterpret_cast<const int32_t*>(dv + o_cd);
+        a.cdstart = reinterpret_cast<const int32_t*>(dv + o_cs);
+        a.keyA = reinterpret_cast<uint64_t*>(dv + o_keyA); a.keyB = reinterpret_cast<uint64_t*>(dv + o_keyB);
+        a.conA = reinterpret_cast<uint64_t*>(dv + o_conA); a.conB = reinterpret_cast<uint64_t*>(dv + o_conB);
+        a.sortA = reinterpret_cast<int32_t*>(dv + o_sA); a.sortB = reinterpret_cast<int32_t*>(dv + o_sB);
+        a.gstart = reinterpret_cast<int32_t*>(dv + o_gs); a.pkey = reinterpret_cast<uint64_t*>(dv + o_pk);
+        a.out_counts = reinterpret_cast<int32_t*>(dp + p_cnt);
+        a.pair_a = reinterpret_cast<int32_t*>(dp + p_pa); a.pair_b = reinterpret_cast<int32_t*>(dp + p_pb);
+        a.pair_c = reinterpret_cast<int32_t*>(dp + p_pc);
+        a.c_coords = reinterpret_cast<int32_t*>(dp + p_cc);
+        a.c_off = reinterpret_cast<int64_t*>(dp + p_co);
+        a.cap_pairs = cap; a.cap_c = cap;
+        plan_kernel<<<1, 1024, 0, ctx.stream>>>(a);
+        ITG_CHECK_CUDA(cudaGetLastError());
+        ctx.kernel_launches++;
+        ctx.sync();
+        int32_t const* cnt = reinterpret_cast<int32_t const*>(hp + p_cnt);
+        if (cnt[2]) throw Error(ERR_INTERNAL, "contract planner: capacity overflow");
+        const int np = cnt[0], nc = cnt[1];
+        std::vector<int32_t> pa(reinterpret_cast<int32_t*>(hp + p_pa), reinterpret_cast<int32_t*>(hp + p_pa) + np);
+        std::vector<int32_t> pb(reinterpret_cast<int32_t*>(hp + p_pb), reinterpret_cast<int32_t*>(hp + p_pb) + np);
+        std::vector<int32_t> pc(reinterpret_cast<int32_t*>(hp + p_pc), reinterpret_cast<int32_t*>(hp + p_pc) + np);
+        auto natural = std::make_shared<Layout>();
+        natural->inds = cinds;
+        if (rC > 0) {
+            natural->coords.assign(reinterpret_cast<int32_t*>(hp + p_cc), reinterpret_cast<int32_t*>(hp + p_cc) + (size_t)nc * rC);
+            natural->offs.assign(reinterpret_cast<int64_t*>(hp + p_co), reinterpret_cast<int64_t*>(hp + p_co) + nc);
+            natural->size = reinterpret_cast<int64_t*>(hp + p_co)[nc];
+        } else {
+            natural->finish();  // one scalar block
+        }
+        plan->C = target ? target : natural;
+        // ---- map natural blocks to target blocks
+        const Layout& CL = *plan->C;
+        std::vector<int> nat2t(std::max(nc, 1), 0);
+        if (rC > 0) {
+            std::vector<int32_t> tc(rC);
+            for (int c = 0; c < nc; ++c) {
+                for (int k = 0; k < rC; ++k) tc[perm[k]] = natural->coords[(size_t)c * rC + k];
+                int tb = CL.find_block(tc.data());
+                ITG_REQUIRE(tb >= 0, "contract: target layout lacks a produced block");
+                nat2t[c] = tb;
+            }
+        }
+        // ---- tables
+        std::vector<int32_t> tab;
+        std::vector<int> tamA(nA, -1), takA(nA, -1), tbkB(nB, -1), tbnB(nB, -1);
+        auto ensureA = [&](int ab) {
+            if (tamA[ab] >= 0) return;
+            auto st_ = block_strides(A, ab);
+            std::vector<int> dm, dk; std::vector<int64_t> sm, sk;
+            for (int i : mt.a_unc) { dm.push_back(A.inds[i].bdim(A.block(ab)[i])); sm.push_back(st_[i]); }
+            for (int i : mt.a_con) { dk.push_back(A.inds[i].bdim(A.block(ab)[i])); sk.push_back(st_[i]); }
+            tamA[ab] = (int)tab.size(); enum_offsets(tab, dm, sm);
+            takA[ab] = (int)tab.size(); enum_offsets(tab, dk, sk);
+        };
+        auto ensureB = [&](int bb) {
+            if (tbkB[bb] >= 0) return;
+            auto st_ = block_strides(B, bb);
+            std::vector<int> dk, dn; std::vector<int64_t> sk, sn;
+            for (int j : mt.b_con) { dk.push_back(B.inds[j].bdim(B.block(bb)[j])); sk.push_back(st_[j]); }
+            for (int j : mt.b_unc) { dn.push_back(B.inds[j].bdim(B.block(bb)[j])); sn.push_back(st_[j]); }
+            tbkB[bb] = (int)tab.size(); enum_offsets(tab, dk, sk);
+            tbnB[bb] = (int)tab.size(); enum_offsets(tab, dn, sn);
+        };
+        const int ncb = CL.nblocks();
+        std::vector<CBlockRec> cblk(ncb);
+        for (int c = 0; c < ncb; ++c) {
+            auto st_ = rC ? block_strides(CL, c) : std::vector<int64_t>();
+            std::vector<int> dm, dn; std::vector<int64_t> sm, sn;
+            for (int q = 0; q < nau; ++q) { int tpos = perm[q]; dm.push_back(CL.inds[tpos].bdim(CL.block(c)[tpos])); sm.push_back(st_[tpos]); }
+            for (int q = 0; q < nbu; ++q) { int tpos = perm[nau + q]; dn.push_back(CL.inds[tpos].bdim(CL.block(c)[tpos])); sn.push_back(st_[tpos]); }
+            CBlockRec r;
+            r.coff = CL.offs[c];
+            r.M = 1; for (int d : dm) r.M *= d;
+            r.N = 1; for (int d : dn) r.N *= d;
+            r.tcm = (int)tab.size(); enum_offsets(tab, dm, sm);
+            r.tcn = (int)tab.size(); enum_offsets(tab, dn, sn);
+            cblk[c] = r;
+        }
+        // pairs grouped by target block (stable)
+        std::vector<std::vector<int>> bypc(ncb);
+        for (int p = 0; p < np; ++p) bypc[rC ? nat2t[pc[p]] : 0].push_back(p);
+        std::vector<PairRec> pairs;
+        pairs.reserve(np);
+        std::vector<int> cp0(ncb), cp1(ncb);
+        std::vector<double> cK(ncb, 0.0);
+        double flops = 0; int64_t bytes_ab = 0; int maxK = 0; double sumK = 0;
+        for (int c = 0; c < ncb; ++c) {
+            cp0[c] = (int)pairs.size();
+            int ksum = 0;
+            for (int p : bypc[c]) {
+                ensureA(pa[p]); ensureB(pb[p]);
+                PairRec r;
+                r.aoff = A.offs[pa[p]]; r.boff = B.offs[pb[p]];
+                r.tam = tamA[pa[p]]; r.tak = takA[pa[p]]; r.tbk = tbkB[pb[p]]; r.tbn = tbnB[pb[p]];
+                int K = 1;
+                for (int i : mt.a_con) K *= A.inds[i].bdim(A.block(pa[p])[i]);
+                r.K = K; r.pad = 0;
+                pairs.push_back(r);
+                ksum += K;
+                flops += 2.0 * cblk[c].M * (double)cblk[c].N * K;
+                bytes_ab += (int64_t)cblk[c].M * K + (int64_t)K * cblk[c].N;
+            }
+            cp1[c] = (int)pairs.size();
+            cK[c] = ksum;
+            maxK = std::max(maxK, ksum);
+            sumK += ksum;
+        }
+        // tiles, most expensive first
+        std::vector<ItemRec> items;
+        std::vector<double> cost;
+        for (int c = 0; c < ncb; ++c)
+            for (int m0 = 0; m0 < cblk[c].M; m0 += GEMM_TILE)
+                for (int n0 = 0; n0 < cblk[c].N; n0 += GEMM_TILE) {
+                    items.push_back(ItemRec{c, m0, n0, cp0[c], cp1[c]});
+                    cost.push_back(cK[c] + 1.0);
+                }
+        std::vector<int> ord(items.size());
+        std::iota(ord.begin(), ord.end(), 0);
+        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+        std::vector<ItemRec> sitems(items.size());
+        for (size_t i = 0; i < ord.size(); ++i) sitems[i] = items[ord[i]];
+        // upload
+        size_t t_items = 0, t_pairs = align16(sizeof(ItemRec) * sitems.size());
+        size_t t_cblk = align16(t_pairs + sizeof(PairRec) * pairs.size());
+        size_t t_tab = align16(t_cblk + sizeof(CBlockRec) * cblk.size());
+        size_t tbytes = align16(t_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size()));
+        ctx.ensure_stage(tbytes);
+        st = static_cast<char*>(ctx.stage);
+        if (!sitems.empty()) std::memcpy(st + t_items, sitems.data(), sizeof(ItemRec) * sitems.size());
+        if (!pairs.empty()) std::memcpy(st + t_pairs, pairs.data(), sizeof(PairRec) * pairs.size());
+        if (!cblk.empty()) std::memcpy(st + t_cblk, cblk.data(), sizeof(CBlockRec) * cblk.size());
+        if (!tab.empty()) std::memcpy(st + t_tab, tab.data(), sizeof(int32_t) * tab.size());
+        plan->dev = dev_alloc(tbytes, ctx.stream);
+        char* db = plan->dev->as<char>();
+        ITG_CHECK_CUDA(cudaMemcpyAsync(db, st, tbytes, cudaMemcpyHostToDevice, ctx.stream));
+        ctx.sync();  // staging buffer is reused by the next plan
+        plan->d_items = reinterpret_cast<ItemRec*>(db + t_items);
+        plan->d_pairs = reinterpret_cast<PairRec*>(db + t_pairs);
+        plan->d_cblk = reinterpret_cast<CBlockRec*>(db + t_cblk);
+        plan->d_tab = reinterpret_cast<int32_t*>(db + t_tab);
+        plan->nitems = (int)sitems.size();
+        plan->npairs = np;
+        plan->ncblk = ncb;
+        plan->flops = flops;
+        plan->bytes_ab = bytes_ab;
+        plan->maxK = maxK;
+        plan->avgK = ncb ? sumK / ncb : 0;
+    } else {
+        // an empty operand: the output has no blocks (or is the scalar 0)
+        auto natural = std::make_shared<Layout>();
+        natural->inds = cinds;
+        natural->finish();
+        if (rC > 0) { natural->offs.clear(); natural->size = 0; }
+        plan->C = target ? target : natural;
+        // zero-fill every block of the output layout
+        const Layout& CL = *plan->C;
+        std::vector<CBlockRec> cblk;
+        std::vector<int32_t> tab;
+        std::vector<ItemRec> items;
+        for (int c = 0; c < CL.nblocks(); ++c) {
+            CBlockRec r;
+            r.coff = CL.offs[c];
+            r.M = (int)CL.block_size(c); r.N = 1;
+            r.tcm = (int)tab.size();
+            for (int i = 0; i < r.M; ++i) tab.push_back(i);
+            r.tcn = (int)tab.size(); tab.push_back(0);
+            cblk.push_back(r);
+            for (int m0 = 0; m0 < r.M; m0 += GEMM_TILE) items.push_back(ItemRec{c, m0, 0, 0, 0});
+        }
+        size_t t_items = 0, t_cblk = align16(sizeof(ItemRec) * std::max<size_t>(1, items.size()));
+        size_t t_tab = align16(t_cblk + sizeof(CBlockRec) * std::max<size_t>(1, cblk.size()));
+        size_t tbytes = align16(t_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size()));
+        ctx.ensure_stage(tbytes);
+        char* st = static_cast<char*>(ctx.stage);
+        if (!items.empty()) std::memcpy(st + t_items, items.data(), sizeof(ItemRec) * items.size());
+        if (!cblk.empty()) std::memcpy(st + t_cblk, cblk.data(), sizeof(CBlockRec) * cblk.size());
+        if (!tab.empty()) std::memcpy(st + t_tab, tab.data(), sizeof(int32_t) * tab.size());
+        plan->dev = dev_alloc(tbytes, ctx.stream);
+        char* db = plan->dev->as<char>();
+        ITG_CHECK_CUDA(cudaMemcpyAsync(db, st, tbytes, cudaMemcpyHostToDevice, ctx.stream));
+        ctx.sync();
+        plan->d_items = reinterpret_cast<ItemRec*>(db + t_items);
+        plan->d_pairs = nullptr;
+        plan->d_cblk = reinterpret_cast<CBlockRec*>(db + t_cblk);
+        plan->d_tab = reinterpret_cast<int32_t*>(db + t_tab);
+        plan->nitems = (int)items.size();
+    }
+    plan->scalar = (rC == 0);
+    ctx.plans_built++;
+    if (ctx.plans.size() >= ctx.plan_cache_limit) ctx.plans.clear();
+    ctx.plans.emplace(std::move(key), plan);
+    return plan;
+}
+
+void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int prec) {
+    if (p.nitems == 0) return;
+    if (prec < 0) prec = ctx.precision;
+    ProfRec pr{};
+    if (ctx.profiling) {
+        ITG_CHECK_CUDA(cudaEventCreate(&pr.start));
+        ITG_CHECK_CUDA(cudaEventCreate(&pr.stop));
+        ITG_CHECK_CUDA(cudaEventRecord(pr.start, ctx.stream));
+        pr.flops = p.flops;
+        pr.nitems = p.nitems;
+        pr.kind = (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) ? 1 : 0;
+    }
+    // small-K contractions (the MPO-tensor steps) are bandwidth-shaped: FP64 is exact there
+    if (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) {
+        switch (ctx.ozaki_slices) {
+            case 3: gemm_ozaki_kernel<3><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C); break;
+            case 4: gemm_ozaki_kernel<4><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C); break;
+            case 5: gemm_ozaki_kernel<5><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C); break;
+            default: gemm_ozaki_kernel<6><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C); break;
+        }
+    } else if (prec == PREC_F64 || prec == PREC_OZAKI_BF16) {
+        gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+    } else {
+        throw Error(ERR_ARG, "contract: unsupported precision mode");
+    }
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches++;
+    ctx.flops_done += p.flops;
+    if (ctx.profiling) {
+        ITG_CHECK_CUDA(cudaEventRecord(pr.stop, ctx.stream));
+        ctx.prof.push_back(pr);
+    }
+}
+
+Tensor contract(Ctx& ctx, Tensor const& A, Tensor const& B, int prec, std::shared_ptr<Layout> target) {
+    ITG_REQUIRE(A.valid() && B.valid(), "contract: null tensor");
+    Match mt = match_indices(A.inds(), B.inds());
+    auto plan = get_plan(ctx, *A.lay, *B.lay, mt, target);
+    // plans are shared by every contraction of the same block structure: the
+    // output carries this contraction's own indices (or the caller's target)
+    std::shared_ptr<Layout> CL = target;
+    if (!CL) {
+        CL = std::make_shared<Layout>(*plan->C);
+        CL->inds.clear();
+        for (int i : mt.a_unc) CL->inds.push_back(A.inds()[i]);
+        for (int j : mt.b_unc) CL->inds.push_back(B.inds()[j]);
+    }
+    Tensor C(CL, ctx.stream);
+    exec_plan(ctx, *plan, A.data(), B.data(), C.data(), prec);
+    if (plan->scalar) {
+        double v = 0;
+        ITG_CHECK_CUDA(cudaMemcpyAsync(&v, C.data(), sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+        ctx.sync();
+        C.scalar = v;
+    }
+    return C;
+}
+
+}  // namespace itg

@@ -1,0 +1,104 @@
+// Two-site DMRG sweep loop on the device path: DMRGWorker
+// (itensor/mps/dmrg.h:336-467), sweepnext (itensor/mps/sweeps.h:489-503),
+// LocalMPO environments (itensor/mps/localmpo.h:443-618).
+#include "algo.h"
+#include <chrono>
+
+namespace itg {
+
+namespace {
+struct Environments {
+    std::vector<Tensor> const* W;
+    std::vector<Tensor> PH;   // PH[k]: sites 1..k (left) or k..N (right)
+    int N, LHlim, RHlim;
+    Environments(std::vector<Tensor> const& w) : W(&w), PH(w.size() + 2), N((int)w.size()), LHlim(0), RHlim((int)w.size() + 1) {}
+
+    Tensor grow(Ctx& ctx, Tensor const* E, Tensor const& A, Tensor const& Wn, int prec) {
+        Tensor T = E ? contract(ctx, *E, A, prec) : A;
+        T = contract(ctx, T, Wn, prec);
+        Tensor Ad = relabel(A, prime_all(dag_all(A.inds())));
+        return contract(ctx, T, Ad, prec);
+    }
+    void makeL(Ctx& ctx, std::vector<Tensor> const& psi, int k, int prec) {
+        while (LHlim < k) {
+            int ll = LHlim;
+            PH[ll + 1] = grow(ctx, PH[ll].valid() ? &PH[ll] : nullptr, psi[ll], (*W)[ll], prec);
+            LHlim = ll + 1;
+        }
+    }
+    void makeR(Ctx& ctx, std::vector<Tensor> const& psi, int k, int prec) {
+        while (RHlim > k) {
+            int rl = RHlim;
+            PH[rl - 1] = grow(ctx, PH[rl].valid() ? &PH[rl] : nullptr, psi[rl - 2], (*W)[rl - 2], prec);
+            RHlim = rl - 1;
+        }
+    }
+    LocalOp position(Ctx& ctx, int b, std::vector<Tensor> const& psi, int prec) {
+        makeL(ctx, psi, b - 1, prec);
+        makeR(ctx, psi, b + 2, prec);
+        LHlim = b - 1;
+        RHlim = b + 2;
+        LocalOp op;
+        op.L = (b - 1 >= 1) ? &PH[b - 1] : nullptr;
+        op.R = (b + 2 <= N) ? &PH[b + 2] : nullptr;
+        op.W1 = &(*W)[b - 1];
+        op.W2 = &(*W)[b];
+        return op;
+    }
+};
+}  // namespace
+
+DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<SweepSpec> const& sweeps, int prec) {
+    const int N = (int)psi.size();
+    ITG_REQUIRE(N >= 2 && (int)H.W.size() == N, "dmrg: MPO and MPS lengths differ");
+    Environments env(H.W);
+    DmrgResult res;
+    double energy = 0;
+    for (size_t sw = 0; sw < sweeps.size(); ++sw) {
+        auto t0 = std::chrono::steady_clock::now();
+        SweepSpec const& s = sweeps[sw];
+        for (int b = 1, ha = 1; ha <= 2;) {
+          try {
+            LocalOp op = env.position(ctx, b, psi, prec);
+            // phi on every block of its divergence, so H_eff and Davidson work on flat vectors
+            Tensor const& A = psi[b - 1];
+            Tensor const& B = psi[b];
+            Match mt = match_indices(A.inds(), B.inds());
+            std::vector<Index> pinds;
+            for (int i : mt.a_unc) pinds.push_back(A.inds()[i]);
+            for (int j : mt.b_unc) pinds.push_back(B.inds()[j]);
+            auto full = std::make_shared<Layout>(allowed_layout(pinds, tensor_div(A) + tensor_div(B)));
+            Tensor phi = contract(ctx, A, B, prec, full);
+            energy = davidson(ctx, op, phi, s.niter, 1e-14, 1, prec, &res.heff_applies);
+            SplitArgs sa;
+            sa.cutoff = s.cutoff;
+            sa.maxdim = s.maxdim;
+            sa.mindim = s.mindim;
+            sa.respect_degenerate = true;
+            sa.normalize = true;
+            SplitResult sr = denmat_decomp(ctx, phi, A, B, ha == 1, sa, prec);
+            psi[b - 1] = sr.A;
+            psi[b] = sr.B;
+            res.bonds.push_back(BondRecord{(int)sw + 1, ha, b, energy, sr.truncerr, (long)sr.link.dim()});
+          } catch (Error const& e) {
+            throw Error(e.code, std::string(e.what()) + " [sweep " + std::to_string(sw + 1) + ", half-sweep " +
+                                    std::to_string(ha) + ", bond " + std::to_string(b) + "]");
+          }
+            // sweepnext: b = 1..N-1, then N-1..1
+            const int inc = (ha == 1) ? 1 : -1;
+            b += inc;
+            if (b == (ha == 1 ? N : 0)) { b -= inc; ++ha; }
+        }
+        ctx.sync();
+        res.sweep_seconds.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+    }
+    res.energy = energy;
+    for (int b = 0; b + 1 < N; ++b) {
+        Match mt = match_indices(psi[b].inds(), psi[b + 1].inds());
+        ITG_REQUIRE(!mt.a_con.empty(), "dmrg: neighbouring tensors share no link");
+        res.links.push_back(psi[b].inds()[mt.a_con[0]]);
+    }
+    return res;
+}
+
+}  // namespace itg

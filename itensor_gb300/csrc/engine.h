@@ -1,0 +1,124 @@
+// Contraction engine and per-context state.
+//
+// A contraction C = A*B of block-sparse tensors runs in two phases:
+//   plan  -- block-pair matching, output-block set and offsets, computed on
+//            the device (planner kernel), then the GEMM work tables;
+//            cached by block structure so repeated applies (Davidson) reuse it;
+//   exec  -- one grouped launch over all output tiles: every output tile walks
+//            the block pairs that feed its block, so each output element is
+//            written once (no atomics, deterministic order).
+// Reference: doTask(Contract,QDense,QDense) itensor/itdata/qdense.cc:671-743,
+// getContractedOffsets itensor/itdata/qutil.h:93-242,
+// loopContractedBlocks itensor/itdata/qutil.h:244-371,
+// contract(CProps,...) itensor/tensor/contract.cc:733-824.
+#pragma once
+#include "tensor.h"
+#include <mutex>
+
+namespace itg {
+
+struct PairRec {          // one (A block, B block) product feeding an output block
+    int64_t aoff, boff;   // element offsets of the two blocks
+    int32_t tam, tak;     // table positions: A offsets along m and along k
+    int32_t tbk, tbn;     // table positions: B offsets along k and along n
+    int32_t K;            // contracted extent
+    int32_t pad;
+};
+struct CBlockRec {        // output block
+    int64_t coff;
+    int32_t tcm, tcn;     // table positions: C offsets along m and along n
+    int32_t M, N;
+};
+struct ItemRec {          // one output tile (TILE x TILE) of one output block
+    int32_t c, m0, n0, p0, p1;
+};
+
+constexpr int GEMM_TILE = 32;
+
+struct Plan {
+    std::shared_ptr<Layout> C;       // output layout
+    DevBufPtr dev;                   // packed device tables
+    ItemRec* d_items = nullptr;
+    PairRec* d_pairs = nullptr;
+    CBlockRec* d_cblk = nullptr;
+    int32_t* d_tab = nullptr;
+    int nitems = 0, npairs = 0, ncblk = 0;
+    double flops = 0;                // sum over block pairs of 2*M*N*K
+    int64_t bytes_ab = 0;            // elements of A and B blocks touched
+    int maxK = 0;                    // largest summed K of one output block
+    double avgK = 0;
+    bool scalar = false;             // rank-0 result
+};
+
+struct ProfRec {          // one timed GEMM launch (profiling mode)
+    cudaEvent_t start, stop;
+    double flops;
+    int kind;             // 0 FP64, 1 Ozaki BF16
+    int nitems;
+};
+
+struct Ctx {
+    int device = 0;
+    bool profiling = false;
+    std::vector<ProfRec> prof;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    // host-mapped pinned buffer the planner kernel writes its result into
+    void* pin = nullptr;
+    void* pin_dev = nullptr;
+    size_t pin_bytes = 0;
+    // pinned staging buffer for host->device table uploads
+    void* stage = nullptr;
+    size_t stage_bytes = 0;
+    std::unordered_map<std::string, std::shared_ptr<Plan>> plans;
+    size_t plan_cache_limit = 4096;
+    // counters
+    uint64_t kernel_launches = 0;
+    uint64_t plans_built = 0, plan_hits = 0;
+    double flops_done = 0;
+    int precision = PREC_F64;
+    int ozaki_slices = 6;
+    int sm_count = 152;
+
+    explicit Ctx(int dev);
+    ~Ctx();
+    void ensure_pin(size_t bytes);
+    void ensure_stage(size_t bytes);
+    void sync() { ITG_CHECK_CUDA(cudaStreamSynchronize(stream)); }
+};
+
+// Labels: which A index matches which B index (ITensor computeLabels semantics).
+struct Match {
+    std::vector<int> a_con, b_con;   // contracted positions, in A's order
+    std::vector<int> a_unc, b_unc;   // uncontracted positions
+};
+Match match_indices(std::vector<Index> const& A, std::vector<Index> const& B);
+
+// Builds (or fetches from the cache) the plan for C = A*B. If `target` is
+// given, C is produced in that layout (any index order, any superset of the
+// produced blocks; blocks with no contributing pair are written as zeros).
+std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match const& mt,
+                               std::shared_ptr<Layout> target = nullptr);
+// Runs a plan: C = A*B with the given arithmetic.
+void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int prec);
+
+// ITensor operator*: contracts every index common to A and B.
+Tensor contract(Ctx& ctx, Tensor const& A, Tensor const& B, int prec = -1,
+                std::shared_ptr<Layout> target = nullptr);
+
+// ---- kernels launched from other translation units (ops.cu)
+void launch_fill(Ctx& ctx, double* x, int64_t n, double v);
+void launch_scale(Ctx& ctx, double* x, int64_t n, double a);
+void launch_axpy(Ctx& ctx, double* y, double const* x, int64_t n, double a);          // y += a x
+void launch_axpby(Ctx& ctx, double* y, double const* x, int64_t n, double a, double b); // y = a x + b y
+// dot products of x with each of nv vectors V[k] (device pointers); result to host
+void dots(Ctx& ctx, double const* const* V, int nv, double const* x, int64_t n, double* out);
+double dot(Ctx& ctx, double const* a, double const* b, int64_t n);
+double norm(Ctx& ctx, double const* a, int64_t n);
+// General block permute / gather: dst[dst_off[e]] = src[src_off[e]] described per
+// block by offset tables (see ops.cu). Used for combiner, uncombine and
+// layout changes.
+struct GatherPlan;
+void launch_gather(Ctx& ctx, GatherPlan const& g, double const* src, double* dst);
+
+}  // namespace itg

@@ -1,0 +1,43 @@
+// Gather plans and the batched eigensolver interface (kernels in ops.cu).
+#pragma once
+#include "engine.h"
+
+namespace itg {
+
+struct GatherItem {
+    int64_t soff, doff;
+    int32_t n1, n2;        // element grid n1 x n2 (n1 fastest)
+    int32_t ts1, ts2;      // table positions of source offsets along 1 and 2
+    int32_t td1, td2;      // table positions of destination offsets along 1 and 2
+};
+
+struct GatherPlan {
+    std::vector<GatherItem> items;
+    std::vector<int32_t> tab;
+    DevBufPtr dev;
+    GatherItem* d_items = nullptr;
+    int32_t* d_tab = nullptr;
+    int nitems = 0;
+    int32_t add_table(std::vector<int32_t> const& t) {
+        int32_t p = (int32_t)tab.size();
+        tab.insert(tab.end(), t.begin(), t.end());
+        return p;
+    }
+    void upload(Ctx& ctx);
+};
+
+// One symmetric n x n matrix (column-major) to diagonalise.
+struct EigItem {
+    int64_t a_off;   // input matrix in the source buffer
+    int64_t v_off;   // eigenvectors (columns, eigenvalues descending) in the output buffer
+    int64_t w_off;   // eigenvalues (descending) in the output buffer
+    int64_t s_off;   // 2 n^2 doubles of scratch
+    int32_t n;
+    int32_t pad;
+};
+
+// Diagonalises every item; returns the number of items that hit the sweep cap.
+int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
+                 double* scratch);
+
+}  // namespace itg

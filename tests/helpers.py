@@ -41,3 +41,56 @@ def model_from_json(m, N):
     if t == "hubbard":
         return models.hubbard(m["Lx"], m["Ly"], m["t"], m["U"], m.get("yperiodic", False)), neel
     raise ValueError(t)
+
+
+# ---------------------------------------------------------------- fixtures -> device tensors
+def qn_names(obj, acc=None):
+    """All QN names appearing in a fixture (sorted), used as the slot order."""
+    if acc is None:
+        acc = set()
+    if isinstance(obj, dict):
+        if "sectors" in obj and "id" in obj:
+            for q, _ in obj["sectors"]:
+                for name, _, _ in q:
+                    acc.add(name)
+        for v in obj.values():
+            qn_names(v, acc)
+    elif isinstance(obj, list):
+        for v in obj:
+            qn_names(v, acc)
+    return sorted(acc)
+
+
+def gpu_index(j, names):
+    import itensor_gb300 as itg
+    qns, mods = [], [0, 0, 0, 0]
+    for q, d in j["sectors"]:
+        row = [0, 0, 0, 0]
+        for name, v, m in q:
+            k = names.index(name)
+            row[k] = v
+            mods[k] = m
+        qns.append(row)
+    for k in range(len(names)):
+        if mods[k] == 0:
+            mods[k] = 1
+    return itg.Index(int(j["id"]), j["plev"], j["dir"], qns, [d for _, d in j["sectors"]], mods)
+
+
+def gpu_tensor(ctx, j, names):
+    inds = [gpu_index(x, names) for x in j["inds"]]
+    if not inds:
+        data = j.get("data") or [j.get("scalar", 0.0)]
+        return ctx.tensor([], [], np.asarray(data, np.float64))
+    return ctx.tensor(inds, np.asarray(j["blocks"], np.int32).reshape(-1), np.asarray(j["data"], np.float64))
+
+
+def gpu_layout_matches(t, refj):
+    """(same index order/ids, same blocks+offsets) of a device tensor against a fixture tensor."""
+    inds = t.inds
+    same_inds = [(I.id, I.plev, I.dir) for I in inds] == [(int(x["id"]), x["plev"], x["dir"]) for x in refj["inds"]]
+    coords, offs = t.blocks()
+    rb = np.asarray(refj["blocks"], np.int64).reshape(len(refj["blocks"]), -1) if refj["blocks"] else np.zeros((0, len(inds)))
+    same_blocks = coords.shape[0] == rb.shape[0] and np.array_equal(coords.reshape(rb.shape), rb) and \
+        list(offs) == list(refj["offsets"])
+    return same_inds, same_blocks

@@ -1,0 +1,197 @@
+"""Parity of the sm_103a path (called through the C-ABI) with the reference's
+golden fixtures and with the CPU oracle. GPU only.
+
+Tolerances: contractions 1e-12 relative to the largest output entry; DMRG
+energies 1e-10; truncation errors 1e-12; kept dimensions and QN layouts exact.
+"""
+import numpy as np
+import pytest
+
+from helpers import (T, gpu_tensor, gpu_layout_matches, qn_names, json_sectors, model_from_json)
+
+pytestmark = pytest.mark.gpu
+
+CONTRACT_RTOL = 1e-12
+ENERGY_TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import itensor_gb300 as itg
+    import itensor_gb300.build as b
+    b.build()
+    c = itg.Context(0)
+    yield c
+    c.close()
+
+
+def _relerr(x, ref):
+    ref = np.asarray(ref, np.float64)
+    if ref.size == 0:
+        return 0.0
+    return float(np.max(np.abs(np.asarray(x) - ref)) / max(1.0, np.max(np.abs(ref))))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_contract_golden(ctx, golden, prec):
+    d = golden("contract")
+    names = qn_names(d)
+    for c in d["cases"]:
+        A, B = gpu_tensor(ctx, c["A"], names), gpu_tensor(ctx, c["B"], names)
+        Cg = ctx.contract(A, B, precision=prec)
+        ref = c["C"]
+        # split form: ~2^-42 of row/column maxima per product (6 BF16 slices)
+        tol = CONTRACT_RTOL if prec == 0 else 1e-11
+        if not ref["inds"]:
+            val = ref["data"][0] if ref.get("data") else ref.get("scalar", 0.0)
+            assert abs(Cg.scalar() - val) <= tol * max(1, abs(val)), c["name"]
+            continue
+        same_inds, same_blocks = gpu_layout_matches(Cg, ref)
+        assert same_inds and same_blocks, c["name"]
+        assert _relerr(Cg.numpy(), ref["data"]) <= tol, c["name"]
+
+
+def test_plan_exec_raw_boundary(ctx, golden):
+    """itg_contract_plan/itg_contract_exec: layouts + Lind/Rind labels + device pointers."""
+    d = golden("contract")
+    names = qn_names(d)
+    c = [x for x in d["cases"] if x["name"] == "perm2"][0]
+    A, B = gpu_tensor(ctx, c["A"], names), gpu_tensor(ctx, c["B"], names)
+    ia = [(int(x["id"]), x["plev"]) for x in c["A"]["inds"]]
+    ib = [(int(x["id"]), x["plev"]) for x in c["B"]["inds"]]
+    la, lb = [], []
+    nxt = 1
+    for k in ia:
+        if k in ib:
+            la.append(-(ib.index(k) + 1))
+        else:
+            la.append(nxt); nxt += 1
+    for k in ib:
+        lb.append(-(ib.index(k) + 1) if k in ia else 100 + len(lb))
+    dimsA = [[s[1] for s in x["sectors"]] for x in c["A"]["inds"]]
+    dimsB = [[s[1] for s in x["sectors"]] for x in c["B"]["inds"]]
+    plan = ctx.plan((dimsA, c["A"]["blocks"]), la, (dimsB, c["B"]["blocks"]), lb)
+    coords, offs, size = plan.output()
+    assert coords.tolist() == c["C"]["blocks"]
+    assert offs.tolist() == c["C"]["offsets"]
+    import itensor_gb300 as itg
+    out = ctx.tensor(gpu_tensor(ctx, c["C"], names).inds, np.asarray(c["C"]["blocks"], np.int32).reshape(-1))
+    ctx.contract_exec(plan, A.device_ptr(), B.device_ptr(), out.device_ptr(), precision=itg.PREC_F64)
+    assert _relerr(out.numpy(), c["C"]["data"]) <= CONTRACT_RTOL
+
+
+def _op(ctx, c, names):
+    L = gpu_tensor(ctx, c["L"], names) if c["L"]["inds"] else None
+    R = gpu_tensor(ctx, c["R"], names) if c["R"]["inds"] else None
+    return L, gpu_tensor(ctx, c["W1"], names), gpu_tensor(ctx, c["W2"], names), R
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_heff_golden(ctx, golden, prec):
+    d = golden("heff")
+    names = qn_names(d)
+    for c in d["cases"]:
+        if "Hphi" not in c:
+            continue
+        L, W1, W2, R = _op(ctx, c, names)
+        phi = gpu_tensor(ctx, c["phi"], names)
+        out = ctx.heff_apply(L, W1, W2, R, phi, precision=prec)
+        same_inds, same_blocks = gpu_layout_matches(out, c["Hphi"])
+        assert same_inds and same_blocks, c["name"]
+        assert _relerr(out.numpy(), c["Hphi"]["data"]) <= (CONTRACT_RTOL if prec == 0 else 1e-11), c["name"]
+
+
+def test_davidson_golden(ctx, golden):
+    d = golden("heff")
+    names = qn_names(d)
+    for c in d["cases"]:
+        for key, mi in (("davidson_niter2", 2), ("davidson_niter9", 9)):
+            if key not in c:
+                continue
+            L, W1, W2, R = _op(ctx, c, names)
+            phi = gpu_tensor(ctx, c["phi"], names)
+            e, v = ctx.davidson(L, W1, W2, R, phi, maxiter=mi)
+            assert abs(e - c[key]["energy"]) < 1e-12, (c["name"], key, e)
+            # compare the Ritz vector on the reference's blocks (others are zero)
+            ref = T(c[key]["phi"])
+            coords, offs = v.blocks()
+            data = v.numpy()
+            got = {tuple(cc): data[o:o + int(np.prod(ref.block_shape(tuple(cc))))] for cc, o in zip(coords.tolist(), offs)}
+            for cc, blk in ref.blocks.items():
+                assert np.max(np.abs(got[cc] - blk.reshape(-1, order="F"))) < 1e-10
+    # reference unit value: 4-site Heisenberg, E = -0.95710678118
+    c = [x for x in d["cases"] if x["name"] == "heis4_b2"][0]
+    L, W1, W2, R = _op(ctx, c, names)
+    e, _ = ctx.davidson(L, W1, W2, R, gpu_tensor(ctx, c["phi"], names), maxiter=9)
+    assert abs(e + 0.95710678118) < 1e-10
+
+
+def test_denmat_golden(ctx, golden):
+    from oracle.blocksparse import contract as ocontract
+    d = golden("bondsplit")
+    names = qn_names(d)
+    for c in d["cases"]:
+        if c["usesvd"]:
+            continue
+        AA, A, B = (gpu_tensor(ctx, c[k], names) for k in ("AA", "A", "B"))
+        Ao, Bo, eigs, te = ctx.denmat_decomp(AA, A, B, c["fromleft"], c["cutoff"], c["maxdim"], c["mindim"],
+                                             normalize=False)
+        e = np.asarray(c["spec"]["eigs"])
+        assert len(eigs) == len(e), c["name"]
+        assert np.max(np.abs(eigs - e)) < 1e-12 * max(1.0, e[0]), c["name"]
+        assert abs(te - c["spec"]["truncerr"]) < 1e-12 * max(1.0, e[0])
+        link = [I for I in Ao.inds if any(I.same(J) for J in Bo.inds)][0]
+        ref_secs = json_sectors(c["link"])
+        assert [int(x) for x in link.dims] == [dd for _, dd in ref_secs], c["name"]
+        assert link.dir == c["link"]["dir"]
+        # A*B reconstructs the reference's (gauge-free) product
+        AB = ctx.contract(Ao, Bo)
+        from helpers import layout_and_maxerr
+        from oracle.blocksparse import BSTensor
+        ref = T(c["AB"])
+        coords, offs = AB.blocks()
+        inds_map = [[(int(x["id"]), x["plev"]) for x in c["AB"]["inds"]].index((I.id, I.plev)) for I in AB.inds]
+        data = AB.numpy()
+        for cc, o in zip(coords.tolist(), offs):
+            rc = [0] * len(cc)
+            for k, p in enumerate(inds_map):
+                rc[p] = cc[k]
+            blk_ref = ref.blocks.get(tuple(rc))
+            shp = tuple(int(AB.inds[k].dims[cc[k]]) for k in range(len(cc)))
+            blk = data[o:o + int(np.prod(shp))].reshape(shp, order="F")
+            if blk_ref is None:
+                assert np.max(np.abs(blk)) < 1e-12
+            else:
+                assert np.max(np.abs(np.transpose(blk_ref, inds_map) - blk)) < 1e-11 * max(1, np.abs(ref.flat()).max())
+
+
+@pytest.mark.parametrize("name", ["heis20", "xxz16", "j1j2_16", "tfi16", "hubbard8", "hubbard4x2"])
+def test_dmrg_golden(ctx, golden, name):
+    c = [x for x in golden("dmrg")["cases"] if x["name"] == name][0]
+    m = c["model"]
+    if m["type"] in ("heisenberg", "xxz"):
+        model = dict(type=0, N=c["N"], J=m["J"], Jz=m["Jz"])
+    elif m["type"] == "j1j2":
+        model = dict(type=0, N=c["N"], J=1.0, Jz=1.0, J2=m["J2"])
+    elif m["type"] == "tfi":
+        model = dict(type=1, N=c["N"], h=m["h"])
+    else:
+        model = dict(type=2, Lx=m["Lx"], Ly=m["Ly"], t=m["t"], U=m["U"], yperiodic=int(m.get("yperiodic", False)))
+    res = ctx.dmrg(model, c["sweeps"], precision=0)
+    assert abs(res.energy - c["energy"]) < ENERGY_TOL
+    assert len(res.bonds) == len(c["bonds"])
+    for a, b in zip(res.bonds, c["bonds"]):
+        assert tuple(a[:3]) == tuple(b[:3])
+        assert abs(a[3] - b[3]) < ENERGY_TOL, (a, b)
+        assert abs(a[4] - b[4]) < 1e-12
+        assert a[5] == b[5]
+    for (dr, qn, dims), ref in zip(res.links, c["links"]):
+        assert [int(x) for x in dims] == [d for _, d in ref["sectors"]]
+        assert dr == ref["dir"]
+
+
+def test_dmrg_ozaki_energy_within_1e9(ctx, golden):
+    """Split-precision block GEMMs (6 BF16 slices) keep |dE| <= 1e-9 on the N=20 chain."""
+    c = [x for x in golden("dmrg")["cases"] if x["name"] == "heis20"][0]
+    res = ctx.dmrg(dict(type=0, N=20, J=1.0, Jz=1.0), c["sweeps"], precision=1)
+    assert abs(res.energy - c["energy"]) <= 1e-9
