@@ -225,6 +225,27 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+def run_profile(args):
+    """Short run of the same workload for ncu: for the split form and plain
+    FP64, N prepared applies each (kernels launched one by one)."""
+    import torch
+    import itensor_gb300 as itg
+    from itensor_gb300 import workloads
+    ctx = itg.Context(0)
+    ctx.set_precision(itg.PREC_OZAKI_BF16, args.slices)
+    wl = workloads.heff_workload(M_BOND, K_SECT, SIGMA, SEED)
+    dev = {k: workloads.to_device(ctx, wl[k]) for k in ("psi", "L", "W1", "W2", "R")}
+    for prec in (itg.PREC_OZAKI_BF16, itg.PREC_F64):
+        h = ctx.heff_prepare(dev["L"], dev["W1"], dev["W2"], dev["R"], dev["psi"], precision=prec, use_graph=False)
+        out = torch.empty(h.out_size, dtype=torch.float64, device="cuda")
+        for _ in range(args.profile):
+            h.run(dev["psi"].device_ptr(), out.data_ptr())
+        ctx.sync()
+    ctx.close()
+    print("profile run done")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -234,9 +255,13 @@ def main():
     ap.add_argument("--slices", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-dmrg", action="store_true")
+    ap.add_argument("--profile", type=int, default=0,
+                    help="profiling run for ncu: N prepared applies per arithmetic, no graph, no timing")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile:
+        return run_profile(args)
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
 
@@ -271,10 +296,18 @@ def main():
     dom = max(range(len(prof)), key=lambda i: prof[i][1])  # biggest contraction (psi * L step)
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    # prepared applies (plans resolved once); graph replay for the timed value,
+    # per-launch events (no graph) for the kernel roofline
+    H = {(prec, g): ctx.heff_prepare(L, W1, W2, R, psi, precision=prec, use_graph=g)
+         for prec in (itg.PREC_OZAKI_BF16, itg.PREC_F64) for g in (True, False)}
+    out_n = H[(itg.PREC_F64, True)].out_size
+    outbuf = torch.empty(out_n, dtype=torch.float64, device="cuda")
+    psi_ptr, out_ptr = psi.device_ptr(), outbuf.data_ptr()
 
-    def timed(prec, steps, warmup, profile=False):
+    def timed(prec, steps, warmup, graph=True, profile=False):
+        h = H[(prec, graph)]
         for _ in range(warmup):
-            ctx.heff_apply(L, W1, W2, R, psi, precision=prec)
+            h.run(psi_ptr, out_ptr)
         ctx.sync()
         if dist:
             dist.barrier()
@@ -288,7 +321,7 @@ def main():
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(ext)
-            ctx.heff_apply(L, W1, W2, R, psi, precision=prec)
+            h.run(psi_ptr, out_ptr)
             e1.record(ext)
             e1.synchronize()
             tot += e0.elapsed_time(e1)
@@ -303,14 +336,18 @@ def main():
 
     clocks = ClockSampler(local)
     clocks.start()
-    t_oz, launches, prof_oz = timed(itg.PREC_OZAKI_BF16, args.steps, args.warmup, profile=True)
+    t_oz, launches, _ = timed(itg.PREC_OZAKI_BF16, args.steps, args.warmup, graph=True)
     clk = clocks.stop()
-    t_64, _, prof_64 = timed(itg.PREC_F64, max(3, args.steps // 3), 2, profile=True)
+    n64 = max(3, args.steps // 3)
+    t_64, _, _ = timed(itg.PREC_F64, n64, 2, graph=True)
+    # kernel-level pass: same steps, launches timed one by one
+    t_ozp, _, prof_oz = timed(itg.PREC_OZAKI_BF16, args.steps, 2, graph=False, profile=True)
+    t_64p, _, prof_64 = timed(itg.PREC_F64, n64, 2, graph=False, profile=True)
 
     value = flops_apply * args.steps * world / (t_oz / 1e3) / 1e12
-    f64_value = flops_apply * max(3, args.steps // 3) / (t_64 / 1e3) / 1e12
+    f64_value = flops_apply * n64 / (t_64 / 1e3) / 1e12
 
-    # roofline of the dominant kernel (psi * L block GEMM), averaged over the timed launches
+    # roofline of the dominant kernel (the psi*L block GEMM), averaged over the pass
     def dom_stats(pr):
         per = len(prof)
         ms = [pr[i][0] for i in range(dom, len(pr), per)]
@@ -319,35 +356,49 @@ def main():
     peaks, peak_src = measured_peaks()
     dm_ms, dm_flops, dm_kind = dom_stats(prof_oz)
     achieved = dm_flops / (dm_ms / 1e3) / 1e12
+    nsl = args.slices * (args.slices + 1) // 2
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": achieved / peaks["bf16_tflops"], "traffic": None,
-                "kernel": "gemm_ozaki_kernel<%d> (psi*L block GEMM)" % args.slices,
-                "note": "achieved = algorithmic FP64-equivalent flops of the launch / its CUDA-event duration; "
-                        "peak = dense BF16 burst of %s; the kernel issues %d BF16 slice products per FP64 "
+                "kernel": "ozaki_prep<%d> x2 + gemm_ozaki_kernel<%d> (psi*L block GEMM)" % (args.slices, args.slices),
+                "note": "achieved = algorithmic FP64-equivalent flops of the psi*L contraction / CUDA-event duration "
+                        "of its launches (per-launch events, same steps as the timed region without graph replay); "
+                        "peak = dense BF16 burst of %s (of %s); the kernel issues %d BF16 digit products per FP64 "
                         "product" % ("MEASURED_PEAKS.json" if peak_src == "measured" else "the fallback",
-                                     args.slices * (args.slices + 1) // 2),
-                "slice_tflops": achieved * args.slices * (args.slices + 1) / 2}
+                                     peak_src, nsl),
+                "digit_product_tflops": achieved * nsl, "digit_product_frac": achieved * nsl / peaks["bf16_tflops"]}
     d64_ms, d64_flops, _ = dom_stats(prof_64)
 
-    # end-to-end through the public API: host psi -> device, apply, result -> host
+    # end-to-end through the C-ABI with host buffers: psi host -> device, apply, result -> host
     psi_host = np.ascontiguousarray(wl["psi"]["data"])
-    inds = psi.inds
-    coords = wl["psi"]["coords"].reshape(-1)
-    out_n = len(oz)
+    out_host = np.empty(out_n)
+    he = H[(itg.PREC_OZAKI_BF16, True)]
     e2e_t = 0.0
     for i in range(args.warmup + args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        p = ctx.tensor(inds, coords, psi_host)
-        o = ctx.heff_apply(L, W1, W2, R, p, precision=itg.PREC_OZAKI_BF16).numpy()
+        he.run_host(psi_host, out_host)
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             e2e_t += dt
+    # the unprepared public call: tensor from host data + itg_heff_apply + read back
+    inds = psi.inds
+    coords = wl["psi"]["coords"].reshape(-1)
+    e2u_t = 0.0
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        p = ctx.tensor(inds, coords, psi_host)
+        ctx.heff_apply(L, W1, W2, R, p, precision=itg.PREC_OZAKI_BF16).numpy()
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2u_t += dt
     e2e = {"value": flops_apply * args.steps / e2e_t / 1e12, "unit": UNIT,
            "h2d_bytes_per_step": int(8 * psi_host.size), "d2h_bytes_per_step": int(8 * out_n),
-           "ms_per_step": e2e_t / args.steps * 1e3, "api": "itg_tensor_create(host data) + itg_heff_apply + "
-                                                             "itg_tensor_read"}
+           "ms_per_step": e2e_t / args.steps * 1e3,
+           "api": "itg_heff_run(host=1): host psi -> device, graph-replayed apply, result -> host",
+           "unprepared_call": {"value": flops_apply * args.steps / e2u_t / 1e12,
+                               "ms_per_step": e2u_t / args.steps * 1e3,
+                               "api": "itg_tensor_create(host data) + itg_heff_apply + itg_tensor_read"}}
 
     # DMRG sweep time: N=20 Heisenberg chain (5 sweeps), plain FP64 and split form
     dmrg = None
@@ -380,7 +431,7 @@ def main():
                 "data": "synthetic (seeded N(0,1) blocks of the stated shape)", "config": CONFIG,
                 "algorithmic_gflop_per_apply": flops_apply / 1e9,
                 "split_vs_f64_max_rel_err": rel,
-                "f64_path": {"value": f64_value, "unit": UNIT, "ms_per_step": t_64 / max(3, args.steps // 3),
+                "f64_path": {"value": f64_value, "unit": UNIT, "ms_per_step": t_64 / n64,
                              "dominant_kernel_ms": d64_ms,
                              "dominant_kernel_tflops": d64_flops / (d64_ms / 1e3) / 1e12},
                 "speedup_split_over_f64": value / f64_value,

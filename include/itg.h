@@ -76,6 +76,9 @@ void* itg_stream(itg_ctx* ctx);
  * stream) between begin and end: n launches (capacity *n on input), their
  * durations in ms, algorithmic flops (sum of 2MNK) and arithmetic kind
  * (0 FP64, 1 Ozaki BF16). */
+/* Issue-rate microbenchmarks (register-only loops, ~0.3 s): TFLOP/s of
+ * [FP64 FFMA, FP32 FFMA, FP64 mma.sync, TF32 mma.sync, BF16 mma.sync]. */
+int itg_measure_peaks(itg_ctx* ctx, double* tflops5);
 int itg_profile_begin(itg_ctx* ctx);
 int itg_profile_end(itg_ctx* ctx, int32_t* n, float* ms, double* flops, int32_t* kind);
 
@@ -130,6 +133,20 @@ void itg_plan_free(itg_plan* plan);
  * the reference produces. */
 int itg_heff_apply(itg_ctx* ctx, const itg_tensor* L, const itg_tensor* W1, const itg_tensor* W2, const itg_tensor* R,
                    const itg_tensor* phi, int precision, itg_tensor** out);
+
+/* Prepared H_eff for repeated applies with one (L, W1, W2, R) and one phi
+ * block structure: plans resolved once, intermediates preallocated, and with
+ * use_graph != 0 the launches replayed as one CUDA graph. out_size receives
+ * the number of output elements (the output has the structure itg_heff_apply
+ * returns). itg_heff_run reads phi and writes the result through the given
+ * pointers; host != 0 means they are host memory (the copies are part of the
+ * call, which then returns after the result is written). */
+typedef struct itg_heff itg_heff;
+int itg_heff_create(itg_ctx* ctx, const itg_tensor* L, const itg_tensor* W1, const itg_tensor* W2, const itg_tensor* R,
+                    const itg_tensor* phi, int precision, int use_graph, itg_heff** out, int64_t* out_size,
+                    double* flops);
+int itg_heff_run(itg_ctx* ctx, itg_heff* h, const double* phi, double* out, int host);
+void itg_heff_free(itg_heff* h);
 
 /* davidson (block size 1), itensor/iterativesolvers.h:99-451. Returns the
  * lowest Ritz value and the normalised Ritz vector (on every block of phi's

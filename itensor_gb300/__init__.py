@@ -58,6 +58,7 @@ SIGNATURES = {
     "itg_stats": (C.c_int, [C.c_void_p, _u64p, _f64p, _u64p, _u64p]),
     "itg_reset_stats": (C.c_int, [C.c_void_p]),
     "itg_stream": (C.c_void_p, [C.c_void_p]),
+    "itg_measure_peaks": (C.c_int, [C.c_void_p, _f64p]),
     "itg_profile_begin": (C.c_int, [C.c_void_p]),
     "itg_profile_end": (C.c_int, [C.c_void_p, _i32p, C.POINTER(C.c_float), _f64p, _i32p]),
     "itg_tensor_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(IndexDesc), C.c_int32, _i32p, C.c_void_p,
@@ -79,6 +80,10 @@ SIGNATURES = {
     "itg_plan_free": (None, [C.c_void_p]),
     "itg_heff_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                  C.POINTER(C.c_void_p)]),
+    "itg_heff_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                  C.c_int, C.POINTER(C.c_void_p), _i64p, _f64p]),
+    "itg_heff_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "itg_heff_free": (None, [C.c_void_p]),
     "itg_davidson": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                C.c_double, C.c_int, _f64p, C.POINTER(C.c_void_p)]),
     "itg_denmat_decomp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int32,
@@ -234,6 +239,31 @@ class Plan:
         return f.value
 
 
+class Heff:
+    """Prepared H_eff apply (itg_heff_create / itg_heff_run)."""
+
+    def __init__(self, ctx, handle, out_size, flops):
+        self.ctx, self.h, self.out_size, self.flops = ctx, handle, out_size, flops
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.itg_heff_free(self.h)
+            self.h = C.c_void_p(None)
+
+    def run(self, phi_ptr, out_ptr):
+        """Device pointers in, device pointers out (asynchronous on the context stream)."""
+        self.ctx._ok(lib().itg_heff_run(self.ctx.h, self.h, C.c_void_p(phi_ptr), C.c_void_p(out_ptr), 0), self.ctx.h)
+
+    def run_host(self, phi, out=None):
+        """Host numpy in, host numpy out (copies included; returns when done)."""
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        if out is None:
+            out = np.empty(self.out_size)
+        self.ctx._ok(lib().itg_heff_run(self.ctx.h, self.h, phi.ctypes.data_as(C.c_void_p),
+                                        out.ctypes.data_as(C.c_void_p), 1), self.ctx.h)
+        return out
+
+
 class DmrgResult:
     def __init__(self, energy, bonds, links, sweep_seconds, heff_applies):
         self.energy = energy
@@ -283,6 +313,13 @@ class Context:
         a, f, b, c = C.c_uint64(), C.c_double(), C.c_uint64(), C.c_uint64()
         self._ok(lib().itg_stats(self.h, C.byref(a), C.byref(f), C.byref(b), C.byref(c)), self.h)
         return {"kernel_launches": a.value, "gemm_flops": f.value, "plans_built": b.value, "plan_hits": c.value}
+
+    def measure_peaks(self):
+        """Issue-rate microbenchmarks: dict of TFLOP/s."""
+        out = np.zeros(5)
+        self._ok(lib().itg_measure_peaks(self.h, _p(out, C.c_double)), self.h)
+        return dict(zip(["fp64_ffma", "fp32_ffma", "fp64_mma_sync", "tf32_mma_sync", "bf16_mma_sync"],
+                        out.tolist()))
 
     def profile_begin(self):
         self._ok(lib().itg_profile_begin(self.h), self.h)
@@ -357,6 +394,15 @@ class Context:
         self._ok(lib().itg_heff_apply(self.h, L.h if L is not None else None, W1.h, W2.h,
                                       R.h if R is not None else None, phi.h, precision, C.byref(out)), self.h)
         return Tensor(self, out)
+
+    def heff_prepare(self, L, W1, W2, R, phi, precision=-1, use_graph=True):
+        out = C.c_void_p()
+        n = C.c_int64()
+        f = C.c_double()
+        self._ok(lib().itg_heff_create(self.h, L.h if L is not None else None, W1.h, W2.h,
+                                       R.h if R is not None else None, phi.h, precision, int(use_graph),
+                                       C.byref(out), C.byref(n), C.byref(f)), self.h)
+        return Heff(self, out, n.value, f.value)
 
     def davidson(self, L, W1, W2, R, phi, maxiter=2, errgoal=1e-14, precision=-1):
         out = C.c_void_p()

@@ -49,6 +49,34 @@ struct LocalOp {
 // H_eff * phi written in phi's layout (phi must hold every block of its divergence).
 // into_phi_layout=false returns the reference's own output structure instead.
 Tensor heff_product(Ctx& ctx, LocalOp const& op, Tensor const& phi, int prec, bool into_phi_layout = true);
+// A prepared H_eff apply for a fixed (L, W1, W2, R, phi layout): plans resolved
+// once, intermediates preallocated, launches optionally replayed as one CUDA
+// graph. run() reads phi from `in` and writes H_eff phi to `out` (device
+// pointers, or host pointers when host=true: copies are part of the run).
+struct HeffProgram {
+    struct Step {
+        std::shared_ptr<Plan> plan;
+        Tensor operand;        // L, W1, W2 or R
+        bool operand_left;     // operand is the left factor of the contraction
+        int in_buf, out_buf;   // -1 = program input, -2 = program output, else intermediate
+    };
+    std::vector<Step> steps;
+    std::vector<DevBufPtr> inter;
+    DevBufPtr in, out;
+    int64_t in_size = 0, out_size = 0;
+    std::shared_ptr<Layout> out_layout;
+    int prec = 0;
+    bool use_graph = false;
+    cudaGraphExec_t graph = nullptr;
+    int launches_per_run = 0;
+    double flops = 0;
+    ~HeffProgram();
+    void run(Ctx& ctx, double const* in_ptr, double* out_ptr, bool host = false);
+    void launch_steps(Ctx& ctx);
+};
+std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shared_ptr<Layout> phi_layout, int prec,
+                                          bool into_phi_layout, bool use_graph);
+
 // davidson, block size 1 (itensor/iterativesolvers.h:99-451); phi is replaced by the
 // normalised lowest Ritz vector; returns the Ritz value.
 double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double errgoal, int miniter, int prec,

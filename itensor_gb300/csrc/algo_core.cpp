@@ -421,8 +421,16 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
     std::vector<Tensor> V(msz), AV(msz);
     std::vector<double> M((size_t)msz * msz, std::numeric_limits<double>::quiet_NaN());
     auto Mat = [&](int i, int j) -> double& { return M[(size_t)j * msz + i]; };
+    // one prepared program for every apply of this call (plans resolved once)
+    auto prog = heff_prepare(ctx, op, phi.lay, prec, true, false);
+    auto apply = [&](Tensor const& x) {
+        Tensor y(phi.lay, ctx.stream);
+        prog->run(ctx, x.data(), y.data());
+        ++napply;
+        return y;
+    };
     V[0] = phi;
-    AV[0] = heff_product(ctx, op, V[0], prec); ++napply;
+    AV[0] = apply(V[0]);
     const double initEn = dot(ctx, V[0].data(), AV[0].data(), n);
     double last_lambda = 1000.0, lambda = initEn;
     Tensor phi_t = phi;
@@ -479,7 +487,7 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
         }
         if (done) break;
         V[ni] = q;
-        AV[ni] = heff_product(ctx, op, V[ni], prec); ++napply;
+        AV[ni] = apply(V[ni]);
         std::vector<double const*> vp(ni + 1);
         for (int k = 0; k <= ni; ++k) vp[k] = V[k].data();
         std::vector<double> nc(ni + 1);

@@ -20,6 +20,9 @@ struct itg_plan {
 struct itg_dmrg_result {
     DmrgResult r;
 };
+struct itg_heff {
+    std::shared_ptr<HeffProgram> p;
+};
 
 namespace {
 thread_local std::string g_error;
@@ -100,6 +103,13 @@ int itg_reset_stats(itg_ctx* c) {
 }
 
 void* itg_stream(itg_ctx* c) { return c ? (void*)c->ctx.stream : nullptr; }
+
+int itg_measure_peaks(itg_ctx* c, double* tflops5) {
+    return guard(c, [&] {
+        ITG_REQUIRE(tflops5, "measure_peaks: null output");
+        measure_peaks(c->ctx, tflops5);
+    });
+}
 
 int itg_profile_begin(itg_ctx* c) {
     return guard(c, [&] {
@@ -300,6 +310,28 @@ int itg_heff_apply(itg_ctx* c, const itg_tensor* L, const itg_tensor* W1, const 
         *out = new itg_tensor{heff_product(c->ctx, op, phi->t, precision, false)};
     });
 }
+
+int itg_heff_create(itg_ctx* c, const itg_tensor* L, const itg_tensor* W1, const itg_tensor* W2, const itg_tensor* R,
+                    const itg_tensor* phi, int precision, int use_graph, itg_heff** out, int64_t* out_size,
+                    double* flops) {
+    return guard(c, [&] {
+        ITG_REQUIRE(W1 && W2 && phi && out, "heff_create: null argument");
+        LocalOp op{opt(L), &W1->t, &W2->t, opt(R)};
+        auto p = heff_prepare(c->ctx, op, phi->t.lay, precision, false, use_graph != 0);
+        *out = new itg_heff{p};
+        if (out_size) *out_size = p->out_size;
+        if (flops) *flops = p->flops;
+    });
+}
+
+int itg_heff_run(itg_ctx* c, itg_heff* h, const double* phi, double* out, int host) {
+    return guard(c, [&] {
+        ITG_REQUIRE(h && phi && out, "heff_run: null argument");
+        h->p->run(c->ctx, phi, out, host != 0);
+    });
+}
+
+void itg_heff_free(itg_heff* h) { delete h; }
 
 int itg_davidson(itg_ctx* c, const itg_tensor* L, const itg_tensor* W1, const itg_tensor* W2, const itg_tensor* R,
                  const itg_tensor* phi, int32_t maxiter, double errgoal, int precision, double* energy,

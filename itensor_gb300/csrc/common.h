@@ -43,6 +43,13 @@ struct Error : std::runtime_error {
         if (!(cond)) throw ::itg::Error(::itg::ERR_ARG, (msg)); \
     } while (0)
 
+// Streams of live contexts. A buffer that outlives its context (a tensor
+// handle released after itg_destroy) is freed synchronously instead of on the
+// destroyed stream.
+void stream_register(cudaStream_t s);
+void stream_unregister(cudaStream_t s);
+bool stream_alive(cudaStream_t s);
+
 // Device buffer from the stream-ordered pool (cudaMallocAsync). Freed on the
 // stream it was allocated on, so reuse is ordered after every prior use.
 struct DevBuf {
@@ -54,7 +61,9 @@ struct DevBuf {
         if (n) ITG_CHECK_CUDA(cudaMallocAsync(&p, n, s));
     }
     ~DevBuf() {
-        if (p) cudaFreeAsync(p, stream);
+        if (!p) return;
+        if (stream_alive(stream)) cudaFreeAsync(p, stream);
+        else cudaFree(p);
     }
     DevBuf(DevBuf const&) = delete;
     DevBuf& operator=(DevBuf const&) = delete;

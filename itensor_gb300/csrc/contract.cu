@@ -309,36 +309,76 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
 }
 
 // ------------------------------------------------------------------ Ozaki BF16 block GEMM
-// FP64 operands become fixed-point integers relative to a power-of-two scale
-// per tile row (A) / tile column (B): X = floor(|x| 2^(7S - e)), |x| < 2^e,
-// cut into S digits of 7 bits (sign applied), each exact in BF16. Digit
-// products are exact in FP32 and so are their sums while |sum| < 2^24. Digit
-// pairs (s,t) with s+t < S are accumulated per diagonal D = s+t on the BF16
-// tensor pipe (mma.sync m16n8k16, FP32 accumulate); every 256 k the diagonals
-// are converted to integers and folded into one int64 accumulator
-// sum_D acc_D 2^(7(S-1-D)). One FP64 conversion per output at the end.
-// The slicing and folding use integer instructions only (FP64 issue slots on
-// this part are ~1/60 of FP32). Accuracy ~2^(-7S) of row/column maxima.
+// Split precision (after Ozaki et al., error-free splitting of matrix
+// products). Every operand block is seen as a rows x K matrix (A: rows = m,
+// B: rows = n). Each row gets a power-of-two scale e with |x| < 2^e, and each
+// entry becomes the fixed-point integer X = floor(|x| 2^(7S - e)) cut into S
+// digits of 7 bits (sign applied): integers in [-127, 127], exact in BF16.
+// Digit products are exact in FP32 and so are their sums while |sum| < 2^24.
+// Digit pairs (s,t) with s+t < S are accumulated per diagonal D = s+t on the
+// BF16 tensor pipe (mma.sync m16n8k16, FP32 accumulate), folded exactly into
+// one int64 per output (sum_D acc_D 2^(7(S-1-D))) every 256 k, and scaled into
+// the FP64 output once per block pair. Accuracy ~2^(-7S) of the row/column
+// maxima; all slicing and folding is integer work (FP64 issue slots on this
+// part are ~1/60 of FP32).
+//
+// Pass 1 (prep): one CTA per operand block writes its row exponents and S
+// digit planes, k-contiguous with K padded to a multiple of 16 (zeros).
+// Pass 2 (GEMM): tiles load the planes with 16-byte loads.
 __device__ __forceinline__ int exp_field(double x) {
     return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
 }
 
+constexpr int OZ_TK = 16;
+
+// One prep item: rows [r0, r1) of one operand block, with every k, so the
+// row exponents are complete within the CTA. Items hold ~2048 elements.
+constexpr int OZ_PREP_ROWS = 256;
+
 template <int S>
-__device__ __forceinline__ void ozaki_digits(double x, int e, __nv_bfloat16* dst, int stride) {
-    long long bits = __double_as_longlong(x);
-    int ef = (int)((bits >> 52) & 0x7FF);
-    unsigned long long X = 0;
-    if (ef != 0) {
-        unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-        int sh = ef - 1075 + 7 * S - e;  // |x| = mant 2^(ef-1075)
-        if (sh >= 0) X = mant << sh;
-        else if (sh > -64) X = mant >> (-sh);
+__global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restrict__ items, const OpBlockRec* __restrict__ ops,
+                                                         const int32_t* __restrict__ tab, const double* __restrict__ A,
+                                                         const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
+                                                         int64_t plane, int32_t* __restrict__ exps) {
+    __shared__ int rexp[OZ_PREP_ROWS];
+    const PrepItem pi = items[blockIdx.x];
+    const OpBlockRec ob = ops[pi.op];
+    const double* __restrict__ X = pi.which ? B : A;
+    const int tid = threadIdx.x;
+    const int rows = pi.r1 - pi.r0;
+    const int n = rows * ob.K;
+    for (int r = tid; r < rows; r += blockDim.x) rexp[r] = 0;
+    __syncthreads();
+    const double* base = X + ob.src;
+    const int32_t* trow = tab + ob.trow + pi.r0;
+    const int32_t* tcol = tab + ob.tcol;
+    for (int e = tid; e < n; e += blockDim.x) {
+        int r = e % rows, k = e / rows;
+        atomicMax(&rexp[r], exp_field(base[trow[r] + tcol[k]]));
     }
-    const bool neg = bits < 0;
+    __syncthreads();
+    for (int r = tid; r < rows; r += blockDim.x) exps[ob.exp + pi.r0 + r] = rexp[r] - 1022;  // |x| < 2^(E-1022)
+    // digits, written k-contiguous; padding columns K..Kp-1 are zero
+    const int np = rows * ob.Kp;
+    __nv_bfloat16* pan = panels + ob.panel + (int64_t)pi.r0 * ob.Kp;
+    for (int e = tid; e < np; e += blockDim.x) {
+        int k = e % ob.Kp, r = e / ob.Kp;
+        double x = (k < ob.K) ? base[trow[r] + tcol[k]] : 0.0;
+        long long bits = __double_as_longlong(x);
+        int ef = (int)((bits >> 52) & 0x7FF);
+        unsigned long long Xf = 0;
+        if (ef != 0) {
+            unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+            int sh = ef - 1075 + 7 * S - (rexp[r] - 1022);  // <= 7S - 53 < 0 for S <= 7
+            if (sh > -64) Xf = sh >= 0 ? (mant << sh) : (mant >> (-sh));
+        }
+        const bool neg = bits < 0;
+        __nv_bfloat16* dst = pan + e;
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-        int d = (int)((X >> (7 * (S - 1 - s))) & 127ull);
-        dst[s * stride] = __float2bfloat16_rn((float)(neg ? -d : d));
+        for (int s = 0; s < S; ++s) {
+            int d = (int)((Xf >> (7 * (S - 1 - s))) & 127ull);
+            dst[s * plane] = __float2bfloat16_rn((float)(neg ? -d : d));
+        }
     }
 }
 
@@ -346,79 +386,51 @@ template <int S>
 __global__ void __launch_bounds__(128) gemm_ozaki_kernel(const ItemRec* __restrict__ items,
                                                          const PairRec* __restrict__ pairs,
                                                          const CBlockRec* __restrict__ cblk,
+                                                         const OpBlockRec* __restrict__ ops,
                                                          const int32_t* __restrict__ tab,
-                                                         const double* __restrict__ A,
-                                                         const double* __restrict__ B,
-                                                         double* __restrict__ C) {
-    constexpr int T = GEMM_TILE, TK = 16, KCHUNK = 256, LD = TK + 8;
+                                                         const __nv_bfloat16* __restrict__ panels, int64_t plane,
+                                                         const int32_t* __restrict__ exps, double* __restrict__ C) {
+    constexpr int T = GEMM_TILE, TK = OZ_TK, KCHUNK = 256, LD = TK + 8;  // row stride 48 B (16-B aligned)
     __shared__ __align__(16) __nv_bfloat16 As[S][T][LD];
     __shared__ __align__(16) __nv_bfloat16 Bs[S][T][LD];
-    __shared__ int rowexp[T], colexp[T];
+    __shared__ int ea[T], eb[T];
     const ItemRec it = items[blockIdx.x];
     const CBlockRec cb = cblk[it.c];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = (warp & 1) * 16, wn = (warp >> 1) * 16;  // warp tile 16x16 = 2 mma n-tiles
     const int g = lane >> 2, tg = lane & 3;
-    // pass 1: exponent scale per tile row / column over every pair of the tile
-    if (tid < 2 * T) {
-        const bool isrow = tid < T;
-        const int i = isrow ? tid : tid - T;
-        const int mn = isrow ? it.m0 + i : it.n0 + i;
-        int emax = 0;
-        if (mn < (isrow ? cb.M : cb.N)) {
-            for (int p = it.p0; p < it.p1; ++p) {
-                const PairRec pr = pairs[p];
-                if (isrow) {
-                    const double* a = A + pr.aoff + tab[pr.tam + mn];
-                    for (int k = 0; k < pr.K; ++k) emax = max(emax, exp_field(a[tab[pr.tak + k]]));
-                } else {
-                    const double* b = B + pr.boff + tab[pr.tbn + mn];
-                    for (int k = 0; k < pr.K; ++k) emax = max(emax, exp_field(b[tab[pr.tbk + k]]));
-                }
-            }
-        }
-        // |x| < 2^(emax - 1022) for every x in this row / column
-        if (isrow) rowexp[i] = emax - 1022;
-        else colexp[i] = emax - 1022;
-    }
-    __syncthreads();
-    long long tot[2][4];
+    double out[2][4];
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) tot[j][q] = 0;
-    float acc[S][2][4];
-#pragma unroll
-    for (int d = 0; d < S; ++d)
-#pragma unroll
-        for (int j = 0; j < 2; ++j)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[d][j][q] = 0.f;
-    int kacc = 0;  // k accumulated in acc since the last fold
-    auto fold = [&]() {
+        for (int q = 0; q < 4; ++q) out[j][q] = 0.0;
+    for (int p = it.p0; p < it.p1; ++p) {
+        const PairRec pr = pairs[p];
+        const OpBlockRec oa = ops[pr.ia], ob = ops[pr.ib];
+        if (tid < T) ea[tid] = (it.m0 + tid < cb.M) ? exps[oa.exp + it.m0 + tid] : 0;
+        else if (tid < 2 * T) eb[tid - T] = (it.n0 + tid - T < cb.N) ? exps[ob.exp + it.n0 + tid - T] : 0;
+        long long tot[2][4];
+        float acc[S][2][4];
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                long long v = 0;
+                tot[j][q] = 0;
 #pragma unroll
-                for (int d = 0; d < S; ++d) {
-                    v += (long long)__float2ll_rn(acc[d][j][q]) << (7 * (S - 1 - d));
-                    acc[d][j][q] = 0.f;
-                }
-                tot[j][q] += v;
+                for (int d = 0; d < S; ++d) acc[d][j][q] = 0.f;
             }
-    };
-    for (int p = it.p0; p < it.p1; ++p) {
-        const PairRec pr = pairs[p];
+        int kacc = 0;
         for (int k0 = 0; k0 < pr.K; k0 += TK) {
-            for (int e = tid; e < T * TK; e += 128) {
-                const int i = e % T, kk = e / T, k = k0 + kk;
-                const int m = it.m0 + i, n = it.n0 + i;
-                double x = (m < cb.M && k < pr.K) ? A[pr.aoff + tab[pr.tam + m] + tab[pr.tak + k]] : 0.0;
-                double y = (n < cb.N && k < pr.K) ? B[pr.boff + tab[pr.tbk + k] + tab[pr.tbn + n]] : 0.0;
-                ozaki_digits<S>(x, rowexp[i], &As[0][i][kk], T * LD);
-                ozaki_digits<S>(y, colexp[i], &Bs[0][i][kk], T * LD);
+            // 16-byte loads: per plane and row, k0..k0+15 are two uint4
+            for (int e = tid; e < S * T * 2; e += 128) {
+                const int half = e & 1, row = (e >> 1) % T, s = (e >> 1) / T;
+                uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
+                if (it.m0 + row < cb.M)
+                    va = *reinterpret_cast<const uint4*>(panels + oa.panel + s * plane + (int64_t)(it.m0 + row) * oa.Kp + k0 + half * 8);
+                if (it.n0 + row < cb.N)
+                    vb = *reinterpret_cast<const uint4*>(panels + ob.panel + s * plane + (int64_t)(it.n0 + row) * ob.Kp + k0 + half * 8);
+                *reinterpret_cast<uint4*>(&As[s][row][half * 8]) = va;
+                *reinterpret_cast<uint4*>(&Bs[s][row][half * 8]) = vb;
             }
             __syncthreads();
             uint32_t af[S][4], bfr[S][2][2];
@@ -450,28 +462,70 @@ __global__ void __launch_bounds__(128) gemm_ozaki_kernel(const ItemRec* __restri
                     }
             __syncthreads();
             kacc += TK;
-            if (kacc >= KCHUNK) { fold(); kacc = 0; }
+            if (kacc >= KCHUNK || k0 + TK >= pr.K) {
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        long long v = 0;
+#pragma unroll
+                        for (int d = 0; d < S; ++d) {
+                            v += (long long)__float2ll_rn(acc[d][j][q]) << (7 * (S - 1 - d));
+                            acc[d][j][q] = 0.f;
+                        }
+                        tot[j][q] += v;
+                    }
+                kacc = 0;
+            }
         }
+        // value = tot * 2^(e_row + e_col - 7 S - 7), one FP64 scale per pair
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int r = wm + g + (q >= 2 ? 8 : 0);
+                const int cc = wn + j * 8 + tg * 2 + (q & 1);
+                out[j][q] += ldexp((double)tot[j][q], ea[r] + eb[cc] - 7 * S - 7);
+            }
+        __syncthreads();  // ea/eb are rewritten by the next pair
     }
-    fold();
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const int r = wm + g + (q >= 2 ? 8 : 0);
-            const int cc = wn + j * 8 + tg * 2 + (q & 1);
-            const int m = it.m0 + r, n = it.n0 + cc;
-            if (m < cb.M && n < cb.N) {
-                // value = tot * 2^(e_row + e_col - 7 S - 7)
-                C[cb.coff + tab[cb.tcm + m] + tab[cb.tcn + n]] = ldexp((double)tot[j][q], rowexp[r] + colexp[cc] - 7 * S - 7);
-            }
+            const int m = it.m0 + wm + g + (q >= 2 ? 8 : 0);
+            const int n = it.n0 + wn + j * 8 + tg * 2 + (q & 1);
+            if (m < cb.M && n < cb.N) C[cb.coff + tab[cb.tcm + m] + tab[cb.tcn + n]] = out[j][q];
         }
 }
 
 // ------------------------------------------------------------------ host side
+namespace {
+std::mutex g_streams_mu;
+std::vector<cudaStream_t>& live_streams() {
+    static std::vector<cudaStream_t> v;
+    return v;
+}
+}  // namespace
+void stream_register(cudaStream_t s) {
+    std::lock_guard<std::mutex> g(g_streams_mu);
+    live_streams().push_back(s);
+}
+void stream_unregister(cudaStream_t s) {
+    std::lock_guard<std::mutex> g(g_streams_mu);
+    auto& v = live_streams();
+    v.erase(std::remove(v.begin(), v.end(), s), v.end());
+}
+bool stream_alive(cudaStream_t s) {
+    std::lock_guard<std::mutex> g(g_streams_mu);
+    auto& v = live_streams();
+    return std::find(v.begin(), v.end(), s) != v.end();
+}
+
 Ctx::Ctx(int dev) : device(dev) {
     ITG_CHECK_CUDA(cudaSetDevice(dev));
     ITG_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    stream_register(stream);
     int sms = 0;
     ITG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     sm_count = sms;
@@ -487,7 +541,10 @@ Ctx::~Ctx() {
     plans.clear();
     if (pin) cudaFreeHost(pin);
     if (stage) cudaFreeHost(stage);
-    if (stream) cudaStreamDestroy(stream);
+    if (stream) {
+        stream_unregister(stream);
+        cudaStreamDestroy(stream);
+    }
 }
 
 void Ctx::ensure_pin(size_t bytes) {
@@ -768,6 +825,46 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             maxK = std::max(maxK, ksum);
             sumK += ksum;
         }
+        // operand panels for the split-precision path: every A and B block in use
+        std::vector<OpBlockRec> ops;
+        std::vector<int> ia_of(nA, -1), ib_of(nB, -1);
+        int64_t panel = 0, expo = 0;
+        int max_rows = 1;
+        auto add_op = [&](int64_t src, int rows, int K, int trow, int tcol) {
+            OpBlockRec o;
+            o.src = src; o.rows = rows; o.K = K; o.Kp = (K + 15) / 16 * 16;
+            o.trow = trow; o.tcol = tcol;
+            o.panel = panel; o.exp = (int32_t)expo;
+            panel += ((int64_t)rows * o.Kp + 15) / 16 * 16;
+            expo += rows;
+            max_rows = std::max(max_rows, rows);
+            ops.push_back(o);
+            return (int)ops.size() - 1;
+        };
+        auto rows_of = [&](Layout const& Lx, int b, std::vector<int> const& pos) {
+            int r = 1;
+            for (int i : pos) r *= Lx.inds[i].bdim(Lx.block(b)[i]);
+            return r;
+        };
+        for (int ab = 0; ab < nA; ++ab)
+            if (tamA[ab] >= 0) ia_of[ab] = add_op(A.offs[ab], rows_of(A, ab, mt.a_unc), rows_of(A, ab, mt.a_con), tamA[ab], takA[ab]);
+        const int nopsA = (int)ops.size();
+        for (int bb = 0; bb < nB; ++bb)
+            if (tbkB[bb] >= 0) ib_of[bb] = add_op(B.offs[bb], rows_of(B, bb, mt.b_unc), rows_of(B, bb, mt.b_con), tbnB[bb], tbkB[bb]);
+        const int nopsB = (int)ops.size() - nopsA;
+        // prep items: ~2048 elements each, whole rows (exponents complete per row)
+        std::vector<PrepItem> prep;
+        for (int o = 0; o < (int)ops.size(); ++o) {
+            const int rows = ops[o].rows, Kp = std::max(ops[o].Kp, 1);
+            const int chunk = std::max(1, std::min(OZ_PREP_ROWS, 2048 / Kp));
+            for (int r0 = 0; r0 < rows; r0 += chunk)
+                prep.push_back(PrepItem{o, r0, std::min(rows, r0 + chunk), o < nopsA ? 0 : 1});
+        }
+        {
+            int q = 0;
+            for (int c = 0; c < ncb; ++c)
+                for (int p : bypc[c]) { pairs[q].ia = ia_of[pa[p]]; pairs[q].ib = ib_of[pb[p]]; ++q; }
+        }
         // tiles, most expensive first
         std::vector<ItemRec> items;
         std::vector<double> cost;
@@ -785,14 +882,24 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         // upload
         size_t t_items = 0, t_pairs = align16(sizeof(ItemRec) * sitems.size());
         size_t t_cblk = align16(t_pairs + sizeof(PairRec) * pairs.size());
-        size_t t_tab = align16(t_cblk + sizeof(CBlockRec) * cblk.size());
+        size_t t_ops = align16(t_cblk + sizeof(CBlockRec) * cblk.size());
+        size_t t_prep = align16(t_ops + sizeof(OpBlockRec) * ops.size());
+        size_t t_tab = align16(t_prep + sizeof(PrepItem) * prep.size());
         size_t tbytes = align16(t_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size()));
         ctx.ensure_stage(tbytes);
         st = static_cast<char*>(ctx.stage);
         if (!sitems.empty()) std::memcpy(st + t_items, sitems.data(), sizeof(ItemRec) * sitems.size());
         if (!pairs.empty()) std::memcpy(st + t_pairs, pairs.data(), sizeof(PairRec) * pairs.size());
         if (!cblk.empty()) std::memcpy(st + t_cblk, cblk.data(), sizeof(CBlockRec) * cblk.size());
+        if (!ops.empty()) std::memcpy(st + t_ops, ops.data(), sizeof(OpBlockRec) * ops.size());
+        if (!prep.empty()) std::memcpy(st + t_prep, prep.data(), sizeof(PrepItem) * prep.size());
+        plan->nprep = (int)prep.size();
         if (!tab.empty()) std::memcpy(st + t_tab, tab.data(), sizeof(int32_t) * tab.size());
+        plan->nopsA = nopsA;
+        plan->nopsB = nopsB;
+        plan->panel_elems = panel;
+        plan->exp_elems = expo;
+        plan->max_rows = max_rows;
         plan->dev = dev_alloc(tbytes, ctx.stream);
         char* db = plan->dev->as<char>();
         ITG_CHECK_CUDA(cudaMemcpyAsync(db, st, tbytes, cudaMemcpyHostToDevice, ctx.stream));
@@ -800,6 +907,8 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->d_items = reinterpret_cast<ItemRec*>(db + t_items);
         plan->d_pairs = reinterpret_cast<PairRec*>(db + t_pairs);
         plan->d_cblk = reinterpret_cast<CBlockRec*>(db + t_cblk);
+        plan->d_ops = reinterpret_cast<OpBlockRec*>(db + t_ops);
+        plan->d_prep = reinterpret_cast<PrepItem*>(db + t_prep);
         plan->d_tab = reinterpret_cast<int32_t*>(db + t_tab);
         plan->nitems = (int)sitems.size();
         plan->npairs = np;
@@ -869,12 +978,24 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
     }
     // small-K contractions (the MPO-tensor steps) are bandwidth-shaped: FP64 is exact there
     if (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) {
-        switch (ctx.ozaki_slices) {
-            case 3: gemm_ozaki_kernel<3><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C); break;
-            case 4: gemm_ozaki_kernel<4><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C); break;
-            case 5: gemm_ozaki_kernel<5><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C); break;
-            default: gemm_ozaki_kernel<6><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C); break;
+        const int S = ctx.ozaki_slices;
+        const int64_t plane = (p.panel_elems + 15) / 16 * 16;
+        if (!p.scratch || p.scratch_slices != S) {
+            p.scratch = dev_alloc(sizeof(__nv_bfloat16) * plane * S + sizeof(int32_t) * (p.exp_elems + 4), ctx.stream);
+            p.scratch_slices = S;
         }
+        __nv_bfloat16* panels = p.scratch->as<__nv_bfloat16>();
+        int32_t* exps = reinterpret_cast<int32_t*>(panels + plane * S);
+        auto prep = [&](auto kern) {
+            kern<<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
+        };
+        switch (S) {
+            case 3: prep(ozaki_prep_kernel<3>); gemm_ozaki_kernel<3><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C); break;
+            case 4: prep(ozaki_prep_kernel<4>); gemm_ozaki_kernel<4><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C); break;
+            case 5: prep(ozaki_prep_kernel<5>); gemm_ozaki_kernel<5><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C); break;
+            default: prep(ozaki_prep_kernel<6>); gemm_ozaki_kernel<6><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C); break;
+        }
+        ctx.kernel_launches += 1;
     } else if (prec == PREC_F64 || prec == PREC_OZAKI_BF16) {
         gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
     } else {

@@ -22,7 +22,21 @@ struct PairRec {          // one (A block, B block) product feeding an output bl
     int32_t tam, tak;     // table positions: A offsets along m and along k
     int32_t tbk, tbn;     // table positions: B offsets along k and along n
     int32_t K;            // contracted extent
+    int32_t ia, ib;       // operand-panel records of the two blocks (split-precision path)
     int32_t pad;
+};
+// One operand block seen as a rows x K matrix (rows = A's m or B's n), for the
+// split-precision path: its digit planes are stored k-contiguous, K padded to
+// Kp (multiple of 16), one power-of-two exponent per row.
+struct OpBlockRec {
+    int64_t src;          // element offset of the block in the operand
+    int64_t panel;        // bf16 element offset of digit plane 0 in the panel buffer
+    int32_t rows, K, Kp;
+    int32_t trow, tcol;   // table positions: offsets along rows and along k
+    int32_t exp;          // position of the row exponents in the exponent buffer
+};
+struct PrepItem {         // rows [r0, r1) of operand block `op`; which = 0 (A) or 1 (B)
+    int32_t op, r0, r1, which;
 };
 struct CBlockRec {        // output block
     int64_t coff;
@@ -48,6 +62,16 @@ struct Plan {
     int maxK = 0;                    // largest summed K of one output block
     double avgK = 0;
     bool scalar = false;             // rank-0 result
+    // split-precision operand panels (A blocks, then B blocks)
+    OpBlockRec* d_ops = nullptr;
+    PrepItem* d_prep = nullptr;
+    int nprep = 0;
+    int nopsA = 0, nopsB = 0;
+    int64_t panel_elems = 0;         // bf16 elements per digit plane set (all blocks)
+    int64_t exp_elems = 0;
+    int max_rows = 0;
+    mutable DevBufPtr scratch;       // panels + exponents, allocated on first use
+    mutable int scratch_slices = 0;
 };
 
 struct ProfRec {          // one timed GEMM launch (profiling mode)
@@ -105,6 +129,9 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
 // ITensor operator*: contracts every index common to A and B.
 Tensor contract(Ctx& ctx, Tensor const& A, Tensor const& B, int prec = -1,
                 std::shared_ptr<Layout> target = nullptr);
+
+// TFLOP/s of [FP64 FFMA, FP32 FFMA, FP64 mma.sync, TF32 mma.sync, BF16 mma.sync] (peaks.cu)
+void measure_peaks(Ctx& ctx, double* tflops);
 
 // ---- kernels launched from other translation units (ops.cu)
 void launch_fill(Ctx& ctx, double* x, int64_t n, double v);

@@ -1,0 +1,120 @@
+// Prepared effective-Hamiltonian apply (LocalOp::product,
+// itensor/mps/localop.h:324-365) for repeated use with one operator: the four
+// contraction plans are resolved once, the intermediates are preallocated,
+// and the launches can be replayed as one CUDA graph, so an apply costs no
+// host-side planning.
+#include "algo.h"
+
+namespace itg {
+
+HeffProgram::~HeffProgram() {
+    if (graph) cudaGraphExecDestroy(graph);
+}
+
+std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shared_ptr<Layout> phi_layout, int prec,
+                                          bool into_phi_layout, bool use_graph) {
+    ITG_REQUIRE(op.W1 && op.W2 && phi_layout, "heff_prepare: missing operand");
+    auto P = std::make_shared<HeffProgram>();
+    P->prec = prec < 0 ? ctx.precision : prec;
+    P->use_graph = use_graph;
+    std::vector<Tensor const*> chain;
+    if (!op.L) {
+        if (op.R) chain.push_back(op.R);
+        chain.push_back(op.W2);
+        chain.push_back(op.W1);
+    } else {
+        chain.push_back(op.L);
+        chain.push_back(op.W1);
+        chain.push_back(op.W2);
+        if (op.R) chain.push_back(op.R);
+    }
+    std::shared_ptr<Layout> target;
+    if (into_phi_layout) {
+        target = std::make_shared<Layout>(*phi_layout);
+        target->inds = prime_all(phi_layout->inds);
+    }
+    P->in_size = phi_layout->size;
+    P->in = dev_alloc(sizeof(double) * std::max<int64_t>(1, P->in_size), ctx.stream);
+    std::shared_ptr<Layout> cur = phi_layout;
+    for (size_t s = 0; s < chain.size(); ++s) {
+        const bool last = (s + 1 == chain.size());
+        Match mt = match_indices(cur->inds, chain[s]->inds());
+        auto plan = get_plan(ctx, *cur, *chain[s]->lay, mt, last ? target : nullptr);
+        std::shared_ptr<Layout> outL;
+        if (last && target) {
+            outL = target;
+        } else {
+            outL = std::make_shared<Layout>(*plan->C);
+            outL->inds.clear();
+            for (int i : mt.a_unc) outL->inds.push_back(cur->inds[i]);
+            for (int j : mt.b_unc) outL->inds.push_back(chain[s]->inds()[j]);
+        }
+        HeffProgram::Step st;
+        st.plan = plan;
+        st.operand = *chain[s];
+        st.operand_left = false;
+        st.in_buf = (s == 0) ? -1 : (int)P->inter.size() - 1;
+        if (last) {
+            st.out_buf = -2;
+            P->out_size = outL->size;
+            P->out = dev_alloc(sizeof(double) * std::max<int64_t>(1, P->out_size), ctx.stream);
+        } else {
+            P->inter.push_back(dev_alloc(sizeof(double) * std::max<int64_t>(1, outL->size), ctx.stream));
+            st.out_buf = (int)P->inter.size() - 1;
+        }
+        P->flops += plan->flops;
+        P->steps.push_back(st);
+        cur = outL;
+    }
+    if (into_phi_layout) {
+        P->out_layout = phi_layout;
+    } else {
+        P->out_layout = std::make_shared<Layout>(*cur);
+        P->out_layout->inds = noprime_all(cur->inds);
+    }
+    return P;
+}
+
+void HeffProgram::launch_steps(Ctx& ctx) {
+    for (auto& st : steps) {
+        double const* a = st.in_buf == -1 ? in->as<double>() : inter[st.in_buf]->as<double>();
+        double* c = st.out_buf == -2 ? out->as<double>() : inter[st.out_buf]->as<double>();
+        exec_plan(ctx, *st.plan, a, st.operand.data(), c, prec);
+    }
+}
+
+void HeffProgram::run(Ctx& ctx, double const* in_ptr, double* out_ptr, bool host) {
+    if (in_size > 0)
+        ITG_CHECK_CUDA(cudaMemcpyAsync(in->p, in_ptr, sizeof(double) * in_size,
+                                       host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, ctx.stream));
+    if (use_graph) {
+        if (!graph) {
+            launch_steps(ctx);  // first run outside capture: allocates the split-precision scratch
+            const bool prof = ctx.profiling;
+            ctx.profiling = false;
+            const uint64_t l0 = ctx.kernel_launches;
+            const double f0 = ctx.flops_done;
+            cudaGraph_t g;
+            ITG_CHECK_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
+            launch_steps(ctx);
+            ITG_CHECK_CUDA(cudaStreamEndCapture(ctx.stream, &g));
+            launches_per_run = (int)(ctx.kernel_launches - l0);
+            ctx.kernel_launches = l0;
+            ctx.flops_done = f0;
+            ctx.profiling = prof;
+            ITG_CHECK_CUDA(cudaGraphInstantiate(&graph, g, 0));
+            cudaGraphDestroy(g);
+        }
+        ITG_CHECK_CUDA(cudaGraphLaunch(graph, ctx.stream));
+        ctx.kernel_launches += launches_per_run;
+        ctx.flops_done += flops;
+    } else {
+        launch_steps(ctx);
+    }
+    if (out_size > 0)
+        ITG_CHECK_CUDA(cudaMemcpyAsync(out_ptr, out->p, sizeof(double) * out_size,
+                                       host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, ctx.stream));
+    if (host) ctx.sync();
+}
+
+}  // namespace itg
