@@ -2,6 +2,7 @@
 // stream-ordered device buffers, and the per-context state.
 #pragma once
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
 #include <cstdint>
 #include <cstdio>
 #include <memory>

@@ -308,196 +308,57 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
             if (m + r < cb.M && n + s < cb.N) C[cb.coff + tab[cb.tcm + m + r] + tab[cb.tcn + n + s]] = accs[r][s];
 }
 
-// ------------------------------------------------------------------ Ozaki BF16 block GEMM
-// Split precision (after Ozaki et al., error-free splitting of matrix
-// products). Every operand block is seen as a rows x K matrix (A: rows = m,
-// B: rows = n). Each row gets a power-of-two scale e with |x| < 2^e, and each
-// entry becomes the fixed-point integer X = floor(|x| 2^(7S - e)) cut into S
-// digits of 7 bits (sign applied): integers in [-127, 127], exact in BF16.
-// Digit products are exact in FP32 and so are their sums while |sum| < 2^24.
-// Digit pairs (s,t) with s+t < S are accumulated per diagonal D = s+t on the
-// BF16 tensor pipe (mma.sync m16n8k16, FP32 accumulate), folded exactly into
-// one int64 per output (sum_D acc_D 2^(7(S-1-D))) every 256 k, and scaled into
-// the FP64 output once per block pair. Accuracy ~2^(-7S) of the row/column
-// maxima; all slicing and folding is integer work (FP64 issue slots on this
-// part are ~1/60 of FP32).
-//
-// Pass 1 (prep): one CTA per operand block writes its row exponents and S
-// digit planes, k-contiguous with K padded to a multiple of 16 (zeros).
-// Pass 2 (GEMM): tiles load the planes with 16-byte loads.
-__device__ __forceinline__ int exp_field(double x) {
-    return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
-}
+// ------------------------------------------------------------------ skinny FP64 block GEMM
+// For contractions whose output blocks are at most SKINNY_N columns wide (the
+// MPO-tensor steps of the H_eff apply: N = (s', w') <= 3, K = (s, w) <= 3).
+// One thread per output row keeps all N sums in registers; the B block
+// (K x N) is staged in shared memory. Tiles are SKINNY_M rows of one block.
+constexpr int SKINNY_N = 8, SKINNY_M = 256, SKINNY_K = 64;
 
-constexpr int OZ_TK = 16;
-
-// One prep item: rows [r0, r1) of one operand block, with every k, so the
-// row exponents are complete within the CTA. Items hold ~2048 elements.
-constexpr int OZ_PREP_ROWS = 256;
-
-template <int S>
-__global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restrict__ items, const OpBlockRec* __restrict__ ops,
-                                                         const int32_t* __restrict__ tab, const double* __restrict__ A,
-                                                         const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
-                                                         int64_t plane, int32_t* __restrict__ exps) {
-    __shared__ int rexp[OZ_PREP_ROWS];
-    const PrepItem pi = items[blockIdx.x];
-    const OpBlockRec ob = ops[pi.op];
-    const double* __restrict__ X = pi.which ? B : A;
-    const int tid = threadIdx.x;
-    const int rows = pi.r1 - pi.r0;
-    const int n = rows * ob.K;
-    for (int r = tid; r < rows; r += blockDim.x) rexp[r] = 0;
-    __syncthreads();
-    const double* base = X + ob.src;
-    const int32_t* trow = tab + ob.trow + pi.r0;
-    const int32_t* tcol = tab + ob.tcol;
-    for (int e = tid; e < n; e += blockDim.x) {
-        int r = e % rows, k = e / rows;
-        atomicMax(&rexp[r], exp_field(base[trow[r] + tcol[k]]));
-    }
-    __syncthreads();
-    for (int r = tid; r < rows; r += blockDim.x) exps[ob.exp + pi.r0 + r] = rexp[r] - 1022;  // |x| < 2^(E-1022)
-    // digits, written k-contiguous; padding columns K..Kp-1 are zero
-    const int np = rows * ob.Kp;
-    __nv_bfloat16* pan = panels + ob.panel + (int64_t)pi.r0 * ob.Kp;
-    for (int e = tid; e < np; e += blockDim.x) {
-        int k = e % ob.Kp, r = e / ob.Kp;
-        double x = (k < ob.K) ? base[trow[r] + tcol[k]] : 0.0;
-        long long bits = __double_as_longlong(x);
-        int ef = (int)((bits >> 52) & 0x7FF);
-        unsigned long long Xf = 0;
-        if (ef != 0) {
-            unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-            int sh = ef - 1075 + 7 * S - (rexp[r] - 1022);  // <= 7S - 53 < 0 for S <= 7
-            if (sh > -64) Xf = sh >= 0 ? (mant << sh) : (mant >> (-sh));
-        }
-        const bool neg = bits < 0;
-        __nv_bfloat16* dst = pan + e;
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            int d = (int)((Xf >> (7 * (S - 1 - s))) & 127ull);
-            dst[s * plane] = __float2bfloat16_rn((float)(neg ? -d : d));
-        }
-    }
-}
-
-template <int S>
-__global__ void __launch_bounds__(128) gemm_ozaki_kernel(const ItemRec* __restrict__ items,
-                                                         const PairRec* __restrict__ pairs,
-                                                         const CBlockRec* __restrict__ cblk,
-                                                         const OpBlockRec* __restrict__ ops,
-                                                         const int32_t* __restrict__ tab,
-                                                         const __nv_bfloat16* __restrict__ panels, int64_t plane,
-                                                         const int32_t* __restrict__ exps, double* __restrict__ C) {
-    constexpr int T = GEMM_TILE, TK = OZ_TK, KCHUNK = 256, LD = TK + 8;  // row stride 48 B (16-B aligned)
-    __shared__ __align__(16) __nv_bfloat16 As[S][T][LD];
-    __shared__ __align__(16) __nv_bfloat16 Bs[S][T][LD];
-    __shared__ int ea[T], eb[T];
+__global__ void __launch_bounds__(SKINNY_M) gemm_f64_skinny_kernel(const ItemRec* __restrict__ items,
+                                                                   const PairRec* __restrict__ pairs,
+                                                                   const CBlockRec* __restrict__ cblk,
+                                                                   const int32_t* __restrict__ tab,
+                                                                   const double* __restrict__ A,
+                                                                   const double* __restrict__ B,
+                                                                   double* __restrict__ C) {
+    __shared__ double Bs[SKINNY_K][SKINNY_N];
     const ItemRec it = items[blockIdx.x];
     const CBlockRec cb = cblk[it.c];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = (warp & 1) * 16, wn = (warp >> 1) * 16;  // warp tile 16x16 = 2 mma n-tiles
-    const int g = lane >> 2, tg = lane & 3;
-    double out[2][4];
+    const int m = it.m0 + threadIdx.x;
+    const bool active = m < cb.M;
+    double acc[SKINNY_N];
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) out[j][q] = 0.0;
+    for (int n = 0; n < SKINNY_N; ++n) acc[n] = 0.0;
     for (int p = it.p0; p < it.p1; ++p) {
         const PairRec pr = pairs[p];
-        const OpBlockRec oa = ops[pr.ia], ob = ops[pr.ib];
-        if (tid < T) ea[tid] = (it.m0 + tid < cb.M) ? exps[oa.exp + it.m0 + tid] : 0;
-        else if (tid < 2 * T) eb[tid - T] = (it.n0 + tid - T < cb.N) ? exps[ob.exp + it.n0 + tid - T] : 0;
-        long long tot[2][4];
-        float acc[S][2][4];
-#pragma unroll
-        for (int j = 0; j < 2; ++j)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                tot[j][q] = 0;
-#pragma unroll
-                for (int d = 0; d < S; ++d) acc[d][j][q] = 0.f;
-            }
-        int kacc = 0;
-        for (int k0 = 0; k0 < pr.K; k0 += TK) {
-            // 16-byte loads: per plane and row, k0..k0+15 are two uint4
-            for (int e = tid; e < S * T * 2; e += 128) {
-                const int half = e & 1, row = (e >> 1) % T, s = (e >> 1) / T;
-                uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
-                if (it.m0 + row < cb.M)
-                    va = *reinterpret_cast<const uint4*>(panels + oa.panel + s * plane + (int64_t)(it.m0 + row) * oa.Kp + k0 + half * 8);
-                if (it.n0 + row < cb.N)
-                    vb = *reinterpret_cast<const uint4*>(panels + ob.panel + s * plane + (int64_t)(it.n0 + row) * ob.Kp + k0 + half * 8);
-                *reinterpret_cast<uint4*>(&As[s][row][half * 8]) = va;
-                *reinterpret_cast<uint4*>(&Bs[s][row][half * 8]) = vb;
+        const int arow = active ? tab[pr.tam + m] : 0;
+        for (int k0 = 0; k0 < pr.K; k0 += SKINNY_K) {
+            const int kn = min(SKINNY_K, pr.K - k0);
+            __syncthreads();
+            for (int e = threadIdx.x; e < kn * SKINNY_N; e += blockDim.x) {
+                int k = e / SKINNY_N, n = e % SKINNY_N;
+                Bs[k][n] = (n < cb.N) ? B[pr.boff + tab[pr.tbk + k0 + k] + tab[pr.tbn + n]] : 0.0;
             }
             __syncthreads();
-            uint32_t af[S][4], bfr[S][2][2];
+            if (active) {
+                for (int k = 0; k < kn; ++k) {
+                    const double a = A[pr.aoff + arow + tab[pr.tak + k0 + k]];
 #pragma unroll
-            for (int s = 0; s < S; ++s) {
-                af[s][0] = *reinterpret_cast<const uint32_t*>(&As[s][wm + g][tg * 2]);
-                af[s][1] = *reinterpret_cast<const uint32_t*>(&As[s][wm + g + 8][tg * 2]);
-                af[s][2] = *reinterpret_cast<const uint32_t*>(&As[s][wm + g][tg * 2 + 8]);
-                af[s][3] = *reinterpret_cast<const uint32_t*>(&As[s][wm + g + 8][tg * 2 + 8]);
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    bfr[s][j][0] = *reinterpret_cast<const uint32_t*>(&Bs[s][wn + j * 8 + g][tg * 2]);
-                    bfr[s][j][1] = *reinterpret_cast<const uint32_t*>(&Bs[s][wn + j * 8 + g][tg * 2 + 8]);
+                    for (int n = 0; n < SKINNY_N; ++n) acc[n] = fma(a, Bs[k][n], acc[n]);
                 }
             }
-#pragma unroll
-            for (int s = 0; s < S; ++s)
-#pragma unroll
-                for (int t = 0; t + s < S; ++t)
-#pragma unroll
-                    for (int j = 0; j < 2; ++j) {
-                        float* c = acc[s + t][j];
-                        asm volatile(
-                            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-                            "{%8,%9}, {%0,%1,%2,%3};\n"
-                            : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-                            : "r"(af[s][0]), "r"(af[s][1]), "r"(af[s][2]), "r"(af[s][3]), "r"(bfr[t][j][0]),
-                              "r"(bfr[t][j][1]));
-                    }
-            __syncthreads();
-            kacc += TK;
-            if (kacc >= KCHUNK || k0 + TK >= pr.K) {
-#pragma unroll
-                for (int j = 0; j < 2; ++j)
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        long long v = 0;
-#pragma unroll
-                        for (int d = 0; d < S; ++d) {
-                            v += (long long)__float2ll_rn(acc[d][j][q]) << (7 * (S - 1 - d));
-                            acc[d][j][q] = 0.f;
-                        }
-                        tot[j][q] += v;
-                    }
-                kacc = 0;
-            }
         }
-        // value = tot * 2^(e_row + e_col - 7 S - 7), one FP64 scale per pair
-#pragma unroll
-        for (int j = 0; j < 2; ++j)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int r = wm + g + (q >= 2 ? 8 : 0);
-                const int cc = wn + j * 8 + tg * 2 + (q & 1);
-                out[j][q] += ldexp((double)tot[j][q], ea[r] + eb[cc] - 7 * S - 7);
-            }
-        __syncthreads();  // ea/eb are rewritten by the next pair
     }
+    if (active) {
+        const int64_t crow = cb.coff + tab[cb.tcm + m];
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int m = it.m0 + wm + g + (q >= 2 ? 8 : 0);
-            const int n = it.n0 + wn + j * 8 + tg * 2 + (q & 1);
-            if (m < cb.M && n < cb.N) C[cb.coff + tab[cb.tcm + m] + tab[cb.tcn + n]] = out[j][q];
-        }
+        for (int n = 0; n < SKINNY_N; ++n)
+            if (n < cb.N) C[crow + tab[cb.tcn + n]] = acc[n];
+    }
 }
+
+// The split-precision (Ozaki BF16) kernels live in ozaki.cu.
 
 // ------------------------------------------------------------------ host side
 namespace {
@@ -865,12 +726,16 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             for (int c = 0; c < ncb; ++c)
                 for (int p : bypc[c]) { pairs[q].ia = ia_of[pa[p]]; pairs[q].ib = ib_of[pb[p]]; ++q; }
         }
-        // tiles, most expensive first
+        // tiles, most expensive first; narrow outputs (N <= SKINNY_N) get row tiles
+        int maxN = 0;
+        for (int c = 0; c < ncb; ++c) maxN = std::max(maxN, cblk[c].N);
+        plan->skinny = (maxN <= SKINNY_N);
         std::vector<ItemRec> items;
         std::vector<double> cost;
+        const int tm = plan->skinny ? SKINNY_M : GEMM_TILE, tn = plan->skinny ? SKINNY_N : GEMM_TILE;
         for (int c = 0; c < ncb; ++c)
-            for (int m0 = 0; m0 < cblk[c].M; m0 += GEMM_TILE)
-                for (int n0 = 0; n0 < cblk[c].N; n0 += GEMM_TILE) {
+            for (int m0 = 0; m0 < cblk[c].M; m0 += tm)
+                for (int n0 = 0; n0 < cblk[c].N; n0 += tn) {
                     items.push_back(ItemRec{c, m0, n0, cp0[c], cp1[c]});
                     cost.push_back(cK[c] + 1.0);
                 }
@@ -974,10 +839,12 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
         ITG_CHECK_CUDA(cudaEventRecord(pr.start, ctx.stream));
         pr.flops = p.flops;
         pr.nitems = p.nitems;
-        pr.kind = (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) ? 1 : 0;
+        pr.kind = p.skinny ? 2 : (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) ? 1 : 0;
     }
-    // small-K contractions (the MPO-tensor steps) are bandwidth-shaped: FP64 is exact there
-    if (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) {
+    // narrow, small-K contractions (the MPO-tensor steps) are bandwidth-shaped: FP64 is exact there
+    if (p.skinny && (prec == PREC_F64 || prec == PREC_OZAKI_BF16)) {
+        gemm_f64_skinny_kernel<<<p.nitems, SKINNY_M, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+    } else if (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) {
         const int S = ctx.ozaki_slices;
         const int64_t plane = (p.panel_elems + 15) / 16 * 16;
         if (!p.scratch || p.scratch_slices != S) {
@@ -986,15 +853,7 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
         }
         __nv_bfloat16* panels = p.scratch->as<__nv_bfloat16>();
         int32_t* exps = reinterpret_cast<int32_t*>(panels + plane * S);
-        auto prep = [&](auto kern) {
-            kern<<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
-        };
-        switch (S) {
-            case 3: prep(ozaki_prep_kernel<3>); gemm_ozaki_kernel<3><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C); break;
-            case 4: prep(ozaki_prep_kernel<4>); gemm_ozaki_kernel<4><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C); break;
-            case 5: prep(ozaki_prep_kernel<5>); gemm_ozaki_kernel<5><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C); break;
-            default: prep(ozaki_prep_kernel<6>); gemm_ozaki_kernel<6><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C); break;
-        }
+        launch_ozaki(ctx, p, A, B, C, S, panels, exps);
         ctx.kernel_launches += 1;
     } else if (prec == PREC_F64 || prec == PREC_OZAKI_BF16) {
         gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);

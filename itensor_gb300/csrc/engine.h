@@ -48,6 +48,7 @@ struct ItemRec {          // one output tile (TILE x TILE) of one output block
 };
 
 constexpr int GEMM_TILE = 32;
+constexpr int OZ_PREP_ROWS = 256;   // rows per split-precision prep item (at most)
 
 struct Plan {
     std::shared_ptr<Layout> C;       // output layout
@@ -62,6 +63,7 @@ struct Plan {
     int maxK = 0;                    // largest summed K of one output block
     double avgK = 0;
     bool scalar = false;             // rank-0 result
+    bool skinny = false;             // every output block is <= 8 columns wide (row tiles)
     // split-precision operand panels (A blocks, then B blocks)
     OpBlockRec* d_ops = nullptr;
     PrepItem* d_prep = nullptr;
@@ -129,6 +131,11 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
 // ITensor operator*: contracts every index common to A and B.
 Tensor contract(Ctx& ctx, Tensor const& A, Tensor const& B, int prec = -1,
                 std::shared_ptr<Layout> target = nullptr);
+
+// Split-precision prep + GEMM launches for a plan (ozaki.cu); panels/exps are
+// the plan's scratch (S digit planes of the padded panel size, row exponents).
+void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S, __nv_bfloat16* panels,
+                  int32_t* exps);
 
 // TFLOP/s of [FP64 FFMA, FP32 FFMA, FP64 mma.sync, TF32 mma.sync, BF16 mma.sync] (peaks.cu)
 void measure_peaks(Ctx& ctx, double* tflops);

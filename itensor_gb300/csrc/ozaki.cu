@@ -1,0 +1,240 @@
+// Split-precision block GEMM (after Ozaki et al., error-free splitting of
+// matrix products) on the BF16 tensor pipe of sm_103a.
+//
+// Every operand block is seen as a rows x K matrix (A: rows = m, B: rows = n).
+// Each row gets a power-of-two scale e with |x| < 2^e, and each entry becomes
+// the fixed-point integer X = floor(|x| 2^(7S - e)) cut into S digits of 7
+// bits (sign applied): integers in [-127, 127], exact in BF16. Digit products
+// are exact in FP32 and so are their sums while |sum| < 2^24. Digit pairs
+// (s,t) with s+t < S are accumulated per diagonal D = s+t with mma.sync
+// m16n8k16 (FP32 accumulate), folded exactly into one int64 per output
+// (sum_D acc_D 2^(7(S-1-D))) every 256 k, and scaled into the FP64 output once
+// per block pair. Accuracy ~2^(-7S) of the row/column maxima. Slicing and
+// folding are integer work: FP64 issue slots on this part are ~1/60 of FP32.
+//
+// prep: one CTA per item of whole rows (~2048 elements) writes the row
+//       exponents and the S digit planes, k-contiguous, K padded to 16.
+// gemm: one CTA (4 warps, 16x16 each) per 32x32 output tile; digit panels are
+//       staged with cp.async into a two-stage shared-memory ring and read
+//       with ldmatrix.
+#include "engine.h"
+#include <cuda_bf16.h>
+
+namespace itg {
+
+__device__ __forceinline__ int exp_field(double x) {
+    return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+template <int S>
+__global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restrict__ items, const OpBlockRec* __restrict__ ops,
+                                                         const int32_t* __restrict__ tab, const double* __restrict__ A,
+                                                         const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
+                                                         int64_t plane, int32_t* __restrict__ exps) {
+    __shared__ int rexp[OZ_PREP_ROWS];
+    const PrepItem pi = items[blockIdx.x];
+    const OpBlockRec ob = ops[pi.op];
+    const double* __restrict__ X = pi.which ? B : A;
+    const int tid = threadIdx.x;
+    const int rows = pi.r1 - pi.r0;
+    const int n = rows * ob.K;
+    for (int r = tid; r < rows; r += blockDim.x) rexp[r] = 0;
+    __syncthreads();
+    const double* base = X + ob.src;
+    const int32_t* trow = tab + ob.trow + pi.r0;
+    const int32_t* tcol = tab + ob.tcol;
+    for (int e = tid; e < n; e += blockDim.x) {
+        int r = e % rows, k = e / rows;
+        atomicMax(&rexp[r], exp_field(base[trow[r] + tcol[k]]));
+    }
+    __syncthreads();
+    for (int r = tid; r < rows; r += blockDim.x) exps[ob.exp + pi.r0 + r] = rexp[r] - 1022;  // |x| < 2^(E-1022)
+    const int np = rows * ob.Kp;
+    __nv_bfloat16* pan = panels + ob.panel + (int64_t)pi.r0 * ob.Kp;
+    for (int e = tid; e < np; e += blockDim.x) {
+        int k = e % ob.Kp, r = e / ob.Kp;
+        double x = (k < ob.K) ? base[trow[r] + tcol[k]] : 0.0;
+        long long bits = __double_as_longlong(x);
+        int ef = (int)((bits >> 52) & 0x7FF);
+        unsigned long long Xf = 0;
+        if (ef != 0) {
+            unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+            int sh = ef - 1075 + 7 * S - (rexp[r] - 1022);  // <= 7S - 53 < 0 for S <= 7
+            if (sh > -64) Xf = sh >= 0 ? (mant << sh) : (mant >> (-sh));
+        }
+        const bool neg = bits < 0;
+        __nv_bfloat16* dst = pan + e;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            int d = (int)((Xf >> (7 * (S - 1 - s))) & 127ull);
+            dst[s * plane] = __float2bfloat16_rn((float)(neg ? -d : d));
+        }
+    }
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+    const unsigned saddr = (unsigned)__cvta_generic_to_shared(smem);
+    const int bytes = valid ? 16 : 0;  // 0: zero-fill, nothing read
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(gmem), "r"(bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+__device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void* smem) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+template <int S>
+__global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __restrict__ items,
+                                                         const PairRec* __restrict__ pairs,
+                                                         const CBlockRec* __restrict__ cblk,
+                                                         const OpBlockRec* __restrict__ ops,
+                                                         const int32_t* __restrict__ tab,
+                                                         const __nv_bfloat16* __restrict__ panels, int64_t plane,
+                                                         const int32_t* __restrict__ exps, double* __restrict__ C) {
+    constexpr int T = GEMM_TILE, TK = 16, KCHUNK = 256, LD = TK + 8;  // row stride 48 B: 16-B aligned, no ldmatrix conflicts
+    __shared__ __align__(16) __nv_bfloat16 As[2][S][T][LD];
+    __shared__ __align__(16) __nv_bfloat16 Bs[2][S][T][LD];
+    __shared__ int ea[T], eb[T];
+    const ItemRec it = items[blockIdx.x];
+    const CBlockRec cb = cblk[it.c];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = (warp & 1) * 16, wn = (warp >> 1) * 16;  // warp tile 16x16 = 2 mma n-tiles
+    const int g = lane >> 2, tg = lane & 3;
+    // ldmatrix lane addresses (see the m16n8k16 fragment layouts)
+    const int a_row = wm + (lane & 15), a_col = (lane >> 4) * 8;
+    const int b_row = wn + (lane & 7) + ((lane >> 4) << 3), b_col = ((lane >> 3) & 1) * 8;
+    double out[2][4];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[j][q] = 0.0;
+    for (int p = it.p0; p < it.p1; ++p) {
+        const PairRec pr = pairs[p];
+        const OpBlockRec oa = ops[pr.ia], ob = ops[pr.ib];
+        const __nv_bfloat16* pa = panels + oa.panel;
+        const __nv_bfloat16* pb = panels + ob.panel;
+        // stage k-step k0 into ring slot `buf`: S planes x 32 rows x 2 halves, for A and B
+        auto stage = [&](int k0, int buf) {
+            for (int e = tid; e < 2 * S * T * 2; e += 128) {
+                const int half = e & 1, row = (e >> 1) % T, s = ((e >> 1) / T) % S, isb = (e >> 1) / (T * S);
+                if (!isb) {
+                    const bool ok = it.m0 + row < cb.M;
+                    const __nv_bfloat16* src = ok ? pa + s * plane + (int64_t)(it.m0 + row) * oa.Kp + k0 + half * 8 : pa;
+                    cp_async16(&As[buf][s][row][half * 8], src, ok);
+                } else {
+                    const bool ok = it.n0 + row < cb.N;
+                    const __nv_bfloat16* src = ok ? pb + s * plane + (int64_t)(it.n0 + row) * ob.Kp + k0 + half * 8 : pb;
+                    cp_async16(&Bs[buf][s][row][half * 8], src, ok);
+                }
+            }
+            cp_async_commit();
+        };
+        if (tid < T) ea[tid] = (it.m0 + tid < cb.M) ? exps[oa.exp + it.m0 + tid] : 0;
+        else if (tid < 2 * T) eb[tid - T] = (it.n0 + tid - T < cb.N) ? exps[ob.exp + it.n0 + tid - T] : 0;
+        long long tot[2][4];
+        float acc[S][2][4];
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                tot[j][q] = 0;
+#pragma unroll
+                for (int d = 0; d < S; ++d) acc[d][j][q] = 0.f;
+            }
+        const int nk = (pr.K + TK - 1) / TK;
+        int kacc = 0;
+        stage(0, 0);
+        for (int kk = 0; kk < nk; ++kk) {
+            const int buf = kk & 1;
+            if (kk + 1 < nk) {
+                stage((kk + 1) * TK, buf ^ 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncthreads();
+            uint32_t bfr[S][4];
+#pragma unroll
+            for (int t = 0; t < S; ++t) ldmatrix_x4(bfr[t], &Bs[buf][t][b_row][b_col]);
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                uint32_t af[4];
+                ldmatrix_x4(af, &As[buf][s][a_row][a_col]);
+#pragma unroll
+                for (int t = 0; t + s < S; ++t)
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        float* c = acc[s + t][j];
+                        asm volatile(
+                            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                            "{%8,%9}, {%0,%1,%2,%3};\n"
+                            : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                            : "r"(af[0]), "r"(af[1]), "r"(af[2]), "r"(af[3]), "r"(bfr[t][2 * j]),
+                              "r"(bfr[t][2 * j + 1]));
+                    }
+            }
+            __syncthreads();  // ring slot `buf` is refilled by the next stage()
+            kacc += TK;
+            if (kacc >= KCHUNK || kk + 1 == nk) {
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        long long v = 0;
+#pragma unroll
+                        for (int d = 0; d < S; ++d) {
+                            v += (long long)__float2ll_rn(acc[d][j][q]) << (7 * (S - 1 - d));
+                            acc[d][j][q] = 0.f;
+                        }
+                        tot[j][q] += v;
+                    }
+                kacc = 0;
+            }
+        }
+        // value = tot * 2^(e_row + e_col - 7 S - 7): one FP64 scale per output and pair
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int r = wm + g + (q >= 2 ? 8 : 0);
+                const int cc = wn + j * 8 + tg * 2 + (q & 1);
+                out[j][q] += ldexp((double)tot[j][q], ea[r] + eb[cc] - 7 * S - 7);
+            }
+        __syncthreads();  // ea/eb are rewritten by the next pair
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int m = it.m0 + wm + g + (q >= 2 ? 8 : 0);
+            const int n = it.n0 + wn + j * 8 + tg * 2 + (q & 1);
+            if (m < cb.M && n < cb.N) C[cb.coff + tab[cb.tcm + m] + tab[cb.tcn + n]] = out[j][q];
+        }
+}
+
+template <int S>
+static void launch_s(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, __nv_bfloat16* panels,
+                     int64_t plane, int32_t* exps) {
+    ozaki_prep_kernel<S><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
+    gemm_ozaki_kernel<S><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels,
+                                                           plane, exps, C);
+}
+
+void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S,
+                  __nv_bfloat16* panels, int32_t* exps) {
+    const int64_t plane = (p.panel_elems + 15) / 16 * 16;
+    switch (S) {
+        case 3: launch_s<3>(ctx, p, A, B, C, panels, plane, exps); break;
+        case 4: launch_s<4>(ctx, p, A, B, C, panels, plane, exps); break;
+        case 5: launch_s<5>(ctx, p, A, B, C, panels, plane, exps); break;
+        default: launch_s<6>(ctx, p, A, B, C, panels, plane, exps); break;
+    }
+    ITG_CHECK_CUDA(cudaGetLastError());
+}
+
+}  // namespace itg
