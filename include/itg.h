@@ -127,6 +127,22 @@ int itg_plan_flops(const itg_plan* plan, double* flops);
 int itg_contract_exec(itg_ctx* ctx, const itg_plan* plan, const double* A, const double* B, double* C, int precision);
 void itg_plan_free(itg_plan* plan);
 
+/* No counterpart in the reference: an allocation-free variant of
+ * itg_contract_exec with the split-precision arithmetic (slices 3..6).
+ * For callers that cannot let a library allocate device memory during a call
+ * (another framework's allocator owns the device pool, a real-time loop cannot
+ * take an allocation's implicit synchronisation, a sandbox forbids cudaMalloc
+ * after start-up). The plan (built earlier by itg_contract_plan) and the
+ * operands are the caller's; the digit-panel scratch lives in one fixed
+ * device array of ITG_NOALLOC_SCRATCH_BYTES per device, held until exit.
+ * A plan needing more scratch is rejected with ITG_ERR_RANGE. The first call
+ * on a device looks up the array's address (cudaGetSymbolAddress) and should
+ * come before any stream capture. Calls share the array: calls that overlap on
+ * the GPU race. Nothing in the array needs to start at zero. */
+#define ITG_NOALLOC_SCRATCH_BYTES (16u << 20)
+int itg_contract_exec_noalloc(itg_ctx* ctx, const itg_plan* plan, const double* A, const double* B, double* C,
+                              int slices);
+
 /* ---------------------------------------------------------------- H_eff
  * LocalOp::product, itensor/mps/localop.h:324-365: out = noPrime(((phi*L)*W1)*W2*R)
  * (L or R may be NULL at the chain ends). The output has the block structure

@@ -78,6 +78,7 @@ SIGNATURES = {
     "itg_plan_flops": (C.c_int, [C.c_void_p, _f64p]),
     "itg_contract_exec": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "itg_plan_free": (None, [C.c_void_p]),
+    "itg_contract_exec_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "itg_heff_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                  C.POINTER(C.c_void_p)]),
     "itg_heff_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
@@ -387,6 +388,12 @@ class Context:
     def contract_exec(self, plan, a_ptr, b_ptr, c_ptr, precision=-1):
         self._ok(lib().itg_contract_exec(self.h, plan.h, C.c_void_p(a_ptr), C.c_void_p(b_ptr), C.c_void_p(c_ptr),
                                          precision), self.h)
+
+    def contract_exec_noalloc(self, plan, a_ptr, b_ptr, c_ptr, slices=6):
+        """Split-precision exec of a plan with the library's fixed device scratch
+        array (allocates nothing; see itg_contract_exec_noalloc)."""
+        self._ok(lib().itg_contract_exec_noalloc(self.h, plan.h, C.c_void_p(a_ptr), C.c_void_p(b_ptr),
+                                                 C.c_void_p(c_ptr), slices), self.h)
 
     # ---- DMRG pieces
     def heff_apply(self, L, W1, W2, R, phi, precision=-1):

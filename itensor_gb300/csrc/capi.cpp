@@ -302,6 +302,13 @@ int itg_contract_exec(itg_ctx* c, const itg_plan* p, const double* A, const doub
 
 void itg_plan_free(itg_plan* p) { delete p; }
 
+int itg_contract_exec_noalloc(itg_ctx* c, const itg_plan* p, const double* A, const double* B, double* C, int slices) {
+    return guard(c, [&] {
+        ITG_REQUIRE(p && A && B && C, "contract_exec_noalloc: null argument");
+        exec_plan_noalloc(c->ctx, *p->p, A, B, C, slices);
+    });
+}
+
 int itg_heff_apply(itg_ctx* c, const itg_tensor* L, const itg_tensor* W1, const itg_tensor* W2, const itg_tensor* R,
                    const itg_tensor* phi, int precision, itg_tensor** out) {
     return guard(c, [&] {

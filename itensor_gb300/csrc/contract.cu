@@ -869,6 +869,17 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
     }
 }
 
+void exec_plan_f64_only(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C) {
+    if (p.nitems == 0) return;
+    if (p.skinny)
+        gemm_f64_skinny_kernel<<<p.nitems, SKINNY_M, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+    else
+        gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches++;
+    ctx.flops_done += p.flops;
+}
+
 Tensor contract(Ctx& ctx, Tensor const& A, Tensor const& B, int prec, std::shared_ptr<Layout> target) {
     ITG_REQUIRE(A.valid() && B.valid(), "contract: null tensor");
     Match mt = match_indices(A.inds(), B.inds());

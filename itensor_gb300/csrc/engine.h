@@ -132,6 +132,12 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
 Tensor contract(Ctx& ctx, Tensor const& A, Tensor const& B, int prec = -1,
                 std::shared_ptr<Layout> target = nullptr);
 
+// FP64 kernels of a plan (skinny or tiled), no scratch, no allocation (contract.cu).
+void exec_plan_f64_only(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C);
+// Split-precision exec with the fixed device scratch array instead of pool
+// memory (noalloc.cu); allocates nothing.
+void exec_plan_noalloc(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S);
+
 // Split-precision prep + GEMM launches for a plan (ozaki.cu); panels/exps are
 // the plan's scratch (S digit planes of the padded panel size, row exponents).
 void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S, __nv_bfloat16* panels,
