@@ -181,6 +181,15 @@ int itg_denmat_decomp(itg_ctx* ctx, const itg_tensor* AA, const itg_tensor* A, c
                       int precision, itg_tensor** A_out, itg_tensor** B_out, double* truncerr, double* eigs,
                       int32_t* neigs);
 
+/* SVD route of the bond split: svd (itensor/decomp.cc:121-248) with svdImpl's
+ * QN branch (itensor/svd.cc:169-401), as MPS::svdBond uses it with UseSVD or
+ * cutoff < 1e-12 (itensor/mps/mps_impl.h:50-65). A's indices that B lacks go to
+ * U; the singular values (normalised when normalize != 0) are pushed into B
+ * (fromleft) or A. eigs receives the kept squared singular values. */
+int itg_svd_split(itg_ctx* ctx, const itg_tensor* AA, const itg_tensor* A, const itg_tensor* B, int fromleft,
+                  double cutoff, int32_t maxdim, int32_t mindim, int respect_degenerate, int normalize, int precision,
+                  itg_tensor** A_out, itg_tensor** B_out, double* truncerr, double* eigs, int32_t* neigs);
+
 /* truncate, itensor/decomp.cc:305-463 (host function, same decisions and
  * values as the reference). P sorted descending; Pout capacity n. */
 int itg_truncate(const double* P, int32_t n, int32_t maxdim, int32_t mindim, double cutoff, int absolute_cutoff,
@@ -205,7 +214,8 @@ typedef struct {
     int32_t maxdim, mindim;
     double cutoff;
     int32_t niter;
-    double noise; /* must be 0 */
+    double noise;    /* must be 0 */
+    int32_t use_svd; /* 1: SVD bond split; 0: SVD only when cutoff < 1e-12, else density matrix */
 } itg_sweep_desc;
 
 int itg_dmrg_run(itg_ctx* ctx, const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps,

@@ -45,7 +45,7 @@ class ModelDesc(C.Structure):
 
 class SweepDesc(C.Structure):
     _fields_ = [("maxdim", C.c_int32), ("mindim", C.c_int32), ("cutoff", C.c_double), ("niter", C.c_int32),
-                ("noise", C.c_double)]
+                ("noise", C.c_double), ("use_svd", C.c_int32)]
 
 
 # every exported symbol with its C signature (restype, argtypes)
@@ -90,6 +90,9 @@ SIGNATURES = {
     "itg_denmat_decomp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int32,
                                     C.c_int32, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p),
                                     C.POINTER(C.c_void_p), _f64p, _f64p, _i32p]),
+    "itg_svd_split": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int32,
+                                C.c_int32, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p),
+                                C.POINTER(C.c_void_p), _f64p, _f64p, _i32p]),
     "itg_truncate": (C.c_int, [_f64p, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int, C.c_int, C.c_int, _f64p,
                                _i32p, _f64p, _f64p, _f64p, _i32p]),
     "itg_dmrg_run": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.POINTER(SweepDesc), C.c_int32, C.c_int,
@@ -431,6 +434,18 @@ class Context:
                                          C.byref(bo), C.byref(te), _p(eigs, C.c_double), C.byref(n)), self.h)
         return Tensor(self, ao), Tensor(self, bo), eigs[:n.value].copy(), te.value
 
+    def svd_split(self, AA, A, B, fromleft, cutoff, maxdim, mindim=1, respect_degenerate=True, normalize=True,
+                  precision=-1):
+        ao, bo = C.c_void_p(), C.c_void_p()
+        te = C.c_double()
+        cap = 1 << 16
+        eigs = np.zeros(cap)
+        n = C.c_int32(cap)
+        self._ok(lib().itg_svd_split(self.h, AA.h, A.h, B.h, int(fromleft), cutoff, maxdim, mindim,
+                                     int(respect_degenerate), int(normalize), precision, C.byref(ao),
+                                     C.byref(bo), C.byref(te), _p(eigs, C.c_double), C.byref(n)), self.h)
+        return Tensor(self, ao), Tensor(self, bo), eigs[:n.value].copy(), te.value
+
     def dmrg(self, model, sweeps, precision=-1):
         """model: dict(type, N, J, Jz, J2, h, t, U, Lx, Ly, yperiodic); sweeps: list of
         dict(maxdim, mindim, cutoff, niter)."""
@@ -439,7 +454,8 @@ class Context:
                        float(model.get("h", 0.0)), float(model.get("t", 1.0)), float(model.get("U", 0.0)),
                        int(model.get("Lx", 0)), int(model.get("Ly", 1)), int(model.get("yperiodic", 0)))
         sw = (SweepDesc * len(sweeps))(*[SweepDesc(int(s["maxdim"]), int(s.get("mindim", 1)), float(s["cutoff"]),
-                                                   int(s.get("niter", 2)), float(s.get("noise", 0.0)))
+                                                   int(s.get("niter", 2)), float(s.get("noise", 0.0)),
+                                                   int(s.get("use_svd", 0)))
                                          for s in sweeps])
         out = C.c_void_p()
         self._ok(lib().itg_dmrg_run(self.h, C.byref(md), sw, len(sweeps), precision, C.byref(out)), self.h)

@@ -59,7 +59,11 @@ struct HeffProgram {
         Tensor operand;        // L, W1, W2 or R
         bool operand_left;     // operand is the left factor of the contraction
         int in_buf, out_buf;   // -1 = program input, -2 = program output, else intermediate
+        bool split = false;    // split-precision kernels; scratch holds the digit panels
+        DevBufPtr scratch;
+        bool operand_sliced = false;  // the fixed operand's panels are in place
     };
+    int slices = 6;
     std::vector<Step> steps;
     std::vector<DevBufPtr> inter;
     DevBufPtr in, out;
@@ -99,6 +103,13 @@ struct SplitResult {
 // (itensor/hermitian.cc:180-426) and the DoNormalize step of MPS::svdBond.
 SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor const& B, bool fromleft,
                           SplitArgs const& args, int prec);
+
+// svd route of MPS::svdBond (itensor/mps/mps_impl.h:50-65): svd
+// (itensor/decomp.cc:121-248) with svdImpl's QN branch (itensor/svd.cc:169-401);
+// A's indices not on B go to U. The singular values (normalised when
+// args.normalize) are pushed into B (fromleft) or A. probs = kept s^2.
+SplitResult svd_split(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor const& B, bool fromleft,
+                      SplitArgs const& args, int prec);
 
 // ---------------------------------------------------------------- models / MPO / MPS
 struct SiteType {
@@ -142,7 +153,13 @@ std::vector<Tensor> product_mps(Ctx& ctx, MPO const& H, SiteType const& st, std:
 std::vector<int> default_state(ModelSpec const& m);
 
 // ---------------------------------------------------------------- DMRG
-struct SweepSpec { long maxdim = 0, mindim = 1; double cutoff = 0; int niter = 2; double noise = 0; };
+struct SweepSpec {
+    long maxdim = 0, mindim = 1;
+    double cutoff = 0;
+    int niter = 2;
+    double noise = 0;
+    bool use_svd = false;  // as UseSVD; the SVD route is also taken when cutoff < 1e-12
+};
 struct BondRecord { int sweep, halfsweep, bond; double energy, truncerr; long dim; };
 struct DmrgResult {
     double energy = 0;

@@ -398,6 +398,29 @@ int itg_denmat_decomp(itg_ctx* c, const itg_tensor* AA, const itg_tensor* A, con
     });
 }
 
+int itg_svd_split(itg_ctx* c, const itg_tensor* AA, const itg_tensor* A, const itg_tensor* B, int fromleft,
+                  double cutoff, int32_t maxdim, int32_t mindim, int respect_degenerate, int normalize, int precision,
+                  itg_tensor** A_out, itg_tensor** B_out, double* truncerr, double* eigs, int32_t* neigs) {
+    return guard(c, [&] {
+        ITG_REQUIRE(AA && A && B && A_out && B_out, "svd_split: null argument");
+        SplitArgs sa;
+        sa.cutoff = cutoff;
+        sa.maxdim = maxdim;
+        sa.mindim = mindim;
+        sa.respect_degenerate = respect_degenerate != 0;
+        sa.normalize = normalize != 0;
+        SplitResult r = svd_split(c->ctx, AA->t, A->t, B->t, fromleft != 0, sa, precision);
+        *A_out = new itg_tensor{r.A};
+        *B_out = new itg_tensor{r.B};
+        if (truncerr) *truncerr = r.truncerr;
+        if (neigs) {
+            int cap = *neigs;
+            *neigs = (int32_t)r.probs.size();
+            if (eigs) for (int i = 0; i < std::min<int>(cap, (int)r.probs.size()); ++i) eigs[i] = r.probs[i];
+        }
+    });
+}
+
 int itg_truncate(const double* P, int32_t n, int32_t maxdim, int32_t mindim, double cutoff, int absolute_cutoff,
                  int rel_cutoff, int respect_degenerate, double* Pout, int32_t* m, double* truncerr,
                  double* docut_lower, double* docut_upper, int32_t* ndegen) {
@@ -433,6 +456,7 @@ int itg_dmrg_run(itg_ctx* c, const itg_model_desc* model, const itg_sweep_desc* 
             sw[s].mindim = sweeps[s].mindim;
             sw[s].cutoff = sweeps[s].cutoff;
             sw[s].niter = sweeps[s].niter;
+            sw[s].use_svd = sweeps[s].use_svd != 0;
         }
         auto* res = new itg_dmrg_result;
         try {

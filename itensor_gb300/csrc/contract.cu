@@ -313,48 +313,83 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
 // MPO-tensor steps of the H_eff apply: N = (s', w') <= 3, K = (s, w) <= 3).
 // One thread per output row keeps all N sums in registers; the B block
 // (K x N) is staged in shared memory. Tiles are SKINNY_M rows of one block.
-constexpr int SKINNY_N = 8, SKINNY_M = 256, SKINNY_K = 64;
+constexpr int SKINNY_N = 8, SKINNY_THREADS = 256, SKINNY_R = 4, SKINNY_M = SKINNY_THREADS * SKINNY_R, SKINNY_K = 64;
 
-__global__ void __launch_bounds__(SKINNY_M) gemm_f64_skinny_kernel(const ItemRec* __restrict__ items,
-                                                                   const PairRec* __restrict__ pairs,
-                                                                   const CBlockRec* __restrict__ cblk,
-                                                                   const int32_t* __restrict__ tab,
-                                                                   const double* __restrict__ A,
-                                                                   const double* __restrict__ B,
-                                                                   double* __restrict__ C) {
-    __shared__ double Bs[SKINNY_K][SKINNY_N];
-    const ItemRec it = items[blockIdx.x];
-    const CBlockRec cb = cblk[it.c];
-    const int m = it.m0 + threadIdx.x;
-    const bool active = m < cb.M;
-    double acc[SKINNY_N];
+// NN = exact output width of the block (1..SKINNY_N). Rows m0 + t + j*256,
+// j < SKINNY_R, per thread. Zero entries of the staged B block are skipped with
+// a branch that is uniform over the CTA (MPO-tensor blocks are mostly zeros,
+// and FP64 issue slots bound this step).
+template <int NN>
+__device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& cb, const PairRec* __restrict__ pairs,
+                                            const int32_t* __restrict__ tab, const double* __restrict__ A,
+                                            const double* __restrict__ B, double* __restrict__ C,
+                                            double (*Bs)[SKINNY_N]) {
+    double acc[SKINNY_R][NN];
 #pragma unroll
-    for (int n = 0; n < SKINNY_N; ++n) acc[n] = 0.0;
+    for (int j = 0; j < SKINNY_R; ++j)
+#pragma unroll
+        for (int n = 0; n < NN; ++n) acc[j][n] = 0.0;
+    int mrow[SKINNY_R];
+#pragma unroll
+    for (int j = 0; j < SKINNY_R; ++j) mrow[j] = it.m0 + threadIdx.x + j * SKINNY_THREADS;
     for (int p = it.p0; p < it.p1; ++p) {
         const PairRec pr = pairs[p];
-        const int arow = active ? tab[pr.tam + m] : 0;
+        int arow[SKINNY_R];
+#pragma unroll
+        for (int j = 0; j < SKINNY_R; ++j) arow[j] = mrow[j] < cb.M ? tab[pr.tam + mrow[j]] : -1;
         for (int k0 = 0; k0 < pr.K; k0 += SKINNY_K) {
             const int kn = min(SKINNY_K, pr.K - k0);
             __syncthreads();
-            for (int e = threadIdx.x; e < kn * SKINNY_N; e += blockDim.x) {
-                int k = e / SKINNY_N, n = e % SKINNY_N;
-                Bs[k][n] = (n < cb.N) ? B[pr.boff + tab[pr.tbk + k0 + k] + tab[pr.tbn + n]] : 0.0;
+            for (int e = threadIdx.x; e < kn * NN; e += blockDim.x) {
+                int k = e / NN, n = e % NN;
+                Bs[k][n] = B[pr.boff + tab[pr.tbk + k0 + k] + tab[pr.tbn + n]];
             }
             __syncthreads();
-            if (active) {
-                for (int k = 0; k < kn; ++k) {
-                    const double a = A[pr.aoff + arow + tab[pr.tak + k0 + k]];
+            for (int k = 0; k < kn; ++k) {
+                const int ko = tab[pr.tak + k0 + k];
+                double a[SKINNY_R];
 #pragma unroll
-                    for (int n = 0; n < SKINNY_N; ++n) acc[n] = fma(a, Bs[k][n], acc[n]);
+                for (int j = 0; j < SKINNY_R; ++j) a[j] = arow[j] >= 0 ? A[pr.aoff + arow[j] + ko] : 0.0;
+#pragma unroll
+                for (int n = 0; n < NN; ++n) {
+                    const double b = Bs[k][n];
+                    if (b != 0.0) {
+#pragma unroll
+                        for (int j = 0; j < SKINNY_R; ++j) acc[j][n] = fma(a[j], b, acc[j][n]);
+                    }
                 }
             }
         }
     }
-    if (active) {
-        const int64_t crow = cb.coff + tab[cb.tcm + m];
 #pragma unroll
-        for (int n = 0; n < SKINNY_N; ++n)
-            if (n < cb.N) C[crow + tab[cb.tcn + n]] = acc[n];
+    for (int j = 0; j < SKINNY_R; ++j) {
+        if (mrow[j] < cb.M) {
+            const int64_t crow = cb.coff + tab[cb.tcm + mrow[j]];
+#pragma unroll
+            for (int n = 0; n < NN; ++n) C[crow + tab[cb.tcn + n]] = acc[j][n];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_kernel(const ItemRec* __restrict__ items,
+                                                                         const PairRec* __restrict__ pairs,
+                                                                         const CBlockRec* __restrict__ cblk,
+                                                                         const int32_t* __restrict__ tab,
+                                                                         const double* __restrict__ A,
+                                                                         const double* __restrict__ B,
+                                                                         double* __restrict__ C) {
+    __shared__ double Bs[SKINNY_K][SKINNY_N];
+    const ItemRec it = items[blockIdx.x];
+    const CBlockRec cb = cblk[it.c];
+    switch (cb.N) {
+        case 1: skinny_item<1>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 2: skinny_item<2>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 3: skinny_item<3>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 4: skinny_item<4>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 5: skinny_item<5>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 6: skinny_item<6>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 7: skinny_item<7>(it, cb, pairs, tab, A, B, C, Bs); break;
+        default: skinny_item<8>(it, cb, pairs, tab, A, B, C, Bs); break;
     }
 }
 
@@ -759,6 +794,8 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         if (!ops.empty()) std::memcpy(st + t_ops, ops.data(), sizeof(OpBlockRec) * ops.size());
         if (!prep.empty()) std::memcpy(st + t_prep, prep.data(), sizeof(PrepItem) * prep.size());
         plan->nprep = (int)prep.size();
+        plan->nprepA = 0;
+        for (auto const& it : prep) plan->nprepA += (it.which == 0);
         if (!tab.empty()) std::memcpy(st + t_tab, tab.data(), sizeof(int32_t) * tab.size());
         plan->nopsA = nopsA;
         plan->nopsB = nopsB;
@@ -843,7 +880,7 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
     }
     // narrow, small-K contractions (the MPO-tensor steps) are bandwidth-shaped: FP64 is exact there
     if (p.skinny && (prec == PREC_F64 || prec == PREC_OZAKI_BF16)) {
-        gemm_f64_skinny_kernel<<<p.nitems, SKINNY_M, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+        gemm_f64_skinny_kernel<<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
     } else if (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) {
         const int S = ctx.ozaki_slices;
         const int64_t plane = (p.panel_elems + 15) / 16 * 16;
@@ -872,7 +909,7 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
 void exec_plan_f64_only(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C) {
     if (p.nitems == 0) return;
     if (p.skinny)
-        gemm_f64_skinny_kernel<<<p.nitems, SKINNY_M, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+        gemm_f64_skinny_kernel<<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
     else
         gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
     ITG_CHECK_CUDA(cudaGetLastError());

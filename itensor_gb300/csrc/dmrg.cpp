@@ -76,7 +76,10 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
             sa.mindim = s.mindim;
             sa.respect_degenerate = true;
             sa.normalize = true;
-            SplitResult sr = denmat_decomp(ctx, phi, A, B, ha == 1, sa, prec);
+            // MPS::svdBond: SVD when UseSVD or (noise == 0 and cutoff < 1e-12), else density matrix
+            const bool svd_route = s.use_svd || s.cutoff < 1e-12;
+            SplitResult sr = svd_route ? svd_split(ctx, phi, A, B, ha == 1, sa, prec)
+                                       : denmat_decomp(ctx, phi, A, B, ha == 1, sa, prec);
             psi[b - 1] = sr.A;
             psi[b] = sr.B;
             res.bonds.push_back(BondRecord{(int)sw + 1, ha, b, energy, sr.truncerr, (long)sr.link.dim()});

@@ -67,7 +67,7 @@ struct Plan {
     // split-precision operand panels (A blocks, then B blocks)
     OpBlockRec* d_ops = nullptr;
     PrepItem* d_prep = nullptr;
-    int nprep = 0;
+    int nprep = 0, nprepA = 0;      // prep items: A operand first, then B
     int nopsA = 0, nopsB = 0;
     int64_t panel_elems = 0;         // bf16 elements per digit plane set (all blocks)
     int64_t exp_elems = 0;
@@ -141,7 +141,16 @@ void exec_plan_noalloc(Ctx& ctx, Plan const& p, double const* A, double const* B
 // Split-precision prep + GEMM launches for a plan (ozaki.cu); panels/exps are
 // the plan's scratch (S digit planes of the padded panel size, row exponents).
 void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S, __nv_bfloat16* panels,
-                  int32_t* exps);
+                  int32_t* exps, bool prep_b = true);
+// Whether exec_plan runs this plan with the split-precision kernels.
+inline bool plan_uses_split(Plan const& p, int prec) {
+    return !p.skinny && prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0;
+}
+// Bytes of split-precision scratch (digit planes + row exponents) a plan needs.
+inline size_t split_scratch_bytes(Plan const& p, int S) {
+    const int64_t plane = (p.panel_elems + 15) / 16 * 16;
+    return sizeof(__nv_bfloat16) * (size_t)plane * S + sizeof(int32_t) * (size_t)(p.exp_elems + 4);
+}
 
 // TFLOP/s of [FP64 FFMA, FP32 FFMA, FP64 mma.sync, TF32 mma.sync, BF16 mma.sync] (peaks.cu)
 void measure_peaks(Ctx& ctx, double* tflops);

@@ -17,6 +17,7 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
     auto P = std::make_shared<HeffProgram>();
     P->prec = prec < 0 ? ctx.precision : prec;
     P->use_graph = use_graph;
+    P->slices = ctx.ozaki_slices;
     std::vector<Tensor const*> chain;
     if (!op.L) {
         if (op.R) chain.push_back(op.R);
@@ -54,6 +55,8 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
         st.operand = *chain[s];
         st.operand_left = false;
         st.in_buf = (s == 0) ? -1 : (int)P->inter.size() - 1;
+        st.split = plan_uses_split(*plan, P->prec);
+        if (st.split) st.scratch = dev_alloc(split_scratch_bytes(*plan, P->slices), ctx.stream);
         if (last) {
             st.out_buf = -2;
             P->out_size = outL->size;
@@ -79,7 +82,32 @@ void HeffProgram::launch_steps(Ctx& ctx) {
     for (auto& st : steps) {
         double const* a = st.in_buf == -1 ? in->as<double>() : inter[st.in_buf]->as<double>();
         double* c = st.out_buf == -2 ? out->as<double>() : inter[st.out_buf]->as<double>();
-        exec_plan(ctx, *st.plan, a, st.operand.data(), c, prec);
+        if (st.split) {
+            // the operand (L, W or R) is fixed for the program's life: slice it once
+            Plan const& p = *st.plan;
+            const int64_t plane = (p.panel_elems + 15) / 16 * 16;
+            __nv_bfloat16* panels = st.scratch->as<__nv_bfloat16>();
+            int32_t* exps = reinterpret_cast<int32_t*>(panels + plane * slices);
+            ProfRec pr{};
+            if (ctx.profiling) {
+                ITG_CHECK_CUDA(cudaEventCreate(&pr.start));
+                ITG_CHECK_CUDA(cudaEventCreate(&pr.stop));
+                ITG_CHECK_CUDA(cudaEventRecord(pr.start, ctx.stream));
+                pr.flops = p.flops;
+                pr.kind = 1;
+                pr.nitems = p.nitems;
+            }
+            launch_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps, !st.operand_sliced);
+            if (ctx.profiling) {
+                ITG_CHECK_CUDA(cudaEventRecord(pr.stop, ctx.stream));
+                ctx.prof.push_back(pr);
+            }
+            ctx.kernel_launches += (!st.operand_sliced || p.nprepA > 0) ? 2 : 1;
+            ctx.flops_done += p.flops;
+            st.operand_sliced = true;
+        } else {
+            exec_plan(ctx, *st.plan, a, st.operand.data(), c, prec);
+        }
     }
 }
 

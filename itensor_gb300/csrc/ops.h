@@ -36,6 +36,19 @@ struct EigItem {
     int32_t pad;
 };
 
+// One block to decompose by singular values: X = the m x n (m >= n) matrix read
+// from src at a_off with leading dimension ld (transpose != 0: X = that matrix
+// transposed, i.e. element (i,j) at a_off + j + i*ld). Outputs, singular
+// values descending: U (m x n) at u_off, sigma (n) at s_out, V (n x n) at v_off,
+// with X = U diag(sigma) V^T. Scratch: m n + n n + n doubles at s_off.
+struct SvdItem {
+    int64_t a_off, u_off, v_off, s_off;
+    int64_t s_out;
+    int32_t rows, cols, ld, transpose;
+};
+int batched_svd(Ctx& ctx, std::vector<SvdItem> const& items, double const* src, double* uout, double* sout,
+                double* vout, double* scratch);
+
 // Diagonalises every item; returns the number of items that hit the sweep cap.
 int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
                  double* scratch);

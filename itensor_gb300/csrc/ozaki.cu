@@ -72,6 +72,29 @@ __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restr
     }
 }
 
+// v * 2^e as FP64, built with integer instructions (round to nearest, ties to
+// even): the FP64 unit issues ~1/60 of the FP32 rate on this part. Values stay
+// in the normal range here (|v| < 2^63, e >= -1100 with nonzero v well above).
+__device__ __forceinline__ double scaled_i64(long long v, int e) {
+    if (v == 0) return 0.0;
+    const unsigned long long sign = v < 0 ? (1ull << 63) : 0ull;
+    unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+    int msb = 63 - __clzll(u);
+    unsigned long long mant;
+    if (msb > 52) {
+        const int sh = msb - 52;
+        mant = u >> sh;
+        const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+        if (mant >> 53) { mant >>= 1; ++msb; }
+    } else {
+        mant = u << (52 - msb);
+    }
+    const long long ex = (long long)msb + e + 1023;
+    if (ex <= 0) return 0.0;  // below the normal range: negligible against the tile's scale
+    return __longlong_as_double((long long)(sign | ((unsigned long long)ex << 52) | (mant & ((1ull << 52) - 1))));
+}
+
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
     const unsigned saddr = (unsigned)__cvta_generic_to_shared(smem);
     const int bytes = valid ? 16 : 0;  // 0: zero-fill, nothing read
@@ -203,7 +226,8 @@ __global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __res
             for (int q = 0; q < 4; ++q) {
                 const int r = wm + g + (q >= 2 ? 8 : 0);
                 const int cc = wn + j * 8 + tg * 2 + (q & 1);
-                out[j][q] += ldexp((double)tot[j][q], ea[r] + eb[cc] - 7 * S - 7);
+                const double v = scaled_i64(tot[j][q], ea[r] + eb[cc] - 7 * S - 7);
+                out[j][q] = (p == it.p0) ? v : out[j][q] + v;
             }
         __syncthreads();  // ea/eb are rewritten by the next pair
     }
@@ -219,20 +243,23 @@ __global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __res
 
 template <int S>
 static void launch_s(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, __nv_bfloat16* panels,
-                     int64_t plane, int32_t* exps) {
-    ozaki_prep_kernel<S><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
+                     int64_t plane, int32_t* exps, bool prep_b) {
+    // A items come first: without prep_b only A is sliced (B's panels are already in place)
+    const int nprep = prep_b ? p.nprep : p.nprepA;
+    if (nprep > 0)
+        ozaki_prep_kernel<S><<<nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
     gemm_ozaki_kernel<S><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels,
                                                            plane, exps, C);
 }
 
 void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S,
-                  __nv_bfloat16* panels, int32_t* exps) {
+                  __nv_bfloat16* panels, int32_t* exps, bool prep_b) {
     const int64_t plane = (p.panel_elems + 15) / 16 * 16;
     switch (S) {
-        case 3: launch_s<3>(ctx, p, A, B, C, panels, plane, exps); break;
-        case 4: launch_s<4>(ctx, p, A, B, C, panels, plane, exps); break;
-        case 5: launch_s<5>(ctx, p, A, B, C, panels, plane, exps); break;
-        default: launch_s<6>(ctx, p, A, B, C, panels, plane, exps); break;
+        case 3: launch_s<3>(ctx, p, A, B, C, panels, plane, exps, prep_b); break;
+        case 4: launch_s<4>(ctx, p, A, B, C, panels, plane, exps, prep_b); break;
+        case 5: launch_s<5>(ctx, p, A, B, C, panels, plane, exps, prep_b); break;
+        default: launch_s<6>(ctx, p, A, B, C, panels, plane, exps, prep_b); break;
     }
     ITG_CHECK_CUDA(cudaGetLastError());
 }

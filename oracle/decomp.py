@@ -246,7 +246,8 @@ def svd_split(AA: BSTensor, Uinds, maxdim, mindim, cutoff, respectDegenerate=Tru
     """svd route of MPS::svdBond (itensor/mps/mps_impl.h:50-65): returns
     (A', B', probs, truncerr) with the singular values pushed into the new
     orthogonality centre."""
-    Uinds = [AA.inds[AA.find(I)] for I in Uinds]
+    # U's indices in the order they appear on AA (itensor/decomp.cc:185-192)
+    Uinds = [I for I in AA.inds if any(I.same(J) for J in Uinds)]
     Vinds = [I for I in AA.inds if not any(I.same(J) for J in Uinds)]
     cu = Combiner(Uinds)
     cv = Combiner(Vinds)

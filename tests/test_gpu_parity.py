@@ -195,3 +195,56 @@ def test_dmrg_ozaki_energy_within_1e9(ctx, golden):
     c = [x for x in golden("dmrg")["cases"] if x["name"] == "heis20"][0]
     res = ctx.dmrg(dict(type=0, N=20, J=1.0, Jz=1.0), c["sweeps"], precision=1)
     assert abs(res.energy - c["energy"]) <= 1e-9
+
+
+def test_svd_split_golden(ctx, golden):
+    """SVD route of the bond split against the reference's svd cases."""
+    d = golden("bondsplit")
+    names = qn_names(d)
+    n = 0
+    for c in d["cases"]:
+        if not c["usesvd"]:
+            continue
+        n += 1
+        AA, A, B = (gpu_tensor(ctx, c[k], names) for k in ("AA", "A", "B"))
+        Ao, Bo, eigs, te = ctx.svd_split(AA, A, B, c["fromleft"], c["cutoff"], c["maxdim"], c["mindim"],
+                                         normalize=False)
+        e = np.asarray(c["spec"]["eigs"])
+        assert len(eigs) == len(e), c["name"]
+        assert np.max(np.abs(eigs - e)) < 1e-12 * max(1.0, e[0]), c["name"]
+        assert abs(te - c["spec"]["truncerr"]) < 1e-12 * max(1.0, e[0])
+        link = [I for I in Ao.inds if any(I.same(J) for J in Bo.inds)][0]
+        assert [int(x) for x in link.dims] == [dd for _, dd in json_sectors(c["link"])], c["name"]
+        # A*B reproduces the reference's truncated product
+        AB = ctx.contract(Ao, Bo)
+        ref = T(c["AB"])
+        coords, offs = AB.blocks()
+        pos = [[(int(x["id"]), x["plev"]) for x in c["AB"]["inds"]].index((I.id, I.plev)) for I in AB.inds]
+        data = AB.numpy()
+        scale = max(1.0, np.abs(ref.flat()).max())
+        for cc, o in zip(coords.tolist(), offs):
+            rc = [0] * len(cc)
+            for k, p in enumerate(pos):
+                rc[p] = cc[k]
+            shp = tuple(int(AB.inds[k].dims[cc[k]]) for k in range(len(cc)))
+            blk = data[o:o + int(np.prod(shp))].reshape(shp, order="F")
+            ref_blk = ref.blocks.get(tuple(rc))
+            err = np.max(np.abs(blk)) if ref_blk is None else np.max(np.abs(np.transpose(ref_blk, pos) - blk))
+            assert err < 1e-11 * scale, (c["name"], err)
+    assert n >= 2
+
+
+def test_dmrg_svd_route_matches_oracle(ctx):
+    """DMRG with the SVD bond split (UseSVD) against the CPU oracle's SVD route."""
+    from oracle import models
+    from oracle.dmrg import dmrg as odmrg
+    sweeps = [dict(maxdim=m, mindim=1, cutoff=1e-13, niter=2, use_svd=1) for m in (8, 16, 24)]
+    res = ctx.dmrg(dict(type=0, N=10, J=1.0, Jz=1.0), sweeps, precision=0)
+    H = models.heisenberg(10)
+    sites, W, _ = models.build_mpo(H)
+    psi = models.product_mps(sites, H.st, ["Up" if i % 2 == 0 else "Dn" for i in range(10)])
+    E, _, recs = odmrg(W, psi, sweeps, usesvd=True)
+    assert abs(res.energy - E) < 1e-10
+    for a, b in zip(res.bonds, recs):
+        assert abs(a[3] - b[3]) < 1e-10
+        assert a[5] == b[5]
