@@ -81,6 +81,24 @@ def _oracle_apply_loop(n_applies):
     return time.perf_counter() - t0
 
 
+_WORKER_OP = None
+
+
+def _oracle_worker_init():
+    """Process-pool initializer: the workload and operator are built once per worker."""
+    global _WORKER_OP
+    from oracle.dmrg import LocalOp
+    t = _oracle_setup()
+    _WORKER_OP = (LocalOp(t["W1"], t["W2"], t["L"], t["R"]), t["psi"])
+    _WORKER_OP[0].product(_WORKER_OP[1])  # warm
+
+
+def _oracle_worker_apply(_):
+    op, psi = _WORKER_OP
+    op.product(psi)
+    return 0
+
+
 def _single_thread_env():
     env = dict(os.environ)
     for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
@@ -114,12 +132,12 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     flops = _oracle_flops()
     ctxm = mp.get_context("spawn")
-    with ctxm.Pool(cores) as pool:
+    with ctxm.Pool(cores, initializer=_oracle_worker_init) as pool:
         for _ in range(args.warmup):
-            pool.map(_oracle_apply_loop, [1] * cores)
+            pool.map(_oracle_worker_apply, range(cores), chunksize=1)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            pool.map(_oracle_apply_loop, [1] * cores)
+            pool.map(_oracle_worker_apply, range(cores), chunksize=1)
         el = time.perf_counter() - t0
     # each step: `cores` independent applies in parallel
     value = flops * cores * args.steps / el / 1e12

@@ -227,7 +227,44 @@ int itg_dmrg_bonds(const itg_dmrg_result* r, int32_t* sweep, int32_t* halfsweep,
 /* Final link index b (1..N-1): sectors (4 QN values each) and sizes. */
 int itg_dmrg_link(const itg_dmrg_result* r, int32_t b, int32_t* dir, int32_t* nsect, int32_t* qn, int32_t* dims);
 int itg_dmrg_timing(const itg_dmrg_result* r, int32_t* nsweeps, double* sweep_seconds, int32_t* heff_applies);
+/* Wall seconds spent in [environments + two-site tensor, Davidson, bond split], summed over all bond steps. */
+int itg_dmrg_phases(const itg_dmrg_result* r, double* seconds3);
 void itg_dmrg_free(itg_dmrg_result* r);
+
+/* ---------------------------------------------------------------- solver pool
+ * Many independent ground-state solves (dmrg() as above, one per request) on
+ * one GPU, with continuous batching. Replaces a host loop that calls dmrg()
+ * once per Hamiltonian (sample/dmrg.cc:30-65: MPO, MPS(InitState), Sweeps,
+ * dmrg(H, psi0, sweeps)), one request after the other.
+ *
+ * A request carries a model, a sweep schedule, a precision and an arrival
+ * time (seconds after itg_pool_start; <= 0 means at once). It is admitted
+ * once it has arrived, a slot is free and its device-memory estimate
+ * (itg_pool_estimate) fits in what the budget has left; first come, first
+ * served. `workers` host threads each hold `slots_per_worker` slots; a slot
+ * is a stream of its own, and a worker switches between its solves whenever
+ * one waits for its stream, so every admitted solve has work on the GPU.
+ * Results are identical to a lone itg_dmrg_run with the same arguments.
+ * Requests may be submitted before or after itg_pool_start, from any thread.
+ * Errors of the pool calls are read with itg_last_error(NULL). */
+typedef struct itg_pool itg_pool;
+int itg_pool_create(int device, int32_t workers, int32_t slots_per_worker, double budget_bytes, itg_pool** out);
+int itg_pool_submit(itg_pool* p, const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps,
+                    int precision, double arrival_s, int64_t* id);
+int itg_pool_start(itg_pool* p);
+int itg_pool_drain(itg_pool* p);   /* waits until every submitted request has finished */
+/* status: -1 queued, -2 running, 0 done, else the request's error code (message in itg_pool_error).
+ * Times are seconds after itg_pool_start; latency = t_done - t_arrive. */
+int itg_pool_record(itg_pool* p, int64_t id, int32_t* status, double* energy, double* t_arrive, double* t_admit,
+                    double* t_done, double* est_bytes, double* peak_bytes, int32_t* worker);
+int itg_pool_error(itg_pool* p, int64_t id, char* buf, int32_t buflen);
+/* Full result of a finished request, read with the itg_dmrg_* accessors; free with itg_dmrg_free. */
+int itg_pool_result(itg_pool* p, int64_t id, itg_dmrg_result** out);
+int itg_pool_stats(itg_pool* p, int64_t* submitted, int64_t* done, int64_t* failed, double* peak_reserved_bytes,
+                   int32_t* peak_running, double* elapsed_s);
+int itg_pool_estimate(const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps, int precision,
+                      double* bytes);
+void itg_pool_destroy(itg_pool* p);
 
 #ifdef __cplusplus
 }

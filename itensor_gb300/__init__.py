@@ -102,7 +102,20 @@ SIGNATURES = {
     "itg_dmrg_bonds": (C.c_int, [C.c_void_p, _i32p, _i32p, _i32p, _f64p, _f64p, _i32p]),
     "itg_dmrg_link": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p, _i32p, _i32p]),
     "itg_dmrg_timing": (C.c_int, [C.c_void_p, _i32p, _f64p, _i32p]),
+    "itg_dmrg_phases": (C.c_int, [C.c_void_p, _f64p]),
     "itg_dmrg_free": (None, [C.c_void_p]),
+    "itg_pool_create": (C.c_int, [C.c_int, C.c_int32, C.c_int32, C.c_double, C.POINTER(C.c_void_p)]),
+    "itg_pool_submit": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.POINTER(SweepDesc), C.c_int32, C.c_int,
+                                  C.c_double, C.POINTER(C.c_int64)]),
+    "itg_pool_start": (C.c_int, [C.c_void_p]),
+    "itg_pool_drain": (C.c_int, [C.c_void_p]),
+    "itg_pool_record": (C.c_int, [C.c_void_p, C.c_int64, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _i32p]),
+    "itg_pool_error": (C.c_int, [C.c_void_p, C.c_int64, C.c_char_p, C.c_int32]),
+    "itg_pool_result": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]),
+    "itg_pool_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                 _f64p, _i32p, _f64p]),
+    "itg_pool_estimate": (C.c_int, [C.POINTER(ModelDesc), C.POINTER(SweepDesc), C.c_int32, C.c_int, _f64p]),
+    "itg_pool_destroy": (None, [C.c_void_p]),
 }
 
 _lib = None
@@ -449,46 +462,151 @@ class Context:
     def dmrg(self, model, sweeps, precision=-1):
         """model: dict(type, N, J, Jz, J2, h, t, U, Lx, Ly, yperiodic); sweeps: list of
         dict(maxdim, mindim, cutoff, niter)."""
-        md = ModelDesc(int(model.get("type", 0)), int(model.get("N", 0)), float(model.get("J", 1.0)),
-                       float(model.get("Jz", model.get("J", 1.0))), float(model.get("J2", 0.0)),
-                       float(model.get("h", 0.0)), float(model.get("t", 1.0)), float(model.get("U", 0.0)),
-                       int(model.get("Lx", 0)), int(model.get("Ly", 1)), int(model.get("yperiodic", 0)))
-        sw = (SweepDesc * len(sweeps))(*[SweepDesc(int(s["maxdim"]), int(s.get("mindim", 1)), float(s["cutoff"]),
-                                                   int(s.get("niter", 2)), float(s.get("noise", 0.0)),
-                                                   int(s.get("use_svd", 0)))
-                                         for s in sweeps])
+        md = _model_desc(model)
+        sw = _sweep_descs(sweeps)
         out = C.c_void_p()
         self._ok(lib().itg_dmrg_run(self.h, C.byref(md), sw, len(sweeps), precision, C.byref(out)), self.h)
+        return _take_dmrg_result(out)
+
+
+def _model_desc(model):
+    return ModelDesc(int(model.get("type", 0)), int(model.get("N", 0)), float(model.get("J", 1.0)),
+                     float(model.get("Jz", model.get("J", 1.0))), float(model.get("J2", 0.0)),
+                     float(model.get("h", 0.0)), float(model.get("t", 1.0)), float(model.get("U", 0.0)),
+                     int(model.get("Lx", 0)), int(model.get("Ly", 1)), int(model.get("yperiodic", 0)))
+
+
+def _sweep_descs(sweeps):
+    return (SweepDesc * len(sweeps))(*[SweepDesc(int(s["maxdim"]), int(s.get("mindim", 1)), float(s["cutoff"]),
+                                                 int(s.get("niter", 2)), float(s.get("noise", 0.0)),
+                                                 int(s.get("use_svd", 0)))
+                                       for s in sweeps])
+
+
+def _take_dmrg_result(out):
+    """Reads an itg_dmrg_result handle into a DmrgResult and frees it."""
+    try:
+        L = lib()
+        e = C.c_double()
+        L.itg_dmrg_energy(out, C.byref(e))
+        nb = C.c_int32()
+        L.itg_dmrg_nbonds(out, C.byref(nb))
+        n = nb.value
+        sw_, ha, bb, te, dm = (np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32),
+                               np.zeros(n), np.zeros(n, np.int32))
+        en = np.zeros(n)
+        L.itg_dmrg_bonds(out, _p(sw_, C.c_int32), _p(ha, C.c_int32), _p(bb, C.c_int32), _p(en, C.c_double),
+                         _p(te, C.c_double), _p(dm, C.c_int32))
+        bonds = [(int(sw_[i]), int(ha[i]), int(bb[i]), float(en[i]), float(te[i]), int(dm[i])) for i in range(n)]
+        N = max(b[2] for b in bonds) + 1 if bonds else 0
+        links = []
+        for b in range(1, N):
+            d, ns = C.c_int32(), C.c_int32()
+            L.itg_dmrg_link(out, b, C.byref(d), C.byref(ns), None, None)
+            qn = np.zeros(ns.value * 4, np.int32)
+            dims = np.zeros(ns.value, np.int32)
+            L.itg_dmrg_link(out, b, None, None, _p(qn, C.c_int32), _p(dims, C.c_int32))
+            links.append((d.value, qn.reshape(-1, 4), dims))
+        nsw = C.c_int32()
+        L.itg_dmrg_timing(out, C.byref(nsw), None, None)
+        secs = np.zeros(max(1, nsw.value))
+        ap = C.c_int32()
+        L.itg_dmrg_timing(out, None, _p(secs, C.c_double), C.byref(ap))
+        ph = np.zeros(3)
+        L.itg_dmrg_phases(out, _p(ph, C.c_double))
+        r = DmrgResult(e.value, bonds, links, secs[:nsw.value].tolist(), ap.value)
+        r.phase_seconds = dict(environments=float(ph[0]), davidson=float(ph[1]), bond_split=float(ph[2]))
+        return r
+    finally:
+        lib().itg_dmrg_free(out)
+
+
+class PoolRecord:
+    def __init__(self, id, status, energy, t_arrive, t_admit, t_done, est_bytes, peak_bytes, worker, error):
+        self.id = id
+        self.status = status          # 0 done, -1 queued, -2 running, else an error code
+        self.energy = energy
+        self.t_arrive, self.t_admit, self.t_done = t_arrive, t_admit, t_done
+        self.latency = t_done - t_arrive
+        self.est_bytes, self.peak_bytes = est_bytes, peak_bytes
+        self.worker = worker
+        self.error = error
+
+
+class Pool:
+    """Solver pool (itg_pool_*): many ground-state solves on one GPU with
+    continuous batching and admission by device-memory estimate."""
+
+    def __init__(self, device=0, workers=4, slots_per_worker=4, budget_bytes=None):
+        if budget_bytes is None:
+            budget_bytes = 64 << 30
+        h = C.c_void_p()
+        _check(lib().itg_pool_create(device, workers, slots_per_worker, float(budget_bytes), C.byref(h)))
+        self.h = h
+
+    def submit(self, model, sweeps, precision=0, arrival=0.0):
+        md = _model_desc(model)
+        sw = _sweep_descs(sweeps)
+        i = C.c_int64()
+        _check(lib().itg_pool_submit(self.h, C.byref(md), sw, len(sweeps), precision, float(arrival), C.byref(i)))
+        return i.value
+
+    def start(self):
+        _check(lib().itg_pool_start(self.h))
+
+    def drain(self):
+        _check(lib().itg_pool_drain(self.h))
+
+    def record(self, i):
+        st, wk = C.c_int32(), C.c_int32()
+        e, ta, tad, td, eb, pb = (C.c_double() for _ in range(6))
+        _check(lib().itg_pool_record(self.h, i, C.byref(st), C.byref(e), C.byref(ta), C.byref(tad), C.byref(td),
+                                     C.byref(eb), C.byref(pb), C.byref(wk)))
+        err = ""
+        if st.value not in (0, -1, -2):
+            buf = C.create_string_buffer(4096)
+            _check(lib().itg_pool_error(self.h, i, buf, len(buf)))
+            err = buf.value.decode()
+        return PoolRecord(i, st.value, e.value, ta.value, tad.value, td.value, eb.value, pb.value, wk.value, err)
+
+    def result(self, i):
+        out = C.c_void_p()
+        _check(lib().itg_pool_result(self.h, i, C.byref(out)))
+        return _take_dmrg_result(out)
+
+    def stats(self):
+        s, d, f = C.c_int64(), C.c_int64(), C.c_int64()
+        pr, el = C.c_double(), C.c_double()
+        pk = C.c_int32()
+        _check(lib().itg_pool_stats(self.h, C.byref(s), C.byref(d), C.byref(f), C.byref(pr), C.byref(pk),
+                                    C.byref(el)))
+        return dict(submitted=s.value, done=d.value, failed=f.value, peak_reserved_bytes=pr.value,
+                    peak_running=pk.value, elapsed=el.value)
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().itg_pool_destroy(self.h)
+            self.h = C.c_void_p(None)
+
+    def __del__(self):
         try:
-            L = lib()
-            e = C.c_double()
-            L.itg_dmrg_energy(out, C.byref(e))
-            nb = C.c_int32()
-            L.itg_dmrg_nbonds(out, C.byref(nb))
-            n = nb.value
-            sw_, ha, bb, te, dm = (np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32),
-                                   np.zeros(n), np.zeros(n, np.int32))
-            en = np.zeros(n)
-            L.itg_dmrg_bonds(out, _p(sw_, C.c_int32), _p(ha, C.c_int32), _p(bb, C.c_int32), _p(en, C.c_double),
-                             _p(te, C.c_double), _p(dm, C.c_int32))
-            bonds = [(int(sw_[i]), int(ha[i]), int(bb[i]), float(en[i]), float(te[i]), int(dm[i])) for i in range(n)]
-            N = max(b[2] for b in bonds) + 1 if bonds else 0
-            links = []
-            for b in range(1, N):
-                d, ns = C.c_int32(), C.c_int32()
-                L.itg_dmrg_link(out, b, C.byref(d), C.byref(ns), None, None)
-                qn = np.zeros(ns.value * 4, np.int32)
-                dims = np.zeros(ns.value, np.int32)
-                L.itg_dmrg_link(out, b, None, None, _p(qn, C.c_int32), _p(dims, C.c_int32))
-                links.append((d.value, qn.reshape(-1, 4), dims))
-            nsw = C.c_int32()
-            L.itg_dmrg_timing(out, C.byref(nsw), None, None)
-            secs = np.zeros(max(1, nsw.value))
-            ap = C.c_int32()
-            L.itg_dmrg_timing(out, None, _p(secs, C.c_double), C.byref(ap))
-            return DmrgResult(e.value, bonds, links, secs[:nsw.value].tolist(), ap.value)
-        finally:
-            lib().itg_dmrg_free(out)
+            self.close()
+        except Exception:
+            pass
+
+
+def pool_estimate(model, sweeps, precision=0):
+    """Device-memory estimate (bytes) the pool admits a request by."""
+    b = C.c_double()
+    md = _model_desc(model)
+    sw = _sweep_descs(sweeps)
+    _check(lib().itg_pool_estimate(C.byref(md), sw, len(sweeps), precision, C.byref(b)))
+    return b.value
+
+
+def _check(rc):
+    if rc != 0:
+        raise ITGError(rc, lib().itg_last_error(None).decode())
 
 
 def truncate(P, maxdim, mindim, cutoff, absolute_cutoff=False, rel_cutoff=True, respect_degenerate=False):

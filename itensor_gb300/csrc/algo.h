@@ -141,6 +141,9 @@ struct ModelSpec {
     int yperiodic = 0;
 };
 Hamiltonian make_hamiltonian(ModelSpec const& m);
+// Bond dimension of the MPO build_mpo makes: done, start, and one channel per
+// (left operator, distance still to go).
+int mpo_bond_dim(Hamiltonian const& H);
 
 struct MPO {
     std::vector<Index> sites;
@@ -167,6 +170,8 @@ struct DmrgResult {
     std::vector<Index> links;
     std::vector<double> sweep_seconds;
     int heff_applies = 0;
+    // wall seconds in: environments + two-site tensor, Davidson, bond split
+    double phase_seconds[3] = {0, 0, 0};
 };
 // DMRGWorker (itensor/mps/dmrg.h:336-467) with LocalMPO environments
 // (itensor/mps/localmpo.h:443-618).

@@ -28,8 +28,7 @@ Tensor upload_tensor(Ctx& ctx, std::shared_ptr<Layout> lay, double const* host) 
 std::vector<double> download(Ctx& ctx, Tensor const& t) {
     std::vector<double> h(std::max<int64_t>(t.lay->size, 0));
     if (!h.empty()) {
-        ITG_CHECK_CUDA(cudaMemcpyAsync(h.data(), t.data(), sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx.stream));
-        ctx.sync();
+        ctx.d2h(h.data(), t.data(), sizeof(double) * h.size());
     }
     return h;
 }
@@ -537,8 +536,7 @@ SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor co
     if (bad) throw Error(ERR_NOCONV, "denmat_decomp: eigensolver hit its sweep cap");
     std::vector<double> w(std::max<int64_t>(wtot, 1));
     if (wtot) {
-        ITG_CHECK_CUDA(cudaMemcpyAsync(w.data(), wbuf.as<double>(), sizeof(double) * wtot, cudaMemcpyDeviceToHost, ctx.stream));
-        ctx.sync();
+        ctx.d2h(w.data(), wbuf.as<double>(), sizeof(double) * wtot);
     }
     std::vector<double> alleig(w.begin(), w.begin() + wtot);
     std::sort(alleig.begin(), alleig.end(), std::greater<double>());

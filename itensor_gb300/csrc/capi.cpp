@@ -1,7 +1,7 @@
 // extern "C" boundary (include/itg.h): converts between the flat C
 // descriptions and the host data model, and turns exceptions into status codes.
 #include "../../include/itg.h"
-#include "algo.h"
+#include "pool.h"
 #include <cstring>
 
 using namespace itg;
@@ -58,7 +58,35 @@ Index index_from(itg_index_desc const& d) {
 }
 
 Tensor const* opt(itg_tensor const* t) { return t ? &t->t : nullptr; }
+
+ModelSpec model_from(itg_model_desc const& d) {
+    ModelSpec m;
+    m.type = d.type; m.N = d.N;
+    m.J = d.J; m.Jz = d.Jz; m.J2 = d.J2; m.h = d.h; m.t = d.t; m.U = d.U;
+    m.Lx = d.Lx; m.Ly = d.Ly; m.yperiodic = d.yperiodic;
+    return m;
+}
+
+std::vector<SweepSpec> sweeps_from(itg_sweep_desc const* sweeps, int n) {
+    ITG_REQUIRE(sweeps && n > 0, "dmrg: empty sweep schedule");
+    std::vector<SweepSpec> sw(n);
+    for (int s = 0; s < n; ++s) {
+        ITG_REQUIRE(sweeps[s].noise == 0.0, "dmrg: the noise term is not supported");
+        ITG_REQUIRE(sweeps[s].maxdim >= 1 && sweeps[s].niter >= 1, "dmrg: maxdim and niter must be positive");
+        sw[s].maxdim = sweeps[s].maxdim;
+        sw[s].mindim = sweeps[s].mindim;
+        sw[s].cutoff = sweeps[s].cutoff;
+        sw[s].niter = sweeps[s].niter;
+        sw[s].use_svd = sweeps[s].use_svd != 0;
+    }
+    return sw;
+}
 }  // namespace
+
+struct itg_pool {
+    SolverPool pool;
+    itg_pool(int dev, int w, int s, int64_t budget) : pool(dev, w, s, budget) {}
+};
 
 extern "C" {
 
@@ -441,23 +469,12 @@ int itg_dmrg_run(itg_ctx* c, const itg_model_desc* model, const itg_sweep_desc* 
                  int precision, itg_dmrg_result** out) {
     return guard(c, [&] {
         ITG_REQUIRE(model && sweeps && nsweeps > 0 && out, "dmrg_run: bad arguments");
-        ModelSpec m;
-        m.type = model->type; m.N = model->N;
-        m.J = model->J; m.Jz = model->Jz; m.J2 = model->J2; m.h = model->h; m.t = model->t; m.U = model->U;
-        m.Lx = model->Lx; m.Ly = model->Ly; m.yperiodic = model->yperiodic;
+        ModelSpec m = model_from(*model);
         Hamiltonian H = make_hamiltonian(m);
         ITG_REQUIRE(H.N >= 2, "dmrg_run: need at least two sites");
         MPO mpo = build_mpo(c->ctx, H);
         auto psi = product_mps(c->ctx, mpo, H.st, default_state(m));
-        std::vector<SweepSpec> sw(nsweeps);
-        for (int s = 0; s < nsweeps; ++s) {
-            ITG_REQUIRE(sweeps[s].noise == 0.0, "dmrg_run: the noise term is not supported");
-            sw[s].maxdim = sweeps[s].maxdim;
-            sw[s].mindim = sweeps[s].mindim;
-            sw[s].cutoff = sweeps[s].cutoff;
-            sw[s].niter = sweeps[s].niter;
-            sw[s].use_svd = sweeps[s].use_svd != 0;
-        }
+        std::vector<SweepSpec> sw = sweeps_from(sweeps, nsweeps);
         auto* res = new itg_dmrg_result;
         try {
             res->r = dmrg(c->ctx, mpo, psi, sw, precision);
@@ -510,6 +527,103 @@ int itg_dmrg_timing(const itg_dmrg_result* r, int32_t* nsweeps, double* secs, in
         if (applies) *applies = r->r.heff_applies;
     });
 }
+int itg_dmrg_phases(const itg_dmrg_result* r, double* s) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(r && s, "null");
+        for (int k = 0; k < 3; ++k) s[k] = r->r.phase_seconds[k];
+    });
+}
 void itg_dmrg_free(itg_dmrg_result* r) { delete r; }
+
+int itg_pool_create(int device, int32_t workers, int32_t slots_per_worker, double budget_bytes, itg_pool** out) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(out, "pool_create: null out");
+        int n = 0;
+        ITG_CHECK_CUDA(cudaGetDeviceCount(&n));
+        ITG_REQUIRE(device >= 0 && device < n, "pool_create: no such device");
+        *out = new itg_pool(device, workers, slots_per_worker, (int64_t)budget_bytes);
+    });
+}
+
+int itg_pool_submit(itg_pool* p, const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps,
+                    int precision, double arrival_s, int64_t* id) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p && model && id, "pool_submit: bad arguments");
+        ITG_REQUIRE(precision == PREC_F64 || precision == PREC_OZAKI_BF16, "pool_submit: unsupported precision");
+        SolveRequest r;
+        r.model = model_from(*model);
+        r.sweeps = sweeps_from(sweeps, nsweeps);
+        r.prec = precision;
+        r.arrival = arrival_s;
+        *id = p->pool.submit(std::move(r));
+    });
+}
+
+int itg_pool_start(itg_pool* p) {
+    return guard(nullptr, [&] { ITG_REQUIRE(p, "null pool"); p->pool.start(); });
+}
+
+int itg_pool_drain(itg_pool* p) {
+    return guard(nullptr, [&] { ITG_REQUIRE(p, "null pool"); p->pool.drain(); });
+}
+
+int itg_pool_record(itg_pool* p, int64_t id, int32_t* status, double* energy, double* t_arrive, double* t_admit,
+                    double* t_done, double* est_bytes, double* peak_bytes, int32_t* worker) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p, "null pool");
+        SolveRecord r = p->pool.record(id);
+        if (status) *status = r.status;
+        if (energy) *energy = r.result.energy;
+        if (t_arrive) *t_arrive = r.t_arrive;
+        if (t_admit) *t_admit = r.t_admit;
+        if (t_done) *t_done = r.t_done;
+        if (est_bytes) *est_bytes = (double)r.est_bytes;
+        if (peak_bytes) *peak_bytes = (double)r.peak_bytes;
+        if (worker) *worker = r.worker;
+    });
+}
+
+int itg_pool_error(itg_pool* p, int64_t id, char* buf, int32_t buflen) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p && buf && buflen > 0, "pool_error: bad arguments");
+        SolveRecord r = p->pool.record(id);
+        std::snprintf(buf, (size_t)buflen, "%s", r.error.c_str());
+    });
+}
+
+int itg_pool_result(itg_pool* p, int64_t id, itg_dmrg_result** out) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p && out, "pool_result: bad arguments");
+        SolveRecord r = p->pool.record(id);
+        ITG_REQUIRE(r.status == 0, "pool_result: request " + std::to_string(id) + " has not finished successfully");
+        auto* res = new itg_dmrg_result;
+        res->r = std::move(r.result);
+        *out = res;
+    });
+}
+
+int itg_pool_stats(itg_pool* p, int64_t* submitted, int64_t* done, int64_t* failed, double* peak_reserved_bytes,
+                   int32_t* peak_running, double* elapsed_s) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p, "null pool");
+        PoolStats s = p->pool.stats();
+        if (submitted) *submitted = s.submitted;
+        if (done) *done = s.done;
+        if (failed) *failed = s.failed;
+        if (peak_reserved_bytes) *peak_reserved_bytes = (double)s.peak_reserved_bytes;
+        if (peak_running) *peak_running = s.peak_running;
+        if (elapsed_s) *elapsed_s = s.elapsed;
+    });
+}
+
+int itg_pool_estimate(const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps, int precision,
+                      double* bytes) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(model && bytes, "pool_estimate: bad arguments");
+        *bytes = (double)solve_footprint_estimate(model_from(*model), sweeps_from(sweeps, nsweeps), precision);
+    });
+}
+
+void itg_pool_destroy(itg_pool* p) { delete p; }
 
 }  // extern "C"

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <memory>
@@ -51,18 +52,45 @@ void stream_register(cudaStream_t s);
 void stream_unregister(cudaStream_t s);
 bool stream_alive(cudaStream_t s);
 
+// Cooperative solve multiplexing (fiber.cpp). A solver-pool worker thread runs
+// several solves as fibers; a fiber that must wait for its stream yields to
+// the others instead of blocking the thread.
+bool fiber_active();                    // the calling code runs inside a pool fiber
+void fiber_wait_event(cudaEvent_t ev);  // yield until ev has completed (errors throw)
+
+// Device bytes held by one solve: the solver pool charges every buffer that a
+// solve allocates to its account and reports the peak beside the admission
+// estimate.
+struct MemAccount {
+    std::atomic<int64_t> cur{0}, peak{0};
+    void add(int64_t n) {
+        const int64_t c = cur.fetch_add(n) + n;
+        int64_t p = peak.load();
+        while (c > p && !peak.compare_exchange_weak(p, c)) {}
+    }
+    void sub(int64_t n) { cur.fetch_sub(n); }
+};
+// Account charged by the calling thread's allocations (empty: none).
+std::shared_ptr<MemAccount>& current_account();
+
 // Device buffer from the stream-ordered pool (cudaMallocAsync). Freed on the
 // stream it was allocated on, so reuse is ordered after every prior use.
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
     cudaStream_t stream = nullptr;
+    std::shared_ptr<MemAccount> acct;
     DevBuf() = default;
     DevBuf(size_t n, cudaStream_t s) : bytes(n), stream(s) {
-        if (n) ITG_CHECK_CUDA(cudaMallocAsync(&p, n, s));
+        if (n) {
+            ITG_CHECK_CUDA(cudaMallocAsync(&p, n, s));
+            acct = current_account();
+            if (acct) acct->add((int64_t)n);
+        }
     }
     ~DevBuf() {
         if (!p) return;
+        if (acct) acct->sub((int64_t)bytes);
         if (stream_alive(stream)) cudaFreeAsync(p, stream);
         else cudaFree(p);
     }

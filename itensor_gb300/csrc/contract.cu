@@ -429,12 +429,15 @@ Ctx::Ctx(int dev) : device(dev) {
     ITG_CHECK_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
     uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
     ITG_CHECK_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    ITG_CHECK_CUDA(cudaEventCreateWithFlags(&sync_event, cudaEventDisableTiming));
 }
 
 Ctx::~Ctx() {
     if (stream) cudaStreamSynchronize(stream);
     for (auto& r : prof) { cudaEventDestroy(r.start); cudaEventDestroy(r.stop); }
-    plans.clear();
+    plans.reset();
+    split_scratch.reset();
+    if (sync_event) cudaEventDestroy(sync_event);
     if (pin) cudaFreeHost(pin);
     if (stage) cudaFreeHost(stage);
     if (stream) {
@@ -452,6 +455,34 @@ void Ctx::ensure_pin(size_t bytes) {
     ITG_CHECK_CUDA(cudaHostAlloc(&pin, nb, cudaHostAllocMapped));
     ITG_CHECK_CUDA(cudaHostGetDevicePointer(&pin_dev, pin, 0));
     pin_bytes = nb;
+}
+
+void Ctx::sync() {
+    if (fiber_active()) {
+        ITG_CHECK_CUDA(cudaEventRecord(sync_event, stream));
+        fiber_wait_event(sync_event);
+    } else {
+        ITG_CHECK_CUDA(cudaStreamSynchronize(stream));
+    }
+}
+
+void Ctx::d2h(void* dst, void const* src, size_t bytes) {
+    if (!bytes) return;
+    ensure_pin(bytes);
+    ITG_CHECK_CUDA(cudaMemcpyAsync(pin, src, bytes, cudaMemcpyDeviceToHost, stream));
+    sync();
+    std::memcpy(dst, pin, bytes);
+}
+
+void* Ctx::split_buffer(size_t bytes) {
+    if (!split_scratch || split_scratch->bytes < bytes)
+        split_scratch = dev_alloc(std::max<size_t>(bytes, split_scratch ? split_scratch->bytes * 3 / 2 : 0), stream);
+    return split_scratch->p;
+}
+
+std::shared_ptr<MemAccount>& current_account() {
+    thread_local std::shared_ptr<MemAccount> acct;
+    return acct;
 }
 
 void Ctx::ensure_stage(size_t bytes) {
@@ -555,8 +586,14 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
     putv(key, mt.a_con); putv(key, mt.b_con); putv(key, mt.a_unc); putv(key, mt.b_unc);
     put(key, (int32_t)(target ? 1 : 0));
     if (target) { put_layout_structure(key, *target); putv(key, perm); }
-    auto hit = ctx.plans.find(key);
-    if (hit != ctx.plans.end()) { ctx.plan_hits++; return hit->second; }
+    if (auto hit = ctx.plans->find(key)) { ctx.plan_hits++; return hit; }
+    // plan tables outlive the solve that builds them (the cache is shared):
+    // they are not charged to its memory account
+    struct Uncharged {
+        std::shared_ptr<MemAccount> saved;
+        Uncharged() : saved(std::move(current_account())) { current_account().reset(); }
+        ~Uncharged() { current_account() = std::move(saved); }
+    } uncharged;
 
     const int nA = A.nblocks(), nB = B.nblocks(), rA = A.rank(), rB = B.rank();
     // ---- device planner inputs
@@ -711,6 +748,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
                 int K = 1;
                 for (int i : mt.a_con) K *= A.inds[i].bdim(A.block(pa[p])[i]);
                 r.K = K; r.pad = 0;
+                plan->max_pair_K = std::max(plan->max_pair_K, K);
                 pairs.push_back(r);
                 ksum += K;
                 flops += 2.0 * cblk[c].M * (double)cblk[c].N * K;
@@ -861,9 +899,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
     }
     plan->scalar = (rC == 0);
     ctx.plans_built++;
-    if (ctx.plans.size() >= ctx.plan_cache_limit) ctx.plans.clear();
-    ctx.plans.emplace(std::move(key), plan);
-    return plan;
+    return ctx.plans->insert(std::move(key), plan);
 }
 
 void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int prec) {
@@ -876,19 +912,15 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
         ITG_CHECK_CUDA(cudaEventRecord(pr.start, ctx.stream));
         pr.flops = p.flops;
         pr.nitems = p.nitems;
-        pr.kind = p.skinny ? 2 : (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) ? 1 : 0;
+        pr.kind = p.skinny ? 2 : plan_uses_split(p, prec) ? 1 : 0;
     }
     // narrow, small-K contractions (the MPO-tensor steps) are bandwidth-shaped: FP64 is exact there
     if (p.skinny && (prec == PREC_F64 || prec == PREC_OZAKI_BF16)) {
         gemm_f64_skinny_kernel<<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
-    } else if (prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0) {
+    } else if (plan_uses_split(p, prec)) {
         const int S = ctx.ozaki_slices;
         const int64_t plane = (p.panel_elems + 15) / 16 * 16;
-        if (!p.scratch || p.scratch_slices != S) {
-            p.scratch = dev_alloc(sizeof(__nv_bfloat16) * plane * S + sizeof(int32_t) * (p.exp_elems + 4), ctx.stream);
-            p.scratch_slices = S;
-        }
-        __nv_bfloat16* panels = p.scratch->as<__nv_bfloat16>();
+        __nv_bfloat16* panels = static_cast<__nv_bfloat16*>(ctx.split_buffer(split_scratch_bytes(p, S)));
         int32_t* exps = reinterpret_cast<int32_t*>(panels + plane * S);
         launch_ozaki(ctx, p, A, B, C, S, panels, exps);
         ctx.kernel_launches += 1;
@@ -934,8 +966,7 @@ Tensor contract(Ctx& ctx, Tensor const& A, Tensor const& B, int prec, std::share
     exec_plan(ctx, *plan, A.data(), B.data(), C.data(), prec);
     if (plan->scalar) {
         double v = 0;
-        ITG_CHECK_CUDA(cudaMemcpyAsync(&v, C.data(), sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
-        ctx.sync();
+        ctx.d2h(&v, C.data(), sizeof(double));
         C.scalar = v;
     }
     return C;

@@ -59,6 +59,8 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
         SweepSpec const& s = sweeps[sw];
         for (int b = 1, ha = 1; ha <= 2;) {
           try {
+            using clk = std::chrono::steady_clock;
+            auto tp0 = clk::now();
             LocalOp op = env.position(ctx, b, psi, prec);
             // phi on every block of its divergence, so H_eff and Davidson work on flat vectors
             Tensor const& A = psi[b - 1];
@@ -69,7 +71,9 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
             for (int j : mt.b_unc) pinds.push_back(B.inds()[j]);
             auto full = std::make_shared<Layout>(allowed_layout(pinds, tensor_div(A) + tensor_div(B)));
             Tensor phi = contract(ctx, A, B, prec, full);
+            auto tp1 = clk::now();
             energy = davidson(ctx, op, phi, s.niter, 1e-14, 1, prec, &res.heff_applies);
+            auto tp2 = clk::now();
             SplitArgs sa;
             sa.cutoff = s.cutoff;
             sa.maxdim = s.maxdim;
@@ -82,6 +86,10 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
                                        : denmat_decomp(ctx, phi, A, B, ha == 1, sa, prec);
             psi[b - 1] = sr.A;
             psi[b] = sr.B;
+            auto tp3 = clk::now();
+            res.phase_seconds[0] += std::chrono::duration<double>(tp1 - tp0).count();
+            res.phase_seconds[1] += std::chrono::duration<double>(tp2 - tp1).count();
+            res.phase_seconds[2] += std::chrono::duration<double>(tp3 - tp2).count();
             res.bonds.push_back(BondRecord{(int)sw + 1, ha, b, energy, sr.truncerr, (long)sr.link.dim()});
           } catch (Error const& e) {
             throw Error(e.code, std::string(e.what()) + " [sweep " + std::to_string(sw + 1) + ", half-sweep " +

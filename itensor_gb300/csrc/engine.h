@@ -61,6 +61,7 @@ struct Plan {
     double flops = 0;                // sum over block pairs of 2*M*N*K
     int64_t bytes_ab = 0;            // elements of A and B blocks touched
     int maxK = 0;                    // largest summed K of one output block
+    int max_pair_K = 0;              // largest K of one block pair
     double avgK = 0;
     bool scalar = false;             // rank-0 result
     bool skinny = false;             // every output block is <= 8 columns wide (row tiles)
@@ -72,8 +73,34 @@ struct Plan {
     int64_t panel_elems = 0;         // bf16 elements per digit plane set (all blocks)
     int64_t exp_elems = 0;
     int max_rows = 0;
-    mutable DevBufPtr scratch;       // panels + exponents, allocated on first use
-    mutable int scratch_slices = 0;
+};
+
+// Plans keyed by block structure. One cache may serve several contexts (the
+// solver pool shares one across its slots): lookups and inserts are locked,
+// builds are not (two contexts may build the same plan; the second insert is
+// dropped). A plan's tables are immutable once inserted.
+struct PlanCache {
+    std::mutex mu;
+    std::unordered_map<std::string, std::shared_ptr<Plan>> map;
+    size_t limit = 4096;
+    std::shared_ptr<Plan> find(std::string const& key) {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = map.find(key);
+        return it == map.end() ? nullptr : it->second;
+    }
+    std::shared_ptr<Plan> insert(std::string key, std::shared_ptr<Plan> p) {
+        std::lock_guard<std::mutex> g(mu);
+        if (map.size() >= limit) map.clear();
+        return map.emplace(std::move(key), std::move(p)).first->second;
+    }
+    size_t size() {
+        std::lock_guard<std::mutex> g(mu);
+        return map.size();
+    }
+    void clear() {
+        std::lock_guard<std::mutex> g(mu);
+        map.clear();
+    }
 };
 
 struct ProfRec {          // one timed GEMM launch (profiling mode)
@@ -96,8 +123,12 @@ struct Ctx {
     // pinned staging buffer for host->device table uploads
     void* stage = nullptr;
     size_t stage_bytes = 0;
-    std::unordered_map<std::string, std::shared_ptr<Plan>> plans;
-    size_t plan_cache_limit = 4096;
+    std::shared_ptr<PlanCache> plans = std::make_shared<PlanCache>();
+    // split-precision digit panels of exec_plan: one growing buffer per context
+    // (launches on this stream are ordered, so every exec reuses it)
+    DevBufPtr split_scratch;
+    // event used by sync() when the calling thread multiplexes solves
+    cudaEvent_t sync_event = nullptr;
     // counters
     uint64_t kernel_launches = 0;
     uint64_t plans_built = 0, plan_hits = 0;
@@ -110,7 +141,13 @@ struct Ctx {
     ~Ctx();
     void ensure_pin(size_t bytes);
     void ensure_stage(size_t bytes);
-    void sync() { ITG_CHECK_CUDA(cudaStreamSynchronize(stream)); }
+    // Waits for the stream. Inside a solver-pool fiber the wait yields to the
+    // thread's other solves until the stream's work is done.
+    void sync();
+    // Device -> host copy through the pinned buffer, waiting as sync() does.
+    void d2h(void* dst, void const* src, size_t bytes);
+    // Split-precision scratch of at least `bytes` (grown on this stream).
+    void* split_buffer(size_t bytes);
 };
 
 // Labels: which A index matches which B index (ITensor computeLabels semantics).
@@ -143,8 +180,10 @@ void exec_plan_noalloc(Ctx& ctx, Plan const& p, double const* A, double const* B
 void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S, __nv_bfloat16* panels,
                   int32_t* exps, bool prep_b = true);
 // Whether exec_plan runs this plan with the split-precision kernels.
+// (The int64 digit sums of one block pair are exact up to K = 8192.)
+constexpr int SPLIT_MAX_PAIR_K = 8192;
 inline bool plan_uses_split(Plan const& p, int prec) {
-    return !p.skinny && prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0;
+    return !p.skinny && prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0 && p.max_pair_K <= SPLIT_MAX_PAIR_K;
 }
 // Bytes of split-precision scratch (digit planes + row exponents) a plan needs.
 inline size_t split_scratch_bytes(Plan const& p, int S) {

@@ -157,6 +157,16 @@ static QN op_flux(SiteType const& st, std::vector<double> const& O) {
     return QN();
 }
 
+int mpo_bond_dim(Hamiltonian const& H) {
+    std::vector<std::string> lefts;
+    int rng = 1;
+    for (auto const& t : H.two) {
+        if (std::find(lefts.begin(), lefts.end(), t.a) == lefts.end()) lefts.push_back(t.a);
+        rng = std::max(rng, t.j - t.i);
+    }
+    return 2 + (int)lefts.size() * rng;
+}
+
 MPO build_mpo(Ctx& ctx, Hamiltonian const& H) {
     SiteType const& st = H.st;
     const int N = H.N, d = st.d();

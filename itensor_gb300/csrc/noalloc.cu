@@ -51,7 +51,7 @@ void exec_plan_noalloc(Ctx& ctx, Plan const& p, double const* A, double const* B
     ITG_REQUIRE(S >= 3 && S <= 6, "contract_exec_noalloc: slices must be 3..6");
     if (p.nitems == 0) return;
     // narrow / small-K plans run the FP64 kernels, as itg_contract_exec does; they use no scratch
-    if (p.skinny || !(p.avgK >= 8.0 && p.npairs > 0)) {
+    if (!plan_uses_split(p, PREC_OZAKI_BF16)) {
         exec_plan_f64_only(ctx, p, A, B, C);
         return;
     }

@@ -21,7 +21,14 @@ __global__ void fill_kernel(double* x, int64_t n, double v) {
 __global__ void scale_kernel(double* x, int64_t n, double a) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] *= a;
 }
+// y = a x + b y. With b == 0, y is not read: it may be fresh pool memory whose
+// bits (old digit panels, integers) need not be finite doubles, and 0 * NaN = NaN.
 __global__ void axpby_kernel(double* y, double const* x, int64_t n, double a, double b) {
+    if (b == 0.0) {
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+            y[i] = a * x[i];
+        return;
+    }
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         y[i] = fma(a, x[i], b * y[i]);
 }
@@ -335,8 +342,7 @@ int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src,
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
     std::vector<int> st(items.size());
-    ITG_CHECK_CUDA(cudaMemcpyAsync(st.data(), d_stat, sizeof(int) * items.size(), cudaMemcpyDeviceToHost, ctx.stream));
-    ctx.sync();
+    ctx.d2h(st.data(), d_stat, sizeof(int) * items.size());
     int bad = 0;
     for (int s : st) bad += s;
     return bad;

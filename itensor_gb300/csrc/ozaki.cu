@@ -8,8 +8,13 @@
 // are exact in FP32 and so are their sums while |sum| < 2^24. Digit pairs
 // (s,t) with s+t < S are accumulated per diagonal D = s+t with mma.sync
 // m16n8k16 (FP32 accumulate), folded exactly into one int64 per output
-// (sum_D acc_D 2^(7(S-1-D))) every 256 k, and scaled into the FP64 output once
-// per block pair. Accuracy ~2^(-7S) of the row/column maxima. Slicing and
+// (sum_D acc_D 2^(7(S-1-D))) every KCHUNK k (a diagonal holds at most S
+// digit products of |d| <= 127 per k, so KCHUNK * S * 127^2 <= 2^24 keeps every
+// partial sum an exact FP32 integer: 128 k for S = 5, 6; 256 for S <= 4), and scaled into the FP64 output once
+// per block pair (one fold is below 2^57 in magnitude, so the int64 sum of a
+// pair cannot overflow while the pair's K <= 64 * KCHUNK; plans with a longer
+// pair run the FP64 kernel, see plan_uses_split). Accuracy ~2^(-7S)
+// of the row/column maxima. Slicing and
 // folding are integer work: FP64 issue slots on this part are ~1/60 of FP32.
 //
 // prep: one CTA per item of whole rows (~2048 elements) writes the row
@@ -119,7 +124,9 @@ __global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __res
                                                          const int32_t* __restrict__ tab,
                                                          const __nv_bfloat16* __restrict__ panels, int64_t plane,
                                                          const int32_t* __restrict__ exps, double* __restrict__ C) {
-    constexpr int T = GEMM_TILE, TK = 16, KCHUNK = 256, LD = TK + 8;  // row stride 48 B: 16-B aligned, no ldmatrix conflicts
+    constexpr int T = GEMM_TILE, TK = 16, LD = TK + 8;  // row stride 48 B: 16-B aligned, no ldmatrix conflicts
+    constexpr int KCHUNK = (S <= 4) ? 256 : 128;
+    static_assert((long long)KCHUNK * S * 127 * 127 <= (1LL << 24), "digit sums must stay exact in FP32");
     __shared__ __align__(16) __nv_bfloat16 As[2][S][T][LD];
     __shared__ __align__(16) __nv_bfloat16 Bs[2][S][T][LD];
     __shared__ int ea[T], eb[T];

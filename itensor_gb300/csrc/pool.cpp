@@ -1,0 +1,257 @@
+// Solver pool (see pool.h).
+#include "pool.h"
+#include <algorithm>
+#include <cmath>
+
+namespace itg {
+
+int64_t solve_footprint_estimate(ModelSpec const& m, std::vector<SweepSpec> const& sweeps, int prec) {
+    Hamiltonian H = make_hamiltonian(m);
+    const int N = H.N, d = H.st.d(), D = mpo_bond_dim(H);
+    long maxdim = 1;
+    int niter = 2;
+    for (auto const& s : sweeps) {
+        maxdim = std::max(maxdim, s.maxdim);
+        niter = std::max(niter, s.niter);
+    }
+    // m_b: largest dimension of link b allowed by the schedule and by the half-chains' Hilbert spaces
+    std::vector<double> mb(N + 1, 1.0);
+    for (int b = 1; b < N; ++b) {
+        const double left = std::pow((double)d, std::min(b, 60)), right = std::pow((double)d, std::min(N - b, 60));
+        mb[b] = std::min<double>((double)maxdim, std::min(left, right));
+    }
+    double mps = 0, env = 0, work = 0;
+    for (int n = 1; n <= N; ++n) mps += mb[n - 1] * d * mb[n];
+    for (int b = 1; b < N; ++b) env += mb[b] * D * mb[b];
+    const int S = 6;  // digit planes of the split form
+    for (int b = 1; b < N; ++b) {
+        const double ml = mb[b - 1], mr = mb[b + 1 <= N ? b + 1 : N];
+        const double phi = ml * d * d * mr;
+        const double fused = std::max(ml, mr) * d;
+        // Davidson: V and H V for every iteration; H_eff intermediates (two of D x phi);
+        // bond split: combined copy, density matrix and eigenvectors (or U, V)
+        double w = phi * (2.0 * (niter + 2) + 2.0 * D + 3.0) + 3.0 * fused * fused;
+        if (prec == PREC_OZAKI_BF16) w += (2.0 * S / 8.0) * (2.0 * phi + 2.0 * ml * D * ml + 2.0 * mr * D * mr);
+        work = std::max(work, w);
+    }
+    return (int64_t)(8.0 * (mps + env + work)) + (4 << 20);
+}
+
+SolverPool::SolverPool(int device, int workers, int slots_per_worker, int64_t budget_bytes)
+    : device_(device), workers_(workers), slots_(slots_per_worker), budget_(budget_bytes) {
+    ITG_REQUIRE(workers >= 1 && slots_per_worker >= 1, "pool: need at least one worker and one slot");
+    ITG_REQUIRE(budget_bytes > 0, "pool: memory budget must be positive");
+}
+
+SolverPool::~SolverPool() {
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        stop_ = true;
+    }
+    cv_work_.notify_all();
+    for (auto& t : threads_) t.join();
+}
+
+double SolverPool::now() const {
+    if (!started_) return 0.0;
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0_).count();
+}
+
+int64_t SolverPool::submit(SolveRequest req) {
+    auto rec = std::make_shared<SolveRecord>();
+    rec->est_bytes = solve_footprint_estimate(req.model, req.sweeps, req.prec);
+    ITG_REQUIRE(!req.sweeps.empty(), "pool: empty sweep schedule");
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        rec->id = (int64_t)records_.size();
+        rec->t_arrive = std::max(req.arrival, now());
+        rec->req = std::move(req);
+        records_.push_back(rec);
+        st_.submitted++;
+        if (rec->est_bytes > budget_) {
+            rec->status = ERR_RANGE;
+            rec->error = "pool: the request's memory estimate (" + std::to_string(rec->est_bytes) +
+                         " bytes) exceeds the pool budget";
+            st_.failed++;
+            cv_done_.notify_all();
+            return rec->id;
+        }
+        auto pos = std::upper_bound(queue_.begin(), queue_.end(), rec,
+                                    [](auto const& a, auto const& b) { return a->t_arrive < b->t_arrive; });
+        queue_.insert(pos, rec);
+    }
+    cv_work_.notify_all();
+    return rec->id;
+}
+
+void SolverPool::start() {
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        ITG_REQUIRE(!started_, "pool: already started");
+        t0_ = std::chrono::steady_clock::now();
+        started_ = true;
+        init_pending_ = workers_;
+    }
+    for (int w = 0; w < workers_; ++w) threads_.emplace_back(&SolverPool::worker_main, this, w);
+    std::unique_lock<std::mutex> lk(mu_);
+    cv_done_.wait(lk, [&] { return init_pending_ == 0; });
+    if (!init_error_.empty()) {
+        stop_ = true;
+        lk.unlock();
+        cv_work_.notify_all();
+        for (auto& t : threads_) t.join();
+        threads_.clear();
+        throw Error(ERR_CUDA, "pool: worker setup failed: " + init_error_);
+    }
+}
+
+void SolverPool::drain() {
+    std::unique_lock<std::mutex> lk(mu_);
+    ITG_REQUIRE(started_, "pool: drain before start");
+    cv_done_.wait(lk, [&] { return st_.done + st_.failed == st_.submitted; });
+}
+
+SolveRecord SolverPool::record(int64_t id) {
+    std::lock_guard<std::mutex> g(mu_);
+    ITG_REQUIRE(id >= 0 && id < (int64_t)records_.size(), "pool: unknown request id");
+    return *records_[id];
+}
+
+PoolStats SolverPool::stats() {
+    std::lock_guard<std::mutex> g(mu_);
+    PoolStats s = st_;
+    s.elapsed = now();
+    return s;
+}
+
+std::shared_ptr<SolveRecord> SolverPool::try_admit() {
+    std::lock_guard<std::mutex> g(mu_);
+    if (queue_.empty() || stop_) return nullptr;
+    auto rec = queue_.front();
+    const double t = now();
+    if (rec->t_arrive > t) return nullptr;
+    // first come, first served: the head waits until its memory estimate fits
+    if (st_.running > 0 && st_.reserved_bytes + rec->est_bytes > budget_) return nullptr;
+    queue_.pop_front();
+    rec->t_admit = t;
+    rec->status = -2;
+    st_.reserved_bytes += rec->est_bytes;
+    st_.peak_reserved_bytes = std::max(st_.peak_reserved_bytes, st_.reserved_bytes);
+    st_.running++;
+    st_.peak_running = std::max(st_.peak_running, st_.running);
+    return rec;
+}
+
+void SolverPool::finish(std::shared_ptr<SolveRecord> const& rec) {
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        st_.reserved_bytes -= rec->est_bytes;
+        st_.running--;
+        if (rec->status == 0) st_.done++;
+        else st_.failed++;
+    }
+    cv_done_.notify_all();
+    cv_work_.notify_all();
+}
+
+namespace {
+void run_solve(Ctx& ctx, SolveRecord& rec, SolverPool const& pool) {
+    try {
+        Hamiltonian H = make_hamiltonian(rec.req.model);
+        ITG_REQUIRE(H.N >= 2, "pool: need at least two sites");
+        MPO mpo = build_mpo(ctx, H);
+        auto psi = product_mps(ctx, mpo, H.st, default_state(rec.req.model));
+        rec.result = dmrg(ctx, mpo, std::move(psi), rec.req.sweeps, rec.req.prec);
+        rec.status = 0;
+    } catch (Error const& e) {
+        rec.status = e.code;
+        rec.error = e.what();
+    } catch (std::exception const& e) {
+        rec.status = ERR_INTERNAL;
+        rec.error = e.what();
+    }
+    ctx.split_scratch.reset();
+    try {
+        ctx.sync();
+    } catch (std::exception const& e) {
+        if (rec.status == 0) { rec.status = ERR_CUDA; rec.error = e.what(); }
+    }
+    rec.t_done = pool.now();
+}
+}  // namespace
+
+void SolverPool::worker_main(int w) {
+    std::vector<std::unique_ptr<Slot>> slots;
+    FiberScheduler sched;
+    try {
+        ITG_CHECK_CUDA(cudaSetDevice(device_));
+        for (int i = 0; i < slots_; ++i) {
+            auto s = std::make_unique<Slot>();
+            s->ctx = std::make_unique<Ctx>(device_);
+            s->ctx->plans = plans_;
+            s->ctx->ensure_pin(1 << 20);
+            s->ctx->ensure_stage(8 << 20);
+            slots.push_back(std::move(s));
+        }
+    } catch (std::exception const& e) {
+        std::lock_guard<std::mutex> g(mu_);
+        init_error_ = e.what();
+        slots.clear();
+    }
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        --init_pending_;
+    }
+    cv_done_.notify_all();
+    if (slots.empty()) return;
+    FiberScheduler::of_thread() = &sched;
+    int idle_spins = 0;
+    for (;;) {
+        bool progressed = false;
+        int busy = 0;
+        for (int i = 0; i < (int)slots.size(); ++i) {
+            Slot& s = *slots[i];
+            if (!s.rec) {
+                if (auto rec = try_admit()) {
+                    s.rec = rec;
+                    rec->worker = w;
+                    rec->slot = i;
+                    s.fiber.acct = std::make_shared<MemAccount>();
+                    Ctx* ctx = s.ctx.get();
+                    SolveRecord* r = rec.get();
+                    sched.start(s.fiber, [ctx, r, this] { run_solve(*ctx, *r, *this); });
+                    progressed = true;
+                }
+            } else if (sched.poll(s.fiber)) {
+                progressed = true;
+            }
+            if (s.rec && !s.fiber.running) {
+                s.rec->peak_bytes = s.fiber.acct->peak.load();
+                finish(s.rec);
+                s.rec.reset();
+                s.fiber.acct.reset();
+            }
+            busy += s.rec ? 1 : 0;
+        }
+        if (busy == 0) {
+            std::unique_lock<std::mutex> lk(mu_);
+            if (stop_) break;
+            // nothing running here: sleep until a request is submitted, memory is
+            // returned, or the next request arrives
+            double wait_s = 0.05;
+            if (!queue_.empty()) wait_s = std::clamp(queue_.front()->t_arrive - now(), 2e-4, 0.05);
+            cv_work_.wait_for(lk, std::chrono::duration<double>(wait_s));
+            continue;
+        }
+        if (progressed) {
+            idle_spins = 0;
+        } else if (++idle_spins > 64) {
+            std::this_thread::sleep_for(std::chrono::microseconds(5));
+        } else {
+            std::this_thread::yield();
+        }
+    }
+    FiberScheduler::of_thread() = nullptr;
+}
+
+}  // namespace itg

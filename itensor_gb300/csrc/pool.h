@@ -1,0 +1,92 @@
+// Solver pool: many independent ground-state solves on one GPU.
+//
+// Requests (model, sweep schedule, precision, arrival time) wait in an
+// arrival-ordered queue. A request is admitted when its arrival time has
+// passed, a solve slot is free, and its device-memory estimate fits in what
+// the budget has left; slots free up and memory returns as solves finish, so
+// requests that arrive while others run join them (continuous batching).
+// Each worker thread owns several slots; a slot is a context (its own stream)
+// and a fiber that runs the plain DMRG sweep loop (itensor/mps/dmrg.h:336-467).
+// While one solve waits for its stream the thread runs the others, so the
+// device sees the kernels of every admitted solve at once. All slots share
+// one plan cache: solves of the same model family reuse contraction plans.
+// A solve's result does not depend on what runs beside it: kernels are
+// deterministic and no state is shared between solves but read-only plans.
+#pragma once
+#include "algo.h"
+#include "fiber.h"
+#include <condition_variable>
+#include <deque>
+#include <thread>
+
+namespace itg {
+
+struct SolveRequest {
+    ModelSpec model;
+    std::vector<SweepSpec> sweeps;
+    int prec = PREC_F64;
+    double arrival = 0;          // seconds after the pool started (<= 0: at once)
+};
+
+struct SolveRecord {
+    int64_t id = 0;
+    SolveRequest req;
+    int status = -1;             // -1 queued, -2 running, 0 done, else an error code
+    std::string error;
+    DmrgResult result;
+    double t_arrive = 0, t_admit = 0, t_done = 0;   // seconds after the pool started
+    int64_t est_bytes = 0, peak_bytes = 0;
+    int worker = -1, slot = -1;
+};
+
+// Upper bound of the device memory of one solve: dense blocks at the bond
+// dimensions the sweep schedule allows (capped by the Hilbert space of each
+// half-chain), for the MPS, the environments and one bond step's workspace
+// (Davidson vectors, H_eff intermediates, density matrix, split-precision
+// digit panels).
+int64_t solve_footprint_estimate(ModelSpec const& m, std::vector<SweepSpec> const& sweeps, int prec);
+
+struct PoolStats {
+    int64_t submitted = 0, done = 0, failed = 0;
+    int64_t reserved_bytes = 0, peak_reserved_bytes = 0;
+    int running = 0, peak_running = 0;
+    double elapsed = 0;          // seconds since start
+};
+
+class SolverPool {
+public:
+    SolverPool(int device, int workers, int slots_per_worker, int64_t budget_bytes);
+    ~SolverPool();
+    int64_t submit(SolveRequest req);  // thread-safe, before or after start()
+    void start();
+    void drain();                      // blocks until every submitted request has finished
+    SolveRecord record(int64_t id);
+    PoolStats stats();
+    double now() const;
+
+private:
+    struct Slot {
+        std::unique_ptr<Ctx> ctx;
+        Fiber fiber;
+        std::shared_ptr<SolveRecord> rec;
+    };
+    void worker_main(int w);
+    std::shared_ptr<SolveRecord> try_admit();
+    void finish(std::shared_ptr<SolveRecord> const& rec);
+
+    int device_, workers_, slots_;
+    int64_t budget_;
+    std::shared_ptr<PlanCache> plans_ = std::make_shared<PlanCache>();
+    std::mutex mu_;
+    std::condition_variable cv_done_, cv_work_;
+    std::deque<std::shared_ptr<SolveRecord>> queue_;        // by arrival time
+    std::vector<std::shared_ptr<SolveRecord>> records_;     // by id
+    PoolStats st_;
+    bool started_ = false, stop_ = false;
+    std::chrono::steady_clock::time_point t0_;
+    std::vector<std::thread> threads_;
+    std::string init_error_;
+    int init_pending_ = 0;
+};
+
+}  // namespace itg

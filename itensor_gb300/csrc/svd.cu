@@ -160,8 +160,7 @@ int batched_svd(Ctx& ctx, std::vector<SvdItem> const& items, double const* src, 
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
     std::vector<int> st(items.size());
-    ITG_CHECK_CUDA(cudaMemcpyAsync(st.data(), d_stat, sizeof(int) * items.size(), cudaMemcpyDeviceToHost, ctx.stream));
-    ctx.sync();
+    ctx.d2h(st.data(), d_stat, sizeof(int) * items.size());
     int bad = 0;
     for (int s : st) bad += s;
     return bad;

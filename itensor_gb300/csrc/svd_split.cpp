@@ -53,8 +53,7 @@ SplitResult svd_split(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor const&
         throw Error(ERR_NOCONV, "svd_split: singular value decomposition hit its sweep cap");
     std::vector<double> s(std::max<int64_t>(so, 1));
     if (so) {
-        ITG_CHECK_CUDA(cudaMemcpyAsync(s.data(), sbuf.p, sizeof(double) * so, cudaMemcpyDeviceToHost, ctx.stream));
-        ctx.sync();
+        ctx.d2h(s.data(), sbuf.p, sizeof(double) * so);
     }
     std::vector<double> probs;
     for (int64_t i = 0; i < so; ++i) probs.push_back(s[i] * s[i]);
