@@ -243,6 +243,156 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+# ---------------------------------------------------------------- many independent solves
+BATCH_SEED, SERVE_SEED = 4242, 5151
+
+
+def ramp_sweeps(maxdim, n=5, cutoff=1e-10):
+    """The last n of the sweeps maxdim/8, maxdim/4, maxdim/2, maxdim, maxdim."""
+    full = [max(8, maxdim // 8), max(16, maxdim // 4), maxdim // 2, maxdim, maxdim]
+    return [dict(maxdim=int(m), mindim=1, cutoff=cutoff, niter=2) for m in full[5 - n:]]
+
+
+def j1j2_chains(n, seed=BATCH_SEED):
+    """Independent J1-J2 Heisenberg chains: J2 ~ U[0, 0.5], N ~ U{16..64},
+    maxdim ~ U{64..256}, Sz QN, Neel start, five sweeps ramping to maxdim."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        N = int(rng.integers(16, 65))
+        J2 = float(rng.uniform(0.0, 0.5))
+        md = int(rng.integers(64, 257))
+        out.append((dict(type=0, N=N, J=1.0, Jz=1.0, J2=J2), ramp_sweeps(md)))
+    return out
+
+
+def serving_requests(n, seed=SERVE_SEED):
+    """Ground-state requests: XXZ chains (Delta ~ U[0, 2], Sz QN) and
+    transverse-field Ising chains (h ~ U[0.5, 1.5], parity QN), N ~ U{16..128},
+    maxdim ~ U{32..512}, four sweeps ramping to maxdim."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        N = int(rng.integers(16, 129))
+        md = int(rng.integers(32, 513))
+        if rng.uniform() < 0.5:
+            m = dict(type=0, N=N, J=1.0, Jz=float(rng.uniform(0.0, 2.0)))
+        else:
+            m = dict(type=1, N=N, h=float(rng.uniform(0.5, 1.5)))
+        out.append((m, ramp_sweeps(md, 4)))
+    return out
+
+
+def pool_shape():
+    cores = os.cpu_count() or 1
+    return max(1, min(16, cores - 1)), 8
+
+
+def bench_batched(ctx, n_chains, n_seq, budget_bytes):
+    """Batched form: every chain submitted at once to the solver pool in the
+    split precision; beside it the plain FP64 path solving chains one after
+    the other on one context (a stride sample of the same chains)."""
+    import itensor_gb300 as itg
+    chains = j1j2_chains(n_chains)
+    stride = max(1, n_chains // n_seq)
+    sample = list(range(0, n_chains, stride))[:n_seq]
+    # plain FP64 path, sequential
+    ctx.dmrg(*chains[sample[0]], precision=itg.PREC_F64)  # warm plans and pool
+    t0 = time.perf_counter()
+    seq = {}
+    for i in sample:
+        seq[i] = ctx.dmrg(*chains[i], precision=itg.PREC_F64)
+    t_seq = time.perf_counter() - t0
+    seq_bonds = sum(len(r.bonds) for r in seq.values())
+    workers, slots = pool_shape()
+    pool = itg.Pool(0, workers=workers, slots_per_worker=slots, budget_bytes=budget_bytes)
+    try:
+        ids = [pool.submit(m, sw, itg.PREC_OZAKI_BF16) for m, sw in chains]
+        t0 = time.perf_counter()
+        pool.start()
+        pool.drain()
+        t_pool = time.perf_counter() - t0
+        st = pool.stats()
+        res = {i: pool.result(ids[i]) for i in range(n_chains) if pool.record(ids[i]).status == 0}
+    finally:
+        pool.close()
+    pool_bonds = sum(len(r.bonds) for r in res.values())
+    dE = [abs(res[i].energy - seq[i].energy) for i in sample if i in res]
+    seq_rate = len(sample) / t_seq
+    pool_rate = len(res) / t_pool
+    return {"workload": "%d independent J1-J2 chains (J2~U[0,0.5], N~U{16..64}, maxdim~U{64..256}, Sz QN, "
+                        "Neel start, 5 sweeps ramping to maxdim, cutoff 1e-10, niter 2; seed %d)" % (n_chains, BATCH_SEED),
+            "batched": {"precision": "split (6 BF16 slices, FP32-exact accumulation); FP64 Davidson, eigensolver, SVD",
+                        "seconds": t_pool, "solves_per_s": pool_rate, "sweeps_per_s": pool_rate * 5,
+                        "bond_steps_per_s": pool_bonds / t_pool, "failed": st["failed"],
+                        "workers": workers, "slots_per_worker": slots, "peak_running": st["peak_running"]},
+            "plain_f64_sequential": {"chains": len(sample), "seconds": t_seq, "solves_per_s": seq_rate,
+                                     "sweeps_per_s": seq_rate * 5, "bond_steps_per_s": seq_bonds / t_seq,
+                                     "sample": "every %dth chain of the same set, one context, one after the other"
+                                               % stride},
+            "speedup_solves_per_s": pool_rate / seq_rate,
+            "energy_vs_f64": {"max_abs_dE": max(dE) if dE else None,
+                              "within_1e-9": sum(1 for x in dE if x <= 1e-9), "compared": len(dE)}}
+
+
+def bench_serving(n_req, budget_bytes, load=0.8):
+    """Serving: requests arrive as a Poisson stream and are admitted by memory
+    while others run. First a saturation pass (every request at t = 0) gives
+    the throughput; then a fresh set arrives at rate lambda = load x that
+    throughput and the latency distribution is measured."""
+    import numpy as np
+    import itensor_gb300 as itg
+    workers, slots = pool_shape()
+
+    def run(reqs, arrivals):
+        pool = itg.Pool(0, workers=workers, slots_per_worker=slots, budget_bytes=budget_bytes)
+        try:
+            pool.start()
+            t0 = time.perf_counter()
+            ids = [pool.submit(m, sw, itg.PREC_OZAKI_BF16, arrival=a) for (m, sw), a in zip(reqs, arrivals)]
+            pool.drain()
+            el = time.perf_counter() - t0
+            recs = [pool.record(i) for i in ids]
+            st = pool.stats()
+        finally:
+            pool.close()
+        return el, recs, st
+
+    sat_reqs = serving_requests(n_req, SERVE_SEED)
+    el, recs, st = run(sat_reqs, [0.0] * n_req)
+    ok = [r for r in recs if r.status == 0]
+    mu = len(ok) / el
+    lam = load * mu
+    rng = np.random.default_rng(SERVE_SEED + 1)
+    arr = np.cumsum(rng.exponential(1.0 / lam, n_req))
+    reqs = serving_requests(n_req, SERVE_SEED + 2)
+    el2, recs2, st2 = run(reqs, arr.tolist())
+    ok2 = [r for r in recs2 if r.status == 0]
+    lat = np.array([r.latency for r in ok2])
+    wait = np.array([r.t_admit - r.t_arrive for r in ok2])
+    est = np.array([r.est_bytes for r in ok2])
+    peak = np.array([r.peak_bytes for r in ok2])
+    return {"workload": "%d requests per pass: XXZ (Delta~U[0,2], Sz QN) and transverse-field Ising (h~U[0.5,1.5], "
+                        "parity QN) chains, N~U{16..128}, maxdim~U{32..512}, 4 sweeps ramping to maxdim, cutoff "
+                        "1e-10, split precision" % n_req,
+            "saturation": {"seconds": el, "solves_per_s": mu, "failed": len(recs) - len(ok),
+                           "peak_running": st["peak_running"]},
+            "poisson": {"lambda_per_s": lam, "load": load, "seconds": el2, "solves_per_s": len(ok2) / el2,
+                        "failed": len(recs2) - len(ok2),
+                        "latency_s": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
+                                      "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+                        "queue_wait_s": {"p50": float(np.percentile(wait, 50)), "p99": float(np.percentile(wait, 99))},
+                        "peak_running": st2["peak_running"],
+                        "peak_reserved_gb": st2["peak_reserved_bytes"] / 1e9,
+                        "hbm_budget_gb": budget_bytes / 1e9,
+                        "reserved_occupancy_peak": st2["peak_reserved_bytes"] / budget_bytes,
+                        "measured_over_estimate": {"max": float((peak / est).max()),
+                                                   "mean": float((peak / est).mean())}},
+            "pool": {"workers": workers, "slots_per_worker": slots}}
+
+
 def run_profile(args):
     """Short run of the same workload for ncu: for the split form and plain
     FP64, N prepared applies each (kernels launched one by one)."""
@@ -273,6 +423,9 @@ def main():
     ap.add_argument("--slices", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-dmrg", action="store_true")
+    ap.add_argument("--chains", type=int, default=256, help="independent chains of the batched form (0: skip)")
+    ap.add_argument("--seq-chains", type=int, default=16, help="chains solved one by one by the plain FP64 path")
+    ap.add_argument("--requests", type=int, default=96, help="requests per serving pass (0: skip)")
     ap.add_argument("--profile", type=int, default=0,
                     help="profiling run for ncu: N prepared applies per arithmetic, no graph, no timing")
     args = ap.parse_args()
@@ -437,6 +590,15 @@ def main():
             dmrg[name] = {"seconds": el, "sweep_seconds": r.sweep_seconds, "energy": r.energy,
                           "dE": None if ref_e is None else r.energy - ref_e, "heff_applies": r.heff_applies}
 
+    # many independent solves: the batched form and the serving loop (rank 0; replicas elsewhere)
+    free_b, total_b = torch.cuda.mem_get_info()
+    budget = int(0.8 * total_b)
+    batched = serving = None
+    if args.chains > 0 and rank == 0:
+        batched = bench_batched(ctx, args.chains, args.seq_chains, budget)
+    if args.requests > 0 and rank == 0:
+        serving = bench_serving(args.requests, budget)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(flops_apply)
@@ -454,7 +616,7 @@ def main():
                              "dominant_kernel_tflops": d64_flops / (d64_ms / 1e3) / 1e12},
                 "speedup_split_over_f64": value / f64_value,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk, "dmrg_heis20": dmrg}
+                "clocks": clk, "dmrg_heis20": dmrg, "batched_chains": batched, "serving": serving}
         print(json.dumps(line))
     ctx.close()
     if dist:
