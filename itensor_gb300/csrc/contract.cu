@@ -312,31 +312,33 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
 // For contractions whose output blocks are at most SKINNY_N columns wide (the
 // MPO-tensor steps of the H_eff apply: N = (s', w') <= 3, K = (s, w) <= 3).
 // One thread per output row keeps all N sums in registers; the B block
-// (K x N) is staged in shared memory. Tiles are SKINNY_M rows of one block.
-constexpr int SKINNY_N = 8, SKINNY_THREADS = 256, SKINNY_R = 4, SKINNY_M = SKINNY_THREADS * SKINNY_R, SKINNY_K = 64;
+// (K x N) is staged in shared memory. Tiles are 256 * R rows of one block.
+constexpr int SKINNY_N = 8, SKINNY_THREADS = 256, SKINNY_K = 64;
 
 // NN = exact output width of the block (1..SKINNY_N). Rows m0 + t + j*256,
-// j < SKINNY_R, per thread. Zero entries of the staged B block are skipped with
-// a branch that is uniform over the CTA (MPO-tensor blocks are mostly zeros,
-// and FP64 issue slots bound this step).
-template <int NN>
+// j < R, per thread; R (1, 2 or 4) is chosen per plan so that small
+// contractions still spread over the SMs (FP64 issue slots bound this step:
+// about two FP64 FMA per clock per SM). Zero entries of the staged B block are
+// skipped with a branch that is uniform over the CTA (MPO-tensor blocks are
+// mostly zeros).
+template <int NN, int R>
 __device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& cb, const PairRec* __restrict__ pairs,
                                             const int32_t* __restrict__ tab, const double* __restrict__ A,
                                             const double* __restrict__ B, double* __restrict__ C,
                                             double (*Bs)[SKINNY_N]) {
-    double acc[SKINNY_R][NN];
+    double acc[R][NN];
 #pragma unroll
-    for (int j = 0; j < SKINNY_R; ++j)
+    for (int j = 0; j < R; ++j)
 #pragma unroll
         for (int n = 0; n < NN; ++n) acc[j][n] = 0.0;
-    int mrow[SKINNY_R];
+    int mrow[R];
 #pragma unroll
-    for (int j = 0; j < SKINNY_R; ++j) mrow[j] = it.m0 + threadIdx.x + j * SKINNY_THREADS;
+    for (int j = 0; j < R; ++j) mrow[j] = it.m0 + threadIdx.x + j * SKINNY_THREADS;
     for (int p = it.p0; p < it.p1; ++p) {
         const PairRec pr = pairs[p];
-        int arow[SKINNY_R];
+        int arow[R];
 #pragma unroll
-        for (int j = 0; j < SKINNY_R; ++j) arow[j] = mrow[j] < cb.M ? tab[pr.tam + mrow[j]] : -1;
+        for (int j = 0; j < R; ++j) arow[j] = mrow[j] < cb.M ? tab[pr.tam + mrow[j]] : -1;
         for (int k0 = 0; k0 < pr.K; k0 += SKINNY_K) {
             const int kn = min(SKINNY_K, pr.K - k0);
             __syncthreads();
@@ -347,22 +349,22 @@ __device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& 
             __syncthreads();
             for (int k = 0; k < kn; ++k) {
                 const int ko = tab[pr.tak + k0 + k];
-                double a[SKINNY_R];
+                double a[R];
 #pragma unroll
-                for (int j = 0; j < SKINNY_R; ++j) a[j] = arow[j] >= 0 ? A[pr.aoff + arow[j] + ko] : 0.0;
+                for (int j = 0; j < R; ++j) a[j] = arow[j] >= 0 ? A[pr.aoff + arow[j] + ko] : 0.0;
 #pragma unroll
                 for (int n = 0; n < NN; ++n) {
                     const double b = Bs[k][n];
                     if (b != 0.0) {
 #pragma unroll
-                        for (int j = 0; j < SKINNY_R; ++j) acc[j][n] = fma(a[j], b, acc[j][n]);
+                        for (int j = 0; j < R; ++j) acc[j][n] = fma(a[j], b, acc[j][n]);
                     }
                 }
             }
         }
     }
 #pragma unroll
-    for (int j = 0; j < SKINNY_R; ++j) {
+    for (int j = 0; j < R; ++j) {
         if (mrow[j] < cb.M) {
             const int64_t crow = cb.coff + tab[cb.tcm + mrow[j]];
 #pragma unroll
@@ -371,6 +373,7 @@ __device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& 
     }
 }
 
+template <int R>
 __global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_kernel(const ItemRec* __restrict__ items,
                                                                          const PairRec* __restrict__ pairs,
                                                                          const CBlockRec* __restrict__ cblk,
@@ -382,14 +385,29 @@ __global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_kernel(const I
     const ItemRec it = items[blockIdx.x];
     const CBlockRec cb = cblk[it.c];
     switch (cb.N) {
-        case 1: skinny_item<1>(it, cb, pairs, tab, A, B, C, Bs); break;
-        case 2: skinny_item<2>(it, cb, pairs, tab, A, B, C, Bs); break;
-        case 3: skinny_item<3>(it, cb, pairs, tab, A, B, C, Bs); break;
-        case 4: skinny_item<4>(it, cb, pairs, tab, A, B, C, Bs); break;
-        case 5: skinny_item<5>(it, cb, pairs, tab, A, B, C, Bs); break;
-        case 6: skinny_item<6>(it, cb, pairs, tab, A, B, C, Bs); break;
-        case 7: skinny_item<7>(it, cb, pairs, tab, A, B, C, Bs); break;
-        default: skinny_item<8>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 1: skinny_item<1, R>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 2: skinny_item<2, R>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 3: skinny_item<3, R>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 4: skinny_item<4, R>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 5: skinny_item<5, R>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 6: skinny_item<6, R>(it, cb, pairs, tab, A, B, C, Bs); break;
+        case 7: skinny_item<7, R>(it, cb, pairs, tab, A, B, C, Bs); break;
+        default: skinny_item<8, R>(it, cb, pairs, tab, A, B, C, Bs); break;
+    }
+}
+
+// Launches the skinny kernel with the plan's rows per thread.
+static void launch_skinny(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C) {
+    switch (p.skinny_r) {
+        case 1:
+            gemm_f64_skinny_kernel<1><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+            break;
+        case 2:
+            gemm_f64_skinny_kernel<2><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+            break;
+        default:
+            gemm_f64_skinny_kernel<4><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+            break;
     }
 }
 
@@ -805,7 +823,17 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->skinny = (maxN <= SKINNY_N);
         std::vector<ItemRec> items;
         std::vector<double> cost;
-        const int tm = plan->skinny ? SKINNY_M : GEMM_TILE, tn = plan->skinny ? SKINNY_N : GEMM_TILE;
+        if (plan->skinny) {
+            // rows per thread: the largest of 4, 2, 1 that still gives two items per SM
+            plan->skinny_r = 4;
+            while (plan->skinny_r > 1) {
+                int64_t n_items = 0;
+                for (int c = 0; c < ncb; ++c) n_items += (cblk[c].M + SKINNY_THREADS * plan->skinny_r - 1) / (SKINNY_THREADS * plan->skinny_r);
+                if (n_items >= 2 * (int64_t)ctx.sm_count) break;
+                plan->skinny_r /= 2;
+            }
+        }
+        const int tm = plan->skinny ? SKINNY_THREADS * plan->skinny_r : GEMM_TILE, tn = plan->skinny ? SKINNY_N : GEMM_TILE;
         for (int c = 0; c < ncb; ++c)
             for (int m0 = 0; m0 < cblk[c].M; m0 += tm)
                 for (int n0 = 0; n0 < cblk[c].N; n0 += tn) {
@@ -916,7 +944,7 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
     }
     // narrow, small-K contractions (the MPO-tensor steps) are bandwidth-shaped: FP64 is exact there
     if (p.skinny && (prec == PREC_F64 || prec == PREC_OZAKI_BF16)) {
-        gemm_f64_skinny_kernel<<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+        launch_skinny(ctx, p, A, B, C);
     } else if (plan_uses_split(p, prec)) {
         const int S = ctx.ozaki_slices;
         const int64_t plane = (p.panel_elems + 15) / 16 * 16;
@@ -941,7 +969,7 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
 void exec_plan_f64_only(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C) {
     if (p.nitems == 0) return;
     if (p.skinny)
-        gemm_f64_skinny_kernel<<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+        launch_skinny(ctx, p, A, B, C);
     else
         gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
     ITG_CHECK_CUDA(cudaGetLastError());

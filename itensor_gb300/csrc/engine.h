@@ -65,6 +65,7 @@ struct Plan {
     double avgK = 0;
     bool scalar = false;             // rank-0 result
     bool skinny = false;             // every output block is <= 8 columns wide (row tiles)
+    int skinny_r = 4;                // rows per thread of the skinny kernel (row tile = 256 * skinny_r)
     // split-precision operand panels (A blocks, then B blocks)
     OpBlockRec* d_ops = nullptr;
     PrepItem* d_prep = nullptr;
