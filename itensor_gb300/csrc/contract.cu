@@ -845,16 +845,34 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });
         std::vector<ItemRec> sitems(items.size());
         for (size_t i = 0; i < ord.size(); ++i) sitems[i] = items[ord[i]];
+        // 64-row tiles for the wider split-precision variant, in the same cost order
+        std::vector<ItemRec> items64;
+        if (!plan->skinny) {
+            std::vector<ItemRec> raw;
+            std::vector<double> cost64;
+            for (int c = 0; c < ncb; ++c)
+                for (int m0 = 0; m0 < cblk[c].M; m0 += 64)
+                    for (int n0 = 0; n0 < cblk[c].N; n0 += GEMM_TILE) {
+                        raw.push_back(ItemRec{c, m0, n0, cp0[c], cp1[c]});
+                        cost64.push_back(cK[c] + 1.0);
+                    }
+            std::vector<int> o64(raw.size());
+            std::iota(o64.begin(), o64.end(), 0);
+            std::stable_sort(o64.begin(), o64.end(), [&](int x, int y) { return cost64[x] > cost64[y]; });
+            for (int i : o64) items64.push_back(raw[i]);
+        }
         // upload
         size_t t_items = 0, t_pairs = align16(sizeof(ItemRec) * sitems.size());
         size_t t_cblk = align16(t_pairs + sizeof(PairRec) * pairs.size());
         size_t t_ops = align16(t_cblk + sizeof(CBlockRec) * cblk.size());
         size_t t_prep = align16(t_ops + sizeof(OpBlockRec) * ops.size());
-        size_t t_tab = align16(t_prep + sizeof(PrepItem) * prep.size());
+        size_t t_i64 = align16(t_prep + sizeof(PrepItem) * prep.size());
+        size_t t_tab = align16(t_i64 + sizeof(ItemRec) * items64.size());
         size_t tbytes = align16(t_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size()));
         ctx.ensure_stage(tbytes);
         st = static_cast<char*>(ctx.stage);
         if (!sitems.empty()) std::memcpy(st + t_items, sitems.data(), sizeof(ItemRec) * sitems.size());
+        if (!items64.empty()) std::memcpy(st + t_i64, items64.data(), sizeof(ItemRec) * items64.size());
         if (!pairs.empty()) std::memcpy(st + t_pairs, pairs.data(), sizeof(PairRec) * pairs.size());
         if (!cblk.empty()) std::memcpy(st + t_cblk, cblk.data(), sizeof(CBlockRec) * cblk.size());
         if (!ops.empty()) std::memcpy(st + t_ops, ops.data(), sizeof(OpBlockRec) * ops.size());
@@ -878,6 +896,8 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->d_ops = reinterpret_cast<OpBlockRec*>(db + t_ops);
         plan->d_prep = reinterpret_cast<PrepItem*>(db + t_prep);
         plan->d_tab = reinterpret_cast<int32_t*>(db + t_tab);
+        plan->d_items64 = reinterpret_cast<ItemRec*>(db + t_i64);
+        plan->nitems64 = (int)items64.size();
         plan->nitems = (int)sitems.size();
         plan->npairs = np;
         plan->ncblk = ncb;
@@ -950,6 +970,8 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
         const int64_t plane = (p.panel_elems + 15) / 16 * 16;
         __nv_bfloat16* panels = static_cast<__nv_bfloat16*>(ctx.split_buffer(split_scratch_bytes(p, S)));
         int32_t* exps = reinterpret_cast<int32_t*>(panels + plane * S);
+        if (p.oz_variant.load(std::memory_order_relaxed) < 0 && p.flops >= AUTOTUNE_MIN_FLOPS)
+            autotune_ozaki(ctx, p, A, B, C, S, panels, exps);
         launch_ozaki(ctx, p, A, B, C, S, panels, exps);
         ctx.kernel_launches += 1;
     } else if (prec == PREC_F64 || prec == PREC_OZAKI_BF16) {

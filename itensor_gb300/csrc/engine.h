@@ -13,6 +13,7 @@
 // contract(CProps,...) itensor/tensor/contract.cc:733-824.
 #pragma once
 #include "tensor.h"
+#include <atomic>
 #include <mutex>
 
 namespace itg {
@@ -74,6 +75,11 @@ struct Plan {
     int64_t panel_elems = 0;         // bf16 elements per digit plane set (all blocks)
     int64_t exp_elems = 0;
     int max_rows = 0;
+    // 64-row tiles of the same output blocks (the 64 x 32 split-precision variant)
+    ItemRec* d_items64 = nullptr;
+    int nitems64 = 0;
+    // split-precision GEMM variant picked by the autotuner (-1: not tuned, run variant 0)
+    mutable std::atomic<int> oz_variant{-1};
 };
 
 // Plans keyed by block structure. One cache may serve several contexts (the
@@ -180,6 +186,12 @@ void exec_plan_noalloc(Ctx& ctx, Plan const& p, double const* A, double const* B
 // the plan's scratch (S digit planes of the padded panel size, row exponents).
 void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S, __nv_bfloat16* panels,
                   int32_t* exps, bool prep_b = true);
+// Times every split-precision GEMM variant of the plan on these operands and
+// stores the fastest in p.oz_variant (ozaki.cu); C is overwritten.
+int autotune_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S,
+                   __nv_bfloat16* panels, int32_t* exps);
+// Plans with at least this many algorithmic flops are tuned on first use.
+constexpr double AUTOTUNE_MIN_FLOPS = 2e7;
 // Whether exec_plan runs this plan with the split-precision kernels.
 // (The int64 digit sums of one block pair are exact up to K = 8192.)
 constexpr int SPLIT_MAX_PAIR_K = 8192;

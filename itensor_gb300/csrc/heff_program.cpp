@@ -97,6 +97,9 @@ void HeffProgram::launch_steps(Ctx& ctx) {
                 pr.kind = 1;
                 pr.nitems = p.nitems;
             }
+            // first run (never inside a graph capture): pick the GEMM tile shape on this data
+            if (!st.operand_sliced && p.oz_variant.load(std::memory_order_relaxed) < 0 && p.flops >= AUTOTUNE_MIN_FLOPS)
+                autotune_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps);
             launch_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps, !st.operand_sliced);
             if (ctx.profiling) {
                 ITG_CHECK_CUDA(cudaEventRecord(pr.stop, ctx.stream));

@@ -19,9 +19,10 @@
 //
 // prep: one CTA per item of whole rows (~2048 elements) writes the row
 //       exponents and the S digit planes, k-contiguous, K padded to 16.
-// gemm: one CTA (4 warps, 16x16 each) per 32x32 output tile; digit panels are
-//       staged with cp.async into a two-stage shared-memory ring and read
-//       with ldmatrix.
+// gemm: output tiles of 32 x 32 (4 warps of 16 x 16) or 64 x 32 (8 warps),
+//       one CTA per tile or persistent CTAs over the tile list; the variant
+//       is chosen per plan by autotune_ozaki. Digit panels are staged with
+//       cp.async into a two-stage shared-memory ring and read with ldmatrix.
 #include "engine.h"
 #include <cuda_bf16.h>
 
@@ -116,24 +117,30 @@ __device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void* smem) 
                  : "r"(a));
 }
 
-template <int S>
-__global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __restrict__ items,
-                                                         const PairRec* __restrict__ pairs,
-                                                         const CBlockRec* __restrict__ cblk,
-                                                         const OpBlockRec* __restrict__ ops,
-                                                         const int32_t* __restrict__ tab,
-                                                         const __nv_bfloat16* __restrict__ panels, int64_t plane,
-                                                         const int32_t* __restrict__ exps, double* __restrict__ C) {
-    constexpr int T = GEMM_TILE, TK = 16, LD = TK + 8;  // row stride 48 B: 16-B aligned, no ldmatrix conflicts
+// One output tile of TM = 16 WM rows x 32 columns, WM x 2 warps of 16 x 16
+// (2 mma n-tiles each). Panels are staged with cp.async into a two-stage ring
+// and read with ldmatrix; per pair the S(S+1)/2 digit products go to S FP32
+// diagonal accumulators, folded into int64 every KCHUNK k, and the pair's int64
+// sum is scaled into the FP64 output (integer instructions) and added.
+template <int S, int WM>
+__device__ __forceinline__ void oz_tile(ItemRec const& it, const PairRec* __restrict__ pairs,
+                                        const CBlockRec* __restrict__ cblk, const OpBlockRec* __restrict__ ops,
+                                        const int32_t* __restrict__ tab, const __nv_bfloat16* __restrict__ panels,
+                                        int64_t plane, const int32_t* __restrict__ exps, double* __restrict__ C,
+                                        unsigned char* smem) {
+    constexpr int TM = 16 * WM, TN = 32, TK = 16, LD = TK + 8;  // row stride 48 B: 16-B aligned, no ldmatrix conflicts
+    constexpr int NT = 64 * WM;
     constexpr int KCHUNK = (S <= 4) ? 256 : 128;
     static_assert((long long)KCHUNK * S * 127 * 127 <= (1LL << 24), "digit sums must stay exact in FP32");
-    __shared__ __align__(16) __nv_bfloat16 As[2][S][T][LD];
-    __shared__ __align__(16) __nv_bfloat16 Bs[2][S][T][LD];
-    __shared__ int ea[T], eb[T];
-    const ItemRec it = items[blockIdx.x];
+    typedef __nv_bfloat16 TileA[S][TM][LD];
+    typedef __nv_bfloat16 TileB[S][TN][LD];
+    TileA* As = reinterpret_cast<TileA*>(smem);                      // [2]
+    TileB* Bs = reinterpret_cast<TileB*>(smem + 2 * sizeof(TileA));  // [2]
+    int* ea = reinterpret_cast<int*>(smem + 2 * sizeof(TileA) + 2 * sizeof(TileB));
+    int* eb = ea + TM;
     const CBlockRec cb = cblk[it.c];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = (warp & 1) * 16, wn = (warp >> 1) * 16;  // warp tile 16x16 = 2 mma n-tiles
+    const int wm = (warp % WM) * 16, wn = (warp / WM) * 16;
     const int g = lane >> 2, tg = lane & 3;
     // ldmatrix lane addresses (see the m16n8k16 fragment layouts)
     const int a_row = wm + (lane & 15), a_col = (lane >> 4) * 8;
@@ -148,15 +155,17 @@ __global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __res
         const OpBlockRec oa = ops[pr.ia], ob = ops[pr.ib];
         const __nv_bfloat16* pa = panels + oa.panel;
         const __nv_bfloat16* pb = panels + ob.panel;
-        // stage k-step k0 into ring slot `buf`: S planes x 32 rows x 2 halves, for A and B
+        // stage k-step k0 into ring slot `buf`: S planes x rows x 2 halves, for A and B
         auto stage = [&](int k0, int buf) {
-            for (int e = tid; e < 2 * S * T * 2; e += 128) {
-                const int half = e & 1, row = (e >> 1) % T, s = ((e >> 1) / T) % S, isb = (e >> 1) / (T * S);
-                if (!isb) {
+            for (int e = tid; e < 2 * S * (TM + TN); e += NT) {
+                const int half = e & 1, r2 = e >> 1;
+                if (r2 < S * TM) {
+                    const int row = r2 % TM, s = r2 / TM;
                     const bool ok = it.m0 + row < cb.M;
                     const __nv_bfloat16* src = ok ? pa + s * plane + (int64_t)(it.m0 + row) * oa.Kp + k0 + half * 8 : pa;
                     cp_async16(&As[buf][s][row][half * 8], src, ok);
                 } else {
+                    const int row = (r2 - S * TM) % TN, s = (r2 - S * TM) / TN;
                     const bool ok = it.n0 + row < cb.N;
                     const __nv_bfloat16* src = ok ? pb + s * plane + (int64_t)(it.n0 + row) * ob.Kp + k0 + half * 8 : pb;
                     cp_async16(&Bs[buf][s][row][half * 8], src, ok);
@@ -164,8 +173,10 @@ __global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __res
             }
             cp_async_commit();
         };
-        if (tid < T) ea[tid] = (it.m0 + tid < cb.M) ? exps[oa.exp + it.m0 + tid] : 0;
-        else if (tid < 2 * T) eb[tid - T] = (it.n0 + tid - T < cb.N) ? exps[ob.exp + it.n0 + tid - T] : 0;
+        for (int r = tid; r < TM + TN; r += NT) {
+            if (r < TM) ea[r] = (it.m0 + r < cb.M) ? exps[oa.exp + it.m0 + r] : 0;
+            else eb[r - TM] = (it.n0 + r - TM < cb.N) ? exps[ob.exp + it.n0 + r - TM] : 0;
+        }
         long long tot[2][4];
         float acc[S][2][4];
 #pragma unroll
@@ -200,8 +211,8 @@ __global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __res
 #pragma unroll
                     for (int j = 0; j < 2; ++j) {
                         float* c = acc[s + t][j];
-                        asm volatile(
-                            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                        // register-only: not volatile, so the compiler may interleave independent MMAs
+                        asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
                             "{%8,%9}, {%0,%1,%2,%3};\n"
                             : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
                             : "r"(af[0]), "r"(af[1]), "r"(af[2]), "r"(af[3]), "r"(bfr[t][2 * j]),
@@ -218,7 +229,8 @@ __global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __res
                         long long v = 0;
 #pragma unroll
                         for (int d = 0; d < S; ++d) {
-                            v += (long long)__float2ll_rn(acc[d][j][q]) << (7 * (S - 1 - d));
+                            // |acc| < 2^24: a 32-bit conversion is exact (64-bit ones issue on the FP64 pipe)
+                            v += (long long)__float2int_rn(acc[d][j][q]) << (7 * (S - 1 - d));
                             acc[d][j][q] = 0.f;
                         }
                         tot[j][q] += v;
@@ -248,27 +260,140 @@ __global__ void __launch_bounds__(128, 4) gemm_ozaki_kernel(const ItemRec* __res
         }
 }
 
+template <int S, int WM>
+constexpr size_t oz_smem_bytes() {
+    return sizeof(__nv_bfloat16) * 2 * S * (16 * WM + 32) * (16 + 8) + sizeof(int) * (16 * WM + 32);
+}
+
+// PERSIST: a grid of (SMs x resident CTAs) walks the cost-ordered tile list
+// with a fixed stride; otherwise one CTA per tile. Either way every output
+// element is computed by one thread in the same order, so all variants give
+// bit-identical results.
+template <int S, int WM, bool PERSIST>
+__global__ void __launch_bounds__(64 * WM, (WM == 2 ? 4 : 2))
+gemm_ozaki_kernel(const ItemRec* __restrict__ items, int nitems, const PairRec* __restrict__ pairs,
+                  const CBlockRec* __restrict__ cblk, const OpBlockRec* __restrict__ ops, const int32_t* __restrict__ tab,
+                  const __nv_bfloat16* __restrict__ panels, int64_t plane, const int32_t* __restrict__ exps,
+                  double* __restrict__ C) {
+    extern __shared__ __align__(16) unsigned char oz_smem[];
+    if (PERSIST) {
+        for (int i = blockIdx.x; i < nitems; i += gridDim.x)
+            oz_tile<S, WM>(items[i], pairs, cblk, ops, tab, panels, plane, exps, C, oz_smem);
+    } else {
+        oz_tile<S, WM>(items[blockIdx.x], pairs, cblk, ops, tab, panels, plane, exps, C, oz_smem);
+    }
+}
+
+namespace {
+// Resident CTAs per SM of a variant (queried once per process).
+template <int S, int WM, bool PERSIST>
+int oz_resident() {
+    static int r = [] {
+        int n = 0;
+        cudaFuncSetAttribute(gemm_ozaki_kernel<S, WM, PERSIST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)oz_smem_bytes<S, WM>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gemm_ozaki_kernel<S, WM, PERSIST>, 64 * WM,
+                                                      oz_smem_bytes<S, WM>());
+        return std::max(1, n);
+    }();
+    return r;
+}
+
+template <int S, int WM, bool PERSIST>
+void launch_gemm(Ctx& ctx, Plan const& p, double* C, __nv_bfloat16 const* panels, int64_t plane, int32_t const* exps) {
+    const ItemRec* items = WM == 2 ? p.d_items : p.d_items64;
+    const int nitems = WM == 2 ? p.nitems : p.nitems64;
+    if (nitems == 0) return;
+    const int resident = oz_resident<S, WM, PERSIST>();
+    const int grid = PERSIST ? std::min(nitems, ctx.sm_count * resident) : nitems;
+    gemm_ozaki_kernel<S, WM, PERSIST><<<grid, 64 * WM, oz_smem_bytes<S, WM>(), ctx.stream>>>(
+        items, nitems, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C);
+}
+
 template <int S>
-static void launch_s(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, __nv_bfloat16* panels,
-                     int64_t plane, int32_t* exps, bool prep_b) {
+void launch_variant(Ctx& ctx, Plan const& p, int v, double* C, __nv_bfloat16 const* panels, int64_t plane,
+                    int32_t const* exps) {
+    switch (v) {
+        case 1: launch_gemm<S, 4, false>(ctx, p, C, panels, plane, exps); break;
+        case 2: launch_gemm<S, 2, true>(ctx, p, C, panels, plane, exps); break;
+        case 3: launch_gemm<S, 4, true>(ctx, p, C, panels, plane, exps); break;
+        default: launch_gemm<S, 2, false>(ctx, p, C, panels, plane, exps); break;
+    }
+}
+
+template <int S>
+void launch_s(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, __nv_bfloat16* panels,
+              int64_t plane, int32_t* exps, bool prep_b, int variant) {
     // A items come first: without prep_b only A is sliced (B's panels are already in place)
     const int nprep = prep_b ? p.nprep : p.nprepA;
     if (nprep > 0)
         ozaki_prep_kernel<S><<<nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
-    gemm_ozaki_kernel<S><<<p.nitems, 128, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels,
-                                                           plane, exps, C);
+    launch_variant<S>(ctx, p, variant, C, panels, plane, exps);
 }
+}  // namespace
 
 void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S,
                   __nv_bfloat16* panels, int32_t* exps, bool prep_b) {
     const int64_t plane = (p.panel_elems + 15) / 16 * 16;
+    const int v = std::max(0, p.oz_variant.load(std::memory_order_relaxed));
     switch (S) {
-        case 3: launch_s<3>(ctx, p, A, B, C, panels, plane, exps, prep_b); break;
-        case 4: launch_s<4>(ctx, p, A, B, C, panels, plane, exps, prep_b); break;
-        case 5: launch_s<5>(ctx, p, A, B, C, panels, plane, exps, prep_b); break;
-        default: launch_s<6>(ctx, p, A, B, C, panels, plane, exps, prep_b); break;
+        case 3: launch_s<3>(ctx, p, A, B, C, panels, plane, exps, prep_b, v); break;
+        case 4: launch_s<4>(ctx, p, A, B, C, panels, plane, exps, prep_b, v); break;
+        case 5: launch_s<5>(ctx, p, A, B, C, panels, plane, exps, prep_b, v); break;
+        default: launch_s<6>(ctx, p, A, B, C, panels, plane, exps, prep_b, v); break;
     }
     ITG_CHECK_CUDA(cudaGetLastError());
+}
+
+// Tile-shape autotuner: slices both operands once, then times every variant
+// (32 x 32 or 64 x 32 tiles; one CTA per tile or persistent CTAs) on the
+// plan's own data with CUDA events and keeps the fastest in the plan. The
+// variants give bit-identical results, so tuning changes only the time.
+int autotune_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S,
+                   __nv_bfloat16* panels, int32_t* exps) {
+    const int64_t plane = (p.panel_elems + 15) / 16 * 16;
+    auto prep = [&] {
+        if (p.nprep == 0) return;
+        switch (S) {
+            case 3: ozaki_prep_kernel<3><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
+            case 4: ozaki_prep_kernel<4><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
+            case 5: ozaki_prep_kernel<5><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
+            default: ozaki_prep_kernel<6><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
+        }
+    };
+    auto run = [&](int v) {
+        switch (S) {
+            case 3: launch_variant<3>(ctx, p, v, C, panels, plane, exps); break;
+            case 4: launch_variant<4>(ctx, p, v, C, panels, plane, exps); break;
+            case 5: launch_variant<5>(ctx, p, v, C, panels, plane, exps); break;
+            default: launch_variant<6>(ctx, p, v, C, panels, plane, exps); break;
+        }
+    };
+    prep();
+    constexpr int NV = 4, REPS = 3;
+    cudaEvent_t ev[NV][2];
+    for (int v = 0; v < NV; ++v)
+        for (int k = 0; k < 2; ++k) ITG_CHECK_CUDA(cudaEventCreate(&ev[v][k]));
+    for (int v = 0; v < NV; ++v) {
+        run(v);  // warm
+        ITG_CHECK_CUDA(cudaEventRecord(ev[v][0], ctx.stream));
+        for (int r = 0; r < REPS; ++r) run(v);
+        ITG_CHECK_CUDA(cudaEventRecord(ev[v][1], ctx.stream));
+    }
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches += 1 + NV * (REPS + 1);
+    ctx.sync();
+    int best = 0;
+    float best_ms = 0;
+    for (int v = 0; v < NV; ++v) {
+        float ms = 0;
+        ITG_CHECK_CUDA(cudaEventElapsedTime(&ms, ev[v][0], ev[v][1]));
+        if (v == 0 || ms < best_ms) { best = v; best_ms = ms; }
+    }
+    for (int v = 0; v < NV; ++v)
+        for (int k = 0; k < 2; ++k) cudaEventDestroy(ev[v][k]);
+    p.oz_variant.store(best, std::memory_order_relaxed);
+    return best;
 }
 
 }  // namespace itg
