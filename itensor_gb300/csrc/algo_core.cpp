@@ -417,6 +417,7 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
     const int64_t maxsize = dense_size(phi);
     const int actual_maxiter = (int)std::min<int64_t>(maxiter, maxsize - 1);
     const int msz = actual_maxiter + 2;
+    ITG_REQUIRE(msz + 1 <= VecList::MAX, "davidson: at most " + std::to_string(VecList::MAX - 3) + " iterations");
     std::vector<Tensor> V(msz), AV(msz);
     std::vector<double> M((size_t)msz * msz, std::numeric_limits<double>::quiet_NaN());
     auto Mat = [&](int i, int j) -> double& { return M[(size_t)j * msz + i]; };
@@ -438,11 +439,15 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
     for (ii = 0; ii <= actual_maxiter; ++ii) {
         const int ni = ii + 1;
         Tensor q(phi.lay, ctx.stream);
+        double qnorm2 = 0;
         if (ii == 0) {
             lambda = initEn;
             Mat(0, 0) = lambda;
-            ITG_CHECK_CUDA(cudaMemcpyAsync(q.data(), AV[0].data(), sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
-            launch_axpy(ctx, q.data(), V[0].data(), n, -lambda);
+            // q = H V0 - lambda V0 and |q|^2, one launch
+            VecList L;
+            L.add(AV[0].data(), 1.0);
+            L.add(V[0].data(), -lambda);
+            qnorm2 = combo(ctx, q.data(), 0.0, L, n, true);
         } else {
             std::vector<double> Msub((size_t)(ii + 1) * (ii + 1));
             for (int j = 0; j <= ii; ++j) for (int i = 0; i <= ii; ++i) Msub[(size_t)j * (ii + 1) + i] = Mat(i, j);
@@ -450,16 +455,18 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
             lambda = D[0];
             const double sgn = U[0] < 0 ? -1.0 : 1.0;  // fix sign: U(0,t) >= 0
             Tensor pt(phi.lay, ctx.stream);
-            launch_axpby(ctx, pt.data(), V[0].data(), n, sgn * U[0], 0.0);
-            launch_axpby(ctx, q.data(), AV[0].data(), n, sgn * U[0], 0.0);
-            for (int k = 1; k <= ii; ++k) {
-                launch_axpy(ctx, pt.data(), V[k].data(), n, sgn * U[k]);
-                launch_axpy(ctx, q.data(), AV[k].data(), n, sgn * U[k]);
+            // Ritz vector pt = sum_k u_k V_k and residual q = sum_k u_k H V_k - lambda pt
+            VecList Lp, Lq;
+            for (int k = 0; k <= ii; ++k) {
+                Lp.add(V[k].data(), sgn * U[k]);
+                Lq.add(AV[k].data(), sgn * U[k]);
             }
-            launch_axpy(ctx, q.data(), pt.data(), n, -lambda);
+            Lq.add(pt.data(), -lambda);
+            combo(ctx, pt.data(), 0.0, Lp, n, false);
+            qnorm2 = combo(ctx, q.data(), 0.0, Lq, n, true);
             phi_t = pt;
         }
-        const double qnorm = norm(ctx, q.data(), n);
+        const double qnorm = std::sqrt(std::max(qnorm2, 0.0));
         const bool converged = (qnorm < errgoal && std::abs(lambda - last_lambda) < errgoal) ||
                                qnorm < std::max(approx0, errgoal * 1e-3);
         last_lambda = lambda;
@@ -473,8 +480,9 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
             for (int k = 0; k < ni; ++k) vp[k] = V[k].data();
             std::vector<double> Vq(ni);
             dots(ctx, vp.data(), ni, q.data(), n, Vq.data());
-            for (int k = 0; k < ni; ++k) launch_axpy(ctx, q.data(), V[k].data(), n, -Vq[k]);
-            double qnrm = norm(ctx, q.data(), n);
+            VecList Lg;
+            for (int k = 0; k < ni; ++k) Lg.add(V[k].data(), -Vq[k]);
+            double qnrm = std::sqrt(std::max(combo(ctx, q.data(), 1.0, Lg, n, true), 0.0));
             if (qnrm < 1e-10) {
                 launch_random(ctx, q.data(), n, 0x9e3779b9ull * (ni + 7 * tot_pass));
                 qnrm = norm(ctx, q.data(), n);

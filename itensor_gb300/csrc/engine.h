@@ -136,6 +136,9 @@ struct Ctx {
     DevBufPtr split_scratch;
     // event used by sync() when the calling thread multiplexes solves
     cudaEvent_t sync_event = nullptr;
+    // partial sums + completion counter of the fused reductions (ops.cu)
+    DevBufPtr reduce_buf;
+    void ensure_reduce();
     // counters
     uint64_t kernel_launches = 0;
     uint64_t plans_built = 0, plan_hits = 0;
@@ -216,6 +219,17 @@ void launch_axpby(Ctx& ctx, double* y, double const* x, int64_t n, double a, dou
 void dots(Ctx& ctx, double const* const* V, int nv, double const* x, int64_t n, double* out);
 double dot(Ctx& ctx, double const* a, double const* b, int64_t n);
 double norm(Ctx& ctx, double const* a, int64_t n);
+// Up to MAX device vectors with coefficients, passed to kernels by value.
+struct VecList {
+    static constexpr int MAX = 24;
+    double const* p[MAX];
+    double c[MAX];
+    int n = 0;
+    void add(double const* x, double a) { p[n] = x; c[n] = a; ++n; }
+};
+// y = a0 y + sum_k c_k X_k in one launch (y is not read when a0 == 0); returns
+// |y|^2 when want_norm (then waits for the stream), else 0.
+double combo(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, bool want_norm);
 // General block permute / gather: dst[dst_off[e]] = src[src_off[e]] described per
 // block by offset tables (see ops.cu). Used for combiner, uncombine and
 // layout changes.

@@ -103,8 +103,16 @@ __global__ void dots_final_kernel(double const* part, int nparts, int nv, double
     }
 }
 
+void dots_fused(Ctx& ctx, VecList const& V, double const* x, int64_t n, double* out);
+
 void dots(Ctx& ctx, double const* const* V, int nv, double const* x, int64_t n, double* out) {
     if (nv <= 0) return;
+    if (nv <= VecList::MAX) {
+        VecList L;
+        for (int k = 0; k < nv; ++k) L.add(V[k], 0.0);
+        dots_fused(ctx, L, x, n, out);
+        return;
+    }
     // pointer list + partials + results in one pool allocation; result via mapped memory
     size_t o_ptr = 0, o_part = ((sizeof(void*) * nv + 15) / 16) * 16;
     size_t bytes = o_part + sizeof(double) * (size_t)DOT_CTAS * nv;
@@ -134,6 +142,124 @@ double dot(Ctx& ctx, double const* a, double const* b, int64_t n) {
 double norm(Ctx& ctx, double const* a, int64_t n) {
     double r = dot(ctx, a, a, n);
     return std::sqrt(std::max(r, 0.0));
+}
+
+// ------------------------------------------------------------------ fused combinations
+// y = a0 y + sum_k c_k X_k (y not read when a0 == 0), the terms added in k
+// order with one FMA each (the same rounding as a chain of axpy calls), and
+// optionally |y|^2: per-CTA partial sums in a fixed order, reduced by the last
+// CTA to finish (deterministic whichever CTA that is). Pointers and
+// coefficients travel as kernel parameters: no upload, one launch.
+__global__ void combo_kernel(double* __restrict__ y, double a0, VecList X, int64_t n, int want_norm,
+                             double* __restrict__ part, unsigned int* __restrict__ counter, double* __restrict__ out) {
+    __shared__ double sh[32];
+    __shared__ bool last;
+    double s2 = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double v = (a0 == 0.0) ? 0.0 : (a0 == 1.0 ? y[i] : a0 * y[i]);
+        int k = 0;
+        if (a0 == 0.0 && X.n > 0) { v = X.c[0] * X.p[0][i]; k = 1; }
+        for (; k < X.n; ++k) v = fma(X.c[k], X.p[k][i], v);
+        y[i] = v;
+        s2 = fma(v, v, s2);
+    }
+    if (!want_norm) return;
+    for (int o = 16; o; o >>= 1) s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+        part[blockIdx.x] = t;
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        double t = 0;
+        for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(part + b);
+        *out = t;
+        *counter = 0;  // ready for the next launch on this stream
+    }
+}
+
+// Dot products of x with every vector of V in one launch: partials per CTA in
+// a fixed order, the last CTA to finish reduces them in CTA order.
+__global__ void dots_fused_kernel(VecList V, double const* __restrict__ x, int64_t n, double* __restrict__ part,
+                                  unsigned int* __restrict__ counter, double* __restrict__ out) {
+    __shared__ double sh[32];
+    __shared__ bool last;
+    for (int v = 0; v < V.n; ++v) {
+        double const* a = V.p[v];
+        double s = 0;
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+            s = fma(a[i], x[i], s);
+        for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+            part[(size_t)v * gridDim.x + blockIdx.x] = t;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int v = threadIdx.x; v < V.n; v += blockDim.x) {
+        double t = 0;
+        for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(part + (size_t)v * gridDim.x + b);
+        out[v] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *counter = 0;  // ready for the next launch on this stream
+}
+
+namespace {
+constexpr size_t REDUCE_DOUBLES = (size_t)DOT_CTAS * VecList::MAX + 4;
+}
+
+void Ctx::ensure_reduce() {
+    if (reduce_buf) return;
+    reduce_buf = dev_alloc(sizeof(double) * REDUCE_DOUBLES, stream);
+    ITG_CHECK_CUDA(cudaMemsetAsync(reduce_buf->p, 0, sizeof(double) * REDUCE_DOUBLES, stream));
+}
+
+void dots_fused(Ctx& ctx, VecList const& V, double const* x, int64_t n, double* out) {
+    ctx.ensure_reduce();
+    ctx.ensure_pin(sizeof(double) * VecList::MAX);
+    double* part = ctx.reduce_buf->as<double>();
+    unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
+    dots_fused_kernel<<<nb, 256, 0, ctx.stream>>>(V, x, n, part, counter, static_cast<double*>(ctx.pin_dev));
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches++;
+    ctx.sync();
+    std::memcpy(out, ctx.pin, sizeof(double) * V.n);
+}
+
+double combo(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, bool want_norm) {
+    ITG_REQUIRE(X.n >= 0 && X.n <= VecList::MAX, "combo: too many terms");
+    if (n <= 0) return 0.0;
+    ctx.ensure_reduce();
+    ctx.ensure_pin(sizeof(double));
+    double* part = ctx.reduce_buf->as<double>();
+    unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
+    combo_kernel<<<nb, 256, 0, ctx.stream>>>(y, a0, X, n, want_norm ? 1 : 0, part, counter,
+                                             static_cast<double*>(ctx.pin_dev));
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches++;
+    if (!want_norm) return 0.0;
+    ctx.sync();
+    return *static_cast<double*>(ctx.pin);
 }
 
 // ------------------------------------------------------------------ gather

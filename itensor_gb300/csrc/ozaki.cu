@@ -25,6 +25,9 @@
 //       cp.async into a two-stage shared-memory ring and read with ldmatrix.
 #include "engine.h"
 #include <cuda_bf16.h>
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 
 namespace itg {
 
@@ -389,6 +392,15 @@ int autotune_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, do
         float ms = 0;
         ITG_CHECK_CUDA(cudaEventElapsedTime(&ms, ev[v][0], ev[v][1]));
         if (v == 0 || ms < best_ms) { best = v; best_ms = ms; }
+    }
+    if (std::getenv("ITG_TUNE_LOG")) {
+        std::fprintf(stderr, "itg autotune: %d tiles, %.3g flops:", p.nitems, p.flops);
+        for (int v = 0; v < NV; ++v) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[v][0], ev[v][1]);
+            std::fprintf(stderr, " v%d %.1f us", v, 1e3 * ms / REPS);
+        }
+        std::fprintf(stderr, " -> v%d\n", best);
     }
     for (int v = 0; v < NV; ++v)
         for (int k = 0; k < 2; ++k) cudaEventDestroy(ev[v][k]);
