@@ -55,6 +55,7 @@ SIGNATURES = {
     "itg_last_error": (C.c_char_p, [C.c_void_p]),
     "itg_synchronize": (C.c_int, [C.c_void_p]),
     "itg_set_precision": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "itg_set_gemm_variant": (C.c_int, [C.c_void_p, C.c_int]),
     "itg_stats": (C.c_int, [C.c_void_p, _u64p, _f64p, _u64p, _u64p]),
     "itg_reset_stats": (C.c_int, [C.c_void_p]),
     "itg_stream": (C.c_void_p, [C.c_void_p]),
@@ -325,6 +326,10 @@ class Context:
 
     def set_precision(self, mode, slices=6):
         self._ok(lib().itg_set_precision(self.h, mode, slices), self.h)
+
+    def set_gemm_variant(self, variant):
+        """-1: autotuned; 0..3: forced split-GEMM tile variant."""
+        self._ok(lib().itg_set_gemm_variant(self.h, variant), self.h)
 
     def stats(self):
         a, f, b, c = C.c_uint64(), C.c_double(), C.c_uint64(), C.c_uint64()

@@ -112,6 +112,13 @@ int itg_set_precision(itg_ctx* c, int mode, int slices) {
     });
 }
 
+int itg_set_gemm_variant(itg_ctx* c, int variant) {
+    return guard(c, [&] {
+        ITG_REQUIRE(variant >= -1 && variant <= 3, "gemm variant must be -1..3");
+        c->ctx.gemm_variant = variant;
+    });
+}
+
 int itg_stats(itg_ctx* c, uint64_t* launches, double* flops, uint64_t* built, uint64_t* hits) {
     return guard(c, [&] {
         if (launches) *launches = c->ctx.kernel_launches;

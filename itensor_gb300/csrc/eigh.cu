@@ -10,24 +10,27 @@
 //   1. every pair's rotation (c, s, t) from its 2x2 pivot;
 //   2. A <- J^T A J as independent 2x2 block updates R_k^T A[k,l] R_l over
 //      block pairs k <= l (the mirror block written from the same values, so
-//      A stays exactly symmetric and only half the blocks are computed), and
-//      V <- V J on column pairs.
+//      A stays exactly symmetric and only half the blocks are computed).
 // FP64 issue slots (~2 FMA per clock per SM on this part) bound the kernel, so
-// block pairs whose two rotations are both the identity are skipped.
-// A rotation is skipped when |a_pq| <= max(1e-15 sqrt(|a_pp a_qq|), 1e-17 ||A||_F):
-// the relative test of Demmel & Veselic, plus an absolute floor at which a
-// rotation moves no eigenvalue by more than 1e-17 ||A||_F. The matrix is
-// converged when a sweep skips every pair. Sweeps are capped; a capped matrix
-// still counts as converged when its largest off-diagonal entry is below
-// 1e-13 ||A||_F. The matrix and vectors live in shared memory when they fit
-// (n up to ~118 for both, ~166 for the matrix alone), else in global scratch.
+// block pairs whose two rotations are both the identity are skipped, and the
+// eigenvectors are not accumulated inside the CTA: every round's (c, s) is
+// logged, and a second kernel applies the logged rotations to the rows of
+// V = I, a few rows per CTA over many SMs (rows transform independently;
+// the rotations of one round touch disjoint columns). Blocks too large for
+// the log fall back to accumulating V in the CTA.
+// A rotation is skipped when |a_pq| <= max(1e-15 sqrt(|a_pp a_qq|), 2^-52 ||A||_F):
+// the relative test of Demmel & Veselic with an absolute floor at the
+// backward-error level of a dense symmetric eigensolver (LAPACK's dsyev is
+// accurate to O(eps ||A||) in absolute terms). The matrix is converged when a
+// sweep skips every pair. Sweeps are capped; a capped matrix still counts as
+// converged when its largest off-diagonal entry is below 1e-13 ||A||_F.
 #include "ops.h"
 #include <algorithm>
 #include <cstring>
 
 namespace itg {
 
-constexpr int EIG_MAX_SWEEPS = 60;
+constexpr int EIG_MAX_SWEEPS = 30;
 constexpr int EIG_THREADS = 256;
 
 struct JacobiShared {
@@ -53,13 +56,16 @@ __device__ __forceinline__ void round_pair(int r, int k, int np, int& p, int& q)
     q = max(a, b);
 }
 
-// Runs sweeps on the symmetric n x n matrix A (element (i,j) at A[j*lda+i]) and
-// accumulates the rotations into V (n x n, element (i,j) at V[j*ldv+i]).
-// Returns true when a sweep skipped every pair.
-__device__ bool jacobi_run(double* A, int lda, double* V, int ldv, int n, int np, double abs_floor,
-                           JacobiShared sh) {
+// Runs sweeps on the symmetric n x n matrix A (element (i,j) at A[j*lda+i]).
+// Rotations are accumulated into V (element (i,j) at V[j*ldv+i]) when V is
+// given, and logged as (c, s) per pair and round when rlog is given. Returns
+// the number of sweeps run; *converged tells whether the last one skipped
+// every pair.
+__device__ int jacobi_run(double* A, int lda, double* V, int ldv, double2* rlog, int n, int np, double abs_floor,
+                          JacobiShared sh, bool* converged) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int half = np / 2;
+    *converged = false;
     for (int sweep = 0; sweep < EIG_MAX_SWEEPS; ++sweep) {
         if (tid == 0) *sh.rotated = 0;
         __syncthreads();
@@ -85,6 +91,7 @@ __device__ bool jacobi_run(double* A, int lda, double* V, int ldv, int n, int np
                 sh.cst[3 * k + 2] = t;
                 sh.pq[2 * k] = p;
                 sh.pq[2 * k + 1] = q;
+                if (rlog) rlog[((size_t)sweep * (np - 1) + r) * half + k] = make_double2(c, s);
             }
             __syncthreads();
             // 2a. A <- J^T A J, block pairs k <= l
@@ -123,38 +130,53 @@ __device__ bool jacobi_run(double* A, int lda, double* V, int ldv, int n, int np
                 if (qk) { A[(size_t)u * lda + q] = z2; A[(size_t)q * lda + u] = z2; }
                 if (qk && wl) { A[(size_t)w * lda + q] = v2; A[(size_t)q * lda + w] = v2; }
             }
-            // 2b. V <- V J on column pairs (rows contiguous)
-            for (int e = tid; e < half * n; e += nt) {
-                const int i = e % n, k = e / n;
-                const double s = sh.cst[3 * k + 1];
-                if (s == 0.0) continue;
-                const double c = sh.cst[3 * k];
-                const int p = sh.pq[2 * k], q = sh.pq[2 * k + 1];
-                const double a = V[(size_t)p * ldv + i], b = V[(size_t)q * ldv + i];
-                V[(size_t)p * ldv + i] = c * a - s * b;
-                V[(size_t)q * ldv + i] = s * a + c * b;
+            // 2b. V <- V J on column pairs (rows contiguous), when accumulated here
+            if (V) {
+                for (int e = tid; e < half * n; e += nt) {
+                    const int i = e % n, k = e / n;
+                    const double s = sh.cst[3 * k + 1];
+                    if (s == 0.0) continue;
+                    const double c = sh.cst[3 * k];
+                    const int p = sh.pq[2 * k], q = sh.pq[2 * k + 1];
+                    const double a = V[(size_t)p * ldv + i], b = V[(size_t)q * ldv + i];
+                    V[(size_t)p * ldv + i] = c * a - s * b;
+                    V[(size_t)q * ldv + i] = s * a + c * b;
+                }
             }
             __syncthreads();
         }
         const bool done = (*sh.rotated == 0);
         __syncthreads();
-        if (done) return true;
+        if (done) {
+            *converged = true;
+            return sweep + 1;
+        }
     }
-    return false;
+    return EIG_MAX_SWEEPS;
 }
 
+// One block on the device: EigItem plus the offset of its rotation log
+// (double2 units; -1 when V is accumulated in the CTA).
+struct EigJob {
+    int64_t a_off, v_off, w_off, s_off, r_off;
+    int32_t n, pad;
+};
+
 template <bool SMEM_A, bool SMEM_V>
-__global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigItem const* __restrict__ items, double const* __restrict__ src,
+__global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigJob const* __restrict__ jobs, double const* __restrict__ src,
                                                              double* __restrict__ vout, double* __restrict__ wout,
-                                                             double* __restrict__ scratch, int* __restrict__ status) {
+                                                             double* __restrict__ scratch, double2* __restrict__ rlog,
+                                                             int* __restrict__ ranks, int* __restrict__ sweeps_out,
+                                                             int* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char eig_smem[];
     __shared__ int rotated;
     __shared__ double red[32];
-    const EigItem it = items[blockIdx.x];
+    const EigJob it = jobs[blockIdx.x];
     const int n = it.n;
     const int np = n + (n & 1);
     const int half = np / 2;
     const int tid = threadIdx.x;
+    const bool logv = it.r_off >= 0;
     // shared layout: cst (3 half doubles) | [A (np x (np+1))] | [V (n x n)] | pq (2 half ints) | rank (n ints)
     double* cst = reinterpret_cast<double*>(eig_smem);
     double* sp = cst + 3 * half;
@@ -162,18 +184,20 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigItem const* __re
     int lda;
     if (SMEM_A) { A = sp; lda = np + 1; sp += (size_t)np * lda; }
     else { A = scratch + it.s_off; lda = n; }
-    double* V;
-    if (SMEM_V) { V = sp; sp += (size_t)n * n; }
-    else { V = scratch + it.s_off + (size_t)n * n; }
+    double* V = nullptr;
+    if (!logv) {
+        if (SMEM_V) { V = sp; sp += (size_t)n * n; }
+        else { V = scratch + it.s_off + (size_t)n * n; }
+    }
     int* pq = reinterpret_cast<int*>(sp);
     int* rank = pq + 2 * half;
-    // load A, V = I, Frobenius norm
+    // load A (and V = I), Frobenius norm
     double loc = 0;
     for (int e = tid; e < n * n; e += blockDim.x) {
         const int i = e % n, j = e / n;
         const double x = src[it.a_off + e];
         A[(size_t)j * lda + i] = x;
-        V[e] = (i == j) ? 1.0 : 0.0;
+        if (V) V[e] = (i == j) ? 1.0 : 0.0;
         loc = fma(x, x, loc);
     }
     for (int o = 16; o; o >>= 1) loc += __shfl_down_sync(0xffffffffu, loc, o);
@@ -183,8 +207,11 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigItem const* __re
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) norm2 += red[w];
     const double normA = sqrt(norm2);
     __syncthreads();
-    bool converged = (n <= 1);
-    if (!converged) converged = jacobi_run(A, lda, V, n, n, np, 1e-17 * normA, JacobiShared{cst, pq, &rotated});
+    bool converged = true;
+    int nsw = 0;
+    if (n > 1)
+        nsw = jacobi_run(A, lda, V, n, logv ? rlog + it.r_off : nullptr, n, np, 0x1p-52 * normA,
+                         JacobiShared{cst, pq, &rotated}, &converged);
     // eigenvalues descending (ties by position); eigenvector columns follow
     for (int i = tid; i < n; i += blockDim.x) {
         const double di = A[(size_t)i * lda + i];
@@ -195,12 +222,16 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigItem const* __re
         }
         wout[it.w_off + r] = di;
         rank[i] = r;
+        if (logv) ranks[it.w_off + i] = r;
     }
     __syncthreads();
-    for (int e = tid; e < n * n; e += blockDim.x) {
-        const int col = e / n, row = e % n;
-        vout[it.v_off + (size_t)rank[col] * n + row] = V[e];
+    if (V) {
+        for (int e = tid; e < n * n; e += blockDim.x) {
+            const int col = e / n, row = e % n;
+            vout[it.v_off + (size_t)rank[col] * n + row] = V[e];
+        }
     }
+    if (tid == 0) sweeps_out[blockIdx.x] = nsw;
     if (!converged) {
         // sweep cap reached: accept when the remaining coupling is negligible
         double mx = 0;
@@ -222,8 +253,56 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigItem const* __re
     }
 }
 
+// Rows [row0, row0 + rows) of one block's eigenvector matrix: V = I, then
+// every logged rotation in order (column pairs of a round are disjoint, so a
+// round is one parallel step), then written to vout in eigenvalue order.
+struct VJob {
+    int64_t v_off, r_off, w_off;
+    int32_t n, row0, rows, blk;
+};
+
+__global__ void __launch_bounds__(EIG_THREADS) vapply_kernel(VJob const* __restrict__ jobs, double2 const* __restrict__ rlog,
+                                                             int const* __restrict__ ranks, int const* __restrict__ sweeps,
+                                                             double* __restrict__ vout) {
+    extern __shared__ __align__(16) unsigned char va_smem[];
+    double* vr = reinterpret_cast<double*>(va_smem);  // rows x n, row-major
+    const VJob j = jobs[blockIdx.x];
+    const int n = j.n, np = n + (n & 1), half = np / 2, R = j.rows;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int e = tid; e < R * n; e += nt) {
+        const int r = e / n, col = e % n;
+        vr[e] = (j.row0 + r == col) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    const int nsw = sweeps[j.blk];
+    for (int sw = 0; sw < nsw; ++sw) {
+        for (int rd = 0; rd < np - 1; ++rd) {
+            const double2* lg = rlog + j.r_off + ((size_t)sw * (np - 1) + rd) * half;
+            for (int e = tid; e < R * half; e += nt) {
+                const int rr = e / half, k = e % half;
+                const double2 cs = lg[k];
+                if (cs.y == 0.0) continue;
+                int p, q;
+                round_pair(rd, k, np, p, q);
+                if (q >= n) continue;
+                double* row = vr + (size_t)rr * n;
+                const double a = row[p], b = row[q];
+                row[p] = cs.x * a - cs.y * b;
+                row[q] = cs.y * a + cs.x * b;
+            }
+            __syncthreads();
+        }
+    }
+    for (int e = tid; e < R * n; e += nt) {
+        const int r = e / n, col = e % n;
+        vout[j.v_off + (size_t)ranks[j.w_off + col] * n + j.row0 + r] = vr[e];
+    }
+}
+
 namespace {
 constexpr size_t EIG_SMEM_LIMIT = 227 * 1024;
+constexpr size_t EIG_LOG_LIMIT = size_t(512) << 20;   // bytes of rotation log per launch
+constexpr int EIG_LOG_MIN_N = 32;                     // smaller blocks accumulate V in the CTA
 
 size_t eig_smem_bytes(int n, bool sa, bool sv) {
     const int np = n + (n & 1), half = np / 2;
@@ -235,11 +314,12 @@ size_t eig_smem_bytes(int n, bool sa, bool sv) {
 }
 
 template <bool SA, bool SV>
-void launch_eig(Ctx& ctx, int nitems, size_t smem, EigItem const* d_items, double const* src, double* vout, double* wout,
-                double* scratch, int* d_stat) {
+void launch_eig(Ctx& ctx, int njobs, size_t smem, EigJob const* d_jobs, double const* src, double* vout, double* wout,
+                double* scratch, double2* rlog, int* ranks, int* sweeps, int* d_stat) {
     if (smem > 48 * 1024)
         ITG_CHECK_CUDA(cudaFuncSetAttribute(jacobi_kernel<SA, SV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    jacobi_kernel<SA, SV><<<nitems, EIG_THREADS, smem, ctx.stream>>>(d_items, src, vout, wout, scratch, d_stat);
+    jacobi_kernel<SA, SV><<<njobs, EIG_THREADS, smem, ctx.stream>>>(d_jobs, src, vout, wout, scratch, rlog, ranks, sweeps,
+                                                                    d_stat);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
@@ -248,27 +328,78 @@ void launch_eig(Ctx& ctx, int nitems, size_t smem, EigItem const* d_items, doubl
 int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
                  double* scratch) {
     if (items.empty()) return 0;
+    const int nb = (int)items.size();
     int nmax = 0;
-    for (auto const& it : items) nmax = std::max(nmax, it.n);
+    int64_t ntot = 0;
+    size_t log_elems = 0;
+    for (auto const& it : items) {
+        nmax = std::max(nmax, it.n);
+        ntot += it.n;
+        const int np = it.n + (it.n & 1);
+        log_elems += (size_t)EIG_MAX_SWEEPS * std::max(np - 1, 0) * (np / 2);
+    }
+    const bool logv = nmax >= EIG_LOG_MIN_N && log_elems * sizeof(double2) <= EIG_LOG_LIMIT;
+    // device jobs; eigenvector rows split so that the rotation pass spreads over the SMs
+    std::vector<EigJob> jobs(nb);
+    std::vector<VJob> vjobs;
+    int rows = 16;
+    if (logv) {
+        while (rows > 1) {
+            int64_t cnt = 0;
+            for (auto const& it : items) cnt += (it.n + rows - 1) / rows;
+            if (cnt >= 2 * (int64_t)ctx.sm_count && (size_t)rows * nmax * sizeof(double) <= EIG_SMEM_LIMIT) break;
+            rows /= 2;
+        }
+        while (rows > 1 && (size_t)rows * nmax * sizeof(double) > EIG_SMEM_LIMIT) rows /= 2;
+    }
+    size_t roff = 0;
+    for (int b = 0; b < nb; ++b) {
+        auto const& it = items[b];
+        const int np = it.n + (it.n & 1);
+        jobs[b] = EigJob{it.a_off, it.v_off, it.w_off, it.s_off, logv ? (int64_t)roff : -1, it.n, 0};
+        if (logv) {
+            for (int r0 = 0; r0 < it.n; r0 += rows)
+                vjobs.push_back(VJob{it.v_off, (int64_t)roff, it.w_off, it.n, r0, std::min(rows, it.n - r0), b});
+            roff += (size_t)EIG_MAX_SWEEPS * std::max(np - 1, 0) * (np / 2);
+        }
+    }
     const bool sa = eig_smem_bytes(nmax, true, false) <= EIG_SMEM_LIMIT;
-    const bool sv = sa && eig_smem_bytes(nmax, true, true) <= EIG_SMEM_LIMIT;
+    const bool sv = !logv && sa && eig_smem_bytes(nmax, true, true) <= EIG_SMEM_LIMIT;
     const size_t smem = eig_smem_bytes(nmax, sa, sv);
-    size_t o_items = 0, o_stat = ((sizeof(EigItem) * items.size() + 15) / 16) * 16;
-    DevBuf buf(o_stat + sizeof(int) * items.size(), ctx.stream);
-    ctx.ensure_stage(sizeof(EigItem) * items.size());
-    std::memcpy(ctx.stage, items.data(), sizeof(EigItem) * items.size());
-    ITG_CHECK_CUDA(cudaMemcpyAsync(buf.as<char>() + o_items, ctx.stage, sizeof(EigItem) * items.size(),
-                                   cudaMemcpyHostToDevice, ctx.stream));
-    EigItem const* d_items = reinterpret_cast<EigItem const*>(buf.as<char>() + o_items);
-    int* d_stat = reinterpret_cast<int*>(buf.as<char>() + o_stat);
-    const int ni = (int)items.size();
-    if (sa && sv) launch_eig<true, true>(ctx, ni, smem, d_items, src, vout, wout, scratch, d_stat);
-    else if (sa) launch_eig<true, false>(ctx, ni, smem, d_items, src, vout, wout, scratch, d_stat);
-    else launch_eig<false, false>(ctx, ni, smem, d_items, src, vout, wout, scratch, d_stat);
-    std::vector<int> st(items.size());
-    ctx.d2h(st.data(), d_stat, sizeof(int) * items.size());
+    // one upload: jobs | vjobs; one device buffer: records | status | sweeps | ranks | log
+    auto a16 = [](size_t x) { return (x + 15) / 16 * 16; };
+    const size_t o_jobs = 0, o_vj = a16(sizeof(EigJob) * nb), up = a16(o_vj + sizeof(VJob) * vjobs.size());
+    const size_t o_stat = up, o_sw = a16(o_stat + sizeof(int) * nb), o_rank = a16(o_sw + sizeof(int) * nb);
+    const size_t o_log = a16(o_rank + sizeof(int) * (size_t)ntot);
+    const size_t total = o_log + (logv ? sizeof(double2) * log_elems : 0);
+    DevBuf buf(total, ctx.stream);
+    ctx.ensure_stage(up);
+    char* st = static_cast<char*>(ctx.stage);
+    std::memcpy(st + o_jobs, jobs.data(), sizeof(EigJob) * nb);
+    if (!vjobs.empty()) std::memcpy(st + o_vj, vjobs.data(), sizeof(VJob) * vjobs.size());
+    ITG_CHECK_CUDA(cudaMemcpyAsync(buf.p, ctx.stage, up, cudaMemcpyHostToDevice, ctx.stream));
+    char* db = buf.as<char>();
+    int* d_stat = reinterpret_cast<int*>(db + o_stat);
+    int* d_sw = reinterpret_cast<int*>(db + o_sw);
+    int* d_rank = reinterpret_cast<int*>(db + o_rank);
+    double2* d_log = logv ? reinterpret_cast<double2*>(db + o_log) : nullptr;
+    EigJob const* d_jobs = reinterpret_cast<EigJob const*>(db + o_jobs);
+    if (sa && sv) launch_eig<true, true>(ctx, nb, smem, d_jobs, src, vout, wout, scratch, d_log, d_rank, d_sw, d_stat);
+    else if (sa) launch_eig<true, false>(ctx, nb, smem, d_jobs, src, vout, wout, scratch, d_log, d_rank, d_sw, d_stat);
+    else launch_eig<false, false>(ctx, nb, smem, d_jobs, src, vout, wout, scratch, d_log, d_rank, d_sw, d_stat);
+    if (logv && !vjobs.empty()) {
+        const size_t vsm = sizeof(double) * (size_t)rows * nmax;
+        if (vsm > 48 * 1024)
+            ITG_CHECK_CUDA(cudaFuncSetAttribute(vapply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsm));
+        vapply_kernel<<<(int)vjobs.size(), EIG_THREADS, vsm, ctx.stream>>>(
+            reinterpret_cast<VJob const*>(db + o_vj), d_log, d_rank, d_sw, vout);
+        ITG_CHECK_CUDA(cudaGetLastError());
+        ctx.kernel_launches++;
+    }
+    std::vector<int> stv(nb);
+    ctx.d2h(stv.data(), d_stat, sizeof(int) * nb);
     int bad = 0;
-    for (int s : st) bad += s;
+    for (int s : stv) bad += s;
     return bad;
 }
 

@@ -145,6 +145,7 @@ struct Ctx {
     double flops_done = 0;
     int precision = PREC_F64;
     int ozaki_slices = 6;
+    int gemm_variant = -1;           // split-precision GEMM variant override (-1: autotuned per plan)
     int sm_count = 152;
 
     explicit Ctx(int dev);

@@ -98,7 +98,8 @@ void HeffProgram::launch_steps(Ctx& ctx) {
                 pr.nitems = p.nitems;
             }
             // first run (never inside a graph capture): pick the GEMM tile shape on this data
-            if (!st.operand_sliced && p.oz_variant.load(std::memory_order_relaxed) < 0 && p.flops >= AUTOTUNE_MIN_FLOPS)
+            if (!st.operand_sliced && ctx.gemm_variant < 0 && p.oz_variant.load(std::memory_order_relaxed) < 0 &&
+                p.flops >= AUTOTUNE_MIN_FLOPS)
                 autotune_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps);
             launch_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps, !st.operand_sliced);
             if (ctx.profiling) {

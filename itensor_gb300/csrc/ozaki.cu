@@ -3,14 +3,17 @@
 //
 // Every operand block is seen as a rows x K matrix (A: rows = m, B: rows = n).
 // Each row gets a power-of-two scale e with |x| < 2^e, and each entry becomes
-// the fixed-point integer X = floor(|x| 2^(7S - e)) cut into S digits of 7
-// bits (sign applied): integers in [-127, 127], exact in BF16. Digit products
-// are exact in FP32 and so are their sums while |sum| < 2^24. Digit pairs
-// (s,t) with s+t < S are accumulated per diagonal D = s+t with mma.sync
-// m16n8k16 (FP32 accumulate), folded exactly into one int64 per output
-// (sum_D acc_D 2^(7(S-1-D))) every KCHUNK k (a diagonal holds at most S
-// digit products of |d| <= 127 per k, so KCHUNK * S * 127^2 <= 2^24 keeps every
-// partial sum an exact FP32 integer: 128 k for S = 5, 6; 256 for S <= 4), and scaled into the FP64 output once
+// the signed fixed-point integer X = round(x 2^(7S - e)) cut into S balanced
+// base-128 digits: d_1..d_{S-1} in [-64, 63], d_0 in [-128, 128], all exact
+// in BF16. Balanced digits carry signs independent of the entry's sign, so
+// the digit products left out below average to zero rather than shrinking
+// every product. Digit products are exact in FP32 and so are their sums while
+// |sum| < 2^24. Digit pairs (s,t) with s+t < S are accumulated per diagonal
+// D = s+t with mma.sync m16n8k16 (FP32 accumulate), folded exactly into one
+// int64 per output (sum_D acc_D 2^(7(S-1-D))) every KCHUNK k (a diagonal holds
+// at most S digit products of |d| <= 128 per k, so KCHUNK * S * 128^2 <= 2^24
+// keeps every partial sum an exact FP32 integer: 128 k for S = 5, 6; 256 for
+// S <= 4), and scaled into the FP64 output once
 // per block pair (one fold is below 2^57 in magnitude, so the int64 sum of a
 // pair cannot overflow while the pair's K <= 64 * KCHUNK; plans with a longer
 // pair run the FP64 kernel, see plan_uses_split). Accuracy ~2^(-7S)
@@ -69,15 +72,26 @@ __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restr
         if (ef != 0) {
             unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
             int sh = ef - 1075 + 7 * S - (rexp[r] - 1022);  // <= 7S - 53 < 0 for S <= 7
-            if (sh > -64) Xf = sh >= 0 ? (mant << sh) : (mant >> (-sh));
+            // rounded to nearest, not truncated: truncation shrinks every entry's
+            // magnitude and the bias adds up coherently in the products
+            if (sh >= 0) Xf = mant << sh;
+            else if (sh > -64) Xf = (mant >> (-sh)) + ((mant >> (-sh - 1)) & 1ull);
         }
-        const bool neg = bits < 0;
+        // balanced digits: d_1..d_{S-1} in [-64, 63], d_0 in [-128, 128] (BF16-exact).
+        // Their signs are independent of the entry's sign, so the digit products
+        // left out (s + t >= S) average to zero instead of always shrinking |x y|.
+        long long X = bits < 0 ? -(long long)Xf : (long long)Xf;
+        int dig[S];
+#pragma unroll
+        for (int s = S - 1; s >= 1; --s) {
+            const long long d = ((X + 64) & 127) - 64;
+            dig[s] = (int)d;
+            X = (X - d) >> 7;
+        }
+        dig[0] = (int)X;
         __nv_bfloat16* dst = pan + e;
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-            int d = (int)((Xf >> (7 * (S - 1 - s))) & 127ull);
-            dst[s * plane] = __float2bfloat16_rn((float)(neg ? -d : d));
-        }
+        for (int s = 0; s < S; ++s) dst[s * plane] = __float2bfloat16_rn((float)dig[s]);
     }
 }
 
@@ -134,7 +148,7 @@ __device__ __forceinline__ void oz_tile(ItemRec const& it, const PairRec* __rest
     constexpr int TM = 16 * WM, TN = 32, TK = 16, LD = TK + 8;  // row stride 48 B: 16-B aligned, no ldmatrix conflicts
     constexpr int NT = 64 * WM;
     constexpr int KCHUNK = (S <= 4) ? 256 : 128;
-    static_assert((long long)KCHUNK * S * 127 * 127 <= (1LL << 24), "digit sums must stay exact in FP32");
+    static_assert((long long)KCHUNK * S * 128 * 128 <= (1LL << 24), "digit sums must stay exact in FP32");
     typedef __nv_bfloat16 TileA[S][TM][LD];
     typedef __nv_bfloat16 TileB[S][TN][LD];
     TileA* As = reinterpret_cast<TileA*>(smem);                      // [2]
@@ -338,7 +352,7 @@ void launch_s(Ctx& ctx, Plan const& p, double const* A, double const* B, double*
 void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S,
                   __nv_bfloat16* panels, int32_t* exps, bool prep_b) {
     const int64_t plane = (p.panel_elems + 15) / 16 * 16;
-    const int v = std::max(0, p.oz_variant.load(std::memory_order_relaxed));
+    const int v = ctx.gemm_variant >= 0 ? ctx.gemm_variant : std::max(0, p.oz_variant.load(std::memory_order_relaxed));
     switch (S) {
         case 3: launch_s<3>(ctx, p, A, B, C, panels, plane, exps, prep_b, v); break;
         case 4: launch_s<4>(ctx, p, A, B, C, panels, plane, exps, prep_b, v); break;

@@ -29,8 +29,9 @@ int64_t solve_footprint_estimate(ModelSpec const& m, std::vector<SweepSpec> cons
         const double phi = ml * d * d * mr;
         const double fused = std::max(ml, mr) * d;
         // Davidson: V and H V for every iteration; H_eff intermediates (two of D x phi);
-        // bond split: combined copy, density matrix and eigenvectors (or U, V)
-        double w = phi * (2.0 * (niter + 2) + 2.0 * D + 3.0) + 3.0 * fused * fused;
+        // bond split: combined copy, density matrix and eigenvectors (or U, V), and
+        // the eigensolver's rotation log (30 sweeps x n^2/2 rotations x 16 B per block)
+        double w = phi * (2.0 * (niter + 2) + 2.0 * D + 3.0) + 3.0 * fused * fused + 30.0 * fused * fused;
         if (prec == PREC_OZAKI_BF16) w += (2.0 * S / 8.0) * (2.0 * phi + 2.0 * ml * D * ml + 2.0 * mr * D * mr);
         work = std::max(work, w);
     }
