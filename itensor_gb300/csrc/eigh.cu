@@ -26,6 +26,8 @@
 // converged when its largest off-diagonal entry is below 1e-13 ||A||_F.
 #include "ops.h"
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 namespace itg {
@@ -400,6 +402,13 @@ int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src,
     ctx.d2h(stv.data(), d_stat, sizeof(int) * nb);
     int bad = 0;
     for (int s : stv) bad += s;
+    if (std::getenv("ITG_EIG_LOG")) {
+        std::vector<int> swv(nb);
+        ctx.d2h(swv.data(), d_sw, sizeof(int) * nb);
+        std::fprintf(stderr, "itg eigh:");
+        for (int b = 0; b < nb; ++b) std::fprintf(stderr, " %d/%d", items[b].n, swv[b]);
+        std::fprintf(stderr, "\n");
+    }
     return bad;
 }
 
