@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <unordered_set>
 
 namespace itg {
 
@@ -415,25 +416,24 @@ static void launch_skinny(Ctx& ctx, Plan const& p, double const* A, double const
 
 // ------------------------------------------------------------------ host side
 namespace {
-std::mutex g_streams_mu;
-std::vector<cudaStream_t>& live_streams() {
-    static std::vector<cudaStream_t> v;
+// every buffer free asks whether its stream is alive: many readers, rare writers
+std::shared_mutex g_streams_mu;
+std::unordered_set<cudaStream_t>& live_streams() {
+    static std::unordered_set<cudaStream_t> v;
     return v;
 }
 }  // namespace
 void stream_register(cudaStream_t s) {
-    std::lock_guard<std::mutex> g(g_streams_mu);
-    live_streams().push_back(s);
+    std::unique_lock<std::shared_mutex> g(g_streams_mu);
+    live_streams().insert(s);
 }
 void stream_unregister(cudaStream_t s) {
-    std::lock_guard<std::mutex> g(g_streams_mu);
-    auto& v = live_streams();
-    v.erase(std::remove(v.begin(), v.end(), s), v.end());
+    std::unique_lock<std::shared_mutex> g(g_streams_mu);
+    live_streams().erase(s);
 }
 bool stream_alive(cudaStream_t s) {
-    std::lock_guard<std::mutex> g(g_streams_mu);
-    auto& v = live_streams();
-    return std::find(v.begin(), v.end(), s) != v.end();
+    std::shared_lock<std::shared_mutex> g(g_streams_mu);
+    return live_streams().count(s) != 0;
 }
 
 Ctx::Ctx(int dev) : device(dev) {

@@ -15,6 +15,7 @@
 #include "tensor.h"
 #include <atomic>
 #include <mutex>
+#include <shared_mutex>
 
 namespace itg {
 
@@ -87,25 +88,25 @@ struct Plan {
 // builds are not (two contexts may build the same plan; the second insert is
 // dropped). A plan's tables are immutable once inserted.
 struct PlanCache {
-    std::mutex mu;
+    std::shared_mutex mu;   // lookups (the common case) share the lock
     std::unordered_map<std::string, std::shared_ptr<Plan>> map;
-    size_t limit = 4096;
+    size_t limit = 16384;
     std::shared_ptr<Plan> find(std::string const& key) {
-        std::lock_guard<std::mutex> g(mu);
+        std::shared_lock<std::shared_mutex> g(mu);
         auto it = map.find(key);
         return it == map.end() ? nullptr : it->second;
     }
     std::shared_ptr<Plan> insert(std::string key, std::shared_ptr<Plan> p) {
-        std::lock_guard<std::mutex> g(mu);
+        std::unique_lock<std::shared_mutex> g(mu);
         if (map.size() >= limit) map.clear();
         return map.emplace(std::move(key), std::move(p)).first->second;
     }
     size_t size() {
-        std::lock_guard<std::mutex> g(mu);
+        std::shared_lock<std::shared_mutex> g(mu);
         return map.size();
     }
     void clear() {
-        std::lock_guard<std::mutex> g(mu);
+        std::unique_lock<std::shared_mutex> g(mu);
         map.clear();
     }
 };
