@@ -393,6 +393,20 @@ def bench_serving(n_req, budget_bytes, load=0.8):
             "pool": {"workers": workers, "slots_per_worker": slots}}
 
 
+def run_profile_dmrg(args):
+    """One DMRG solve for ncu's launch list: J1-J2 chain N=48, J2=0.3, three
+    sweeps with maxdim 64, 128, 256, cutoff 1e-10, niter 2, split precision."""
+    import itensor_gb300 as itg
+    ctx = itg.Context(0)
+    sw = [dict(maxdim=m, mindim=1, cutoff=1e-10, niter=2) for m in (64, 128, 256)]
+    t0 = time.perf_counter()
+    r = ctx.dmrg(dict(type=0, N=48, J=1.0, Jz=1.0, J2=0.3), sw, precision=itg.PREC_OZAKI_BF16)
+    print(json.dumps({"energy": r.energy, "bond_steps": len(r.bonds), "seconds": time.perf_counter() - t0,
+                      "phase_seconds": r.phase_seconds, "stats": ctx.stats()}))
+    ctx.close()
+    return 0
+
+
 def run_profile(args):
     """Short run of the same workload for ncu: for the split form and plain
     FP64, N prepared applies each (kernels launched one by one)."""
@@ -426,6 +440,8 @@ def main():
     ap.add_argument("--chains", type=int, default=256, help="independent chains of the batched form (0: skip)")
     ap.add_argument("--seq-chains", type=int, default=16, help="chains solved one by one by the plain FP64 path")
     ap.add_argument("--requests", type=int, default=96, help="requests per serving pass (0: skip)")
+    ap.add_argument("--profile-dmrg", action="store_true",
+                    help="profiling run for ncu: one J1-J2 chain N=48, J2=0.3, maxdim 64/128/256, split precision")
     ap.add_argument("--profile", type=int, default=0,
                     help="profiling run for ncu: N prepared applies per arithmetic, no graph, no timing")
     args = ap.parse_args()
@@ -433,6 +449,8 @@ def main():
         return run_reference(args)
     if args.profile:
         return run_profile(args)
+    if args.profile_dmrg:
+        return run_profile_dmrg(args)
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
 
@@ -537,6 +555,15 @@ def main():
                         "product" % ("MEASURED_PEAKS.json" if peak_src == "measured" else "the fallback",
                                      peak_src, nsl),
                 "digit_product_tflops": achieved * nsl, "digit_product_frac": achieved * nsl / peaks["bf16_tflops"]}
+    # the kernel issues mma.sync (not tcgen05): its own pipe's measured rate, from the issue-rate microbenchmark
+    try:
+        own = ctx.measure_peaks()
+        roofline["mma_sync_bf16_tflops_measured"] = own["bf16_mma_sync"]
+        roofline["digit_product_frac_of_mma_sync"] = achieved * nsl / own["bf16_mma_sync"]
+        roofline["fp64_ffma_tflops_measured"] = own["fp64_ffma"]
+    except Exception as e:  # the microbenchmark is context only; the line stands without it
+        roofline["mma_sync_bf16_tflops_measured"] = None
+        roofline["peaks_error"] = str(e)[:200]
     d64_ms, d64_flops, _ = dom_stats(prof_64)
 
     # end-to-end through the C-ABI with host buffers: psi host -> device, apply, result -> host

@@ -970,7 +970,8 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
         const int64_t plane = (p.panel_elems + 15) / 16 * 16;
         __nv_bfloat16* panels = static_cast<__nv_bfloat16*>(ctx.split_buffer(split_scratch_bytes(p, S)));
         int32_t* exps = reinterpret_cast<int32_t*>(panels + plane * S);
-        if (ctx.gemm_variant < 0 && p.oz_variant.load(std::memory_order_relaxed) < 0 && p.flops >= AUTOTUNE_MIN_FLOPS)
+        if (ctx.gemm_variant < 0 && p.oz_variant.load(std::memory_order_relaxed) < 0 && p.flops >= AUTOTUNE_MIN_FLOPS &&
+            p.split_uses.fetch_add(1, std::memory_order_relaxed) + 1 >= AUTOTUNE_MIN_USES)
             autotune_ozaki(ctx, p, A, B, C, S, panels, exps);
         launch_ozaki(ctx, p, A, B, C, S, panels, exps);
         ctx.kernel_launches += 1;

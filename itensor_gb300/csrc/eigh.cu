@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(EIG_THREADS) vapply_kernel(VJob const* __restr
         vr[e] = (j.row0 + r == col) ? 1.0 : 0.0;
     }
     __syncthreads();
-    const int nsw = sweeps[j.blk];
+    const int nsw = min(max(sweeps[j.blk], 0), EIG_MAX_SWEEPS);  // the log holds at most this many
     for (int sw = 0; sw < nsw; ++sw) {
         for (int rd = 0; rd < np - 1; ++rd) {
             const double2* lg = rlog + j.r_off + ((size_t)sw * (np - 1) + rd) * half;

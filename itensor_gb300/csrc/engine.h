@@ -81,6 +81,8 @@ struct Plan {
     int nitems64 = 0;
     // split-precision GEMM variant picked by the autotuner (-1: not tuned, run variant 0)
     mutable std::atomic<int> oz_variant{-1};
+    // split-precision executions so far (a plan is tuned only once it is reused)
+    mutable std::atomic<int> split_uses{0};
 };
 
 // Plans keyed by block structure. One cache may serve several contexts (the
@@ -195,8 +197,12 @@ void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, dou
 // stores the fastest in p.oz_variant (ozaki.cu); C is overwritten.
 int autotune_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S,
                    __nv_bfloat16* panels, int32_t* exps);
-// Plans with at least this many algorithmic flops are tuned on first use.
+// Plans with at least this many algorithmic flops are tuned: a prepared H_eff
+// program tunes on its first run, exec_plan once a plan has run
+// AUTOTUNE_MIN_USES times (tuning costs about sixteen executions, which a
+// plan used for one Davidson call never pays back).
 constexpr double AUTOTUNE_MIN_FLOPS = 2e7;
+constexpr int AUTOTUNE_MIN_USES = 32;
 // Whether exec_plan runs this plan with the split-precision kernels.
 // (The int64 digit sums of one block pair are exact up to K = 8192.)
 constexpr int SPLIT_MAX_PAIR_K = 8192;

@@ -98,8 +98,10 @@ void HeffProgram::launch_steps(Ctx& ctx) {
                 pr.nitems = p.nitems;
             }
             // first run (never inside a graph capture): pick the GEMM tile shape on this data
+            // (a graph-replayed program is built to be run many times; otherwise the plan must be reused first)
             if (!st.operand_sliced && ctx.gemm_variant < 0 && p.oz_variant.load(std::memory_order_relaxed) < 0 &&
-                p.flops >= AUTOTUNE_MIN_FLOPS)
+                p.flops >= AUTOTUNE_MIN_FLOPS &&
+                (use_graph || p.split_uses.fetch_add(1, std::memory_order_relaxed) + 1 >= AUTOTUNE_MIN_USES))
                 autotune_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps);
             launch_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps, !st.operand_sliced);
             if (ctx.profiling) {
