@@ -6,7 +6,9 @@
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
@@ -73,6 +75,40 @@ struct MemAccount {
 // Account charged by the calling thread's allocations (empty: none).
 std::shared_ptr<MemAccount>& current_account();
 
+// Blocks a solve has freed on its stream, kept for its next allocations on
+// that stream: reuse in stream order needs no synchronisation, and the solver
+// pool's many threads then make far fewer allocator calls (which serialise
+// on the driver). Blocks are reused for requests of half their size or more;
+// the cache holds at most `limit` bytes and is emptied when the solve ends.
+struct BlockCache {
+    std::mutex mu;
+    cudaStream_t stream = nullptr;
+    std::multimap<size_t, void*> free;
+    size_t held = 0, limit = size_t(1) << 30;
+    explicit BlockCache(cudaStream_t s) : stream(s) {}
+    void* take(size_t n, size_t* got) {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = free.lower_bound(n);
+        if (it == free.end() || it->first > 2 * n) return nullptr;
+        void* p = it->second;
+        *got = it->first;
+        held -= it->first;
+        free.erase(it);
+        return p;
+    }
+    bool put(void* p, size_t n) {
+        std::lock_guard<std::mutex> g(mu);
+        if (held + n > limit) return false;
+        free.emplace(n, p);
+        held += n;
+        return true;
+    }
+    void release();  // frees every cached block (on the stream while it lives)
+    ~BlockCache() { release(); }
+};
+// Cache serving the calling thread's allocations (empty: none).
+std::shared_ptr<BlockCache>& current_cache();
+
 // Device buffer from the stream-ordered pool (cudaMallocAsync). Freed on the
 // stream it was allocated on, so reuse is ordered after every prior use.
 struct DevBuf {
@@ -80,17 +116,26 @@ struct DevBuf {
     size_t bytes = 0;
     cudaStream_t stream = nullptr;
     std::shared_ptr<MemAccount> acct;
+    std::shared_ptr<BlockCache> cache;
     DevBuf() = default;
     DevBuf(size_t n, cudaStream_t s) : bytes(n), stream(s) {
         if (n) {
-            ITG_CHECK_CUDA(cudaMallocAsync(&p, n, s));
+            auto const& c = current_cache();
+            if (c && c->stream == s) {
+                cache = c;
+                size_t got = 0;
+                if ((p = c->take(n, &got))) bytes = got;
+            }
+            if (!p) ITG_CHECK_CUDA(cudaMallocAsync(&p, n, s));
             acct = current_account();
-            if (acct) acct->add((int64_t)n);
+            if (acct) acct->add((int64_t)bytes);
         }
     }
     ~DevBuf() {
         if (!p) return;
         if (acct) acct->sub((int64_t)bytes);
+        // (a cache frees its blocks itself, checking its stream then)
+        if (cache && cache->put(p, bytes)) return;
         if (stream_alive(stream)) cudaFreeAsync(p, stream);
         else cudaFree(p);
     }

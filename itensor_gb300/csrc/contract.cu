@@ -374,6 +374,79 @@ __device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& 
     }
 }
 
+// Barrier-free form for plans whose pairs all have K <= SKINNY_K: every thread
+// reads the (tiny, L1-resident) B entries itself, the same addresses across
+// the CTA, instead of staging each pair's block behind two barriers. Same FMA
+// order per output as skinny_item.
+template <int NN, int R>
+__device__ __forceinline__ void skinny_item_direct(ItemRec const& it, CBlockRec const& cb,
+                                                   const PairRec* __restrict__ pairs, const int32_t* __restrict__ tab,
+                                                   const double* __restrict__ A, const double* __restrict__ B,
+                                                   double* __restrict__ C) {
+    double acc[R][NN];
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+#pragma unroll
+        for (int n = 0; n < NN; ++n) acc[j][n] = 0.0;
+    int mrow[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) mrow[j] = it.m0 + threadIdx.x + j * SKINNY_THREADS;
+    int bcol[NN];
+    for (int p = it.p0; p < it.p1; ++p) {
+        const PairRec pr = pairs[p];
+        int arow[R];
+#pragma unroll
+        for (int j = 0; j < R; ++j) arow[j] = mrow[j] < cb.M ? tab[pr.tam + mrow[j]] : -1;
+#pragma unroll
+        for (int n = 0; n < NN; ++n) bcol[n] = tab[pr.tbn + n];
+        for (int k = 0; k < pr.K; ++k) {
+            const int ko = tab[pr.tak + k];
+            const int64_t bk = pr.boff + tab[pr.tbk + k];
+            double a[R];
+#pragma unroll
+            for (int j = 0; j < R; ++j) a[j] = arow[j] >= 0 ? A[pr.aoff + arow[j] + ko] : 0.0;
+#pragma unroll
+            for (int n = 0; n < NN; ++n) {
+                const double b = __ldg(B + bk + bcol[n]);
+                if (b != 0.0) {
+#pragma unroll
+                    for (int j = 0; j < R; ++j) acc[j][n] = fma(a[j], b, acc[j][n]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        if (mrow[j] < cb.M) {
+            const int64_t crow = cb.coff + tab[cb.tcm + mrow[j]];
+#pragma unroll
+            for (int n = 0; n < NN; ++n) C[crow + tab[cb.tcn + n]] = acc[j][n];
+        }
+    }
+}
+
+template <int R>
+__global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_direct_kernel(const ItemRec* __restrict__ items,
+                                                                                const PairRec* __restrict__ pairs,
+                                                                                const CBlockRec* __restrict__ cblk,
+                                                                                const int32_t* __restrict__ tab,
+                                                                                const double* __restrict__ A,
+                                                                                const double* __restrict__ B,
+                                                                                double* __restrict__ C) {
+    const ItemRec it = items[blockIdx.x];
+    const CBlockRec cb = cblk[it.c];
+    switch (cb.N) {
+        case 1: skinny_item_direct<1, R>(it, cb, pairs, tab, A, B, C); break;
+        case 2: skinny_item_direct<2, R>(it, cb, pairs, tab, A, B, C); break;
+        case 3: skinny_item_direct<3, R>(it, cb, pairs, tab, A, B, C); break;
+        case 4: skinny_item_direct<4, R>(it, cb, pairs, tab, A, B, C); break;
+        case 5: skinny_item_direct<5, R>(it, cb, pairs, tab, A, B, C); break;
+        case 6: skinny_item_direct<6, R>(it, cb, pairs, tab, A, B, C); break;
+        case 7: skinny_item_direct<7, R>(it, cb, pairs, tab, A, B, C); break;
+        default: skinny_item_direct<8, R>(it, cb, pairs, tab, A, B, C); break;
+    }
+}
+
 template <int R>
 __global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_kernel(const ItemRec* __restrict__ items,
                                                                          const PairRec* __restrict__ pairs,
@@ -399,6 +472,23 @@ __global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_kernel(const I
 
 // Launches the skinny kernel with the plan's rows per thread.
 static void launch_skinny(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C) {
+    if (p.max_pair_K <= SKINNY_K) {
+        switch (p.skinny_r) {
+            case 1:
+                gemm_f64_skinny_direct_kernel<1><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk,
+                                                                                               p.d_tab, A, B, C);
+                break;
+            case 2:
+                gemm_f64_skinny_direct_kernel<2><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk,
+                                                                                               p.d_tab, A, B, C);
+                break;
+            default:
+                gemm_f64_skinny_direct_kernel<4><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk,
+                                                                                               p.d_tab, A, B, C);
+                break;
+        }
+        return;
+    }
     switch (p.skinny_r) {
         case 1:
             gemm_f64_skinny_kernel<1><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
@@ -501,6 +591,22 @@ void* Ctx::split_buffer(size_t bytes) {
 std::shared_ptr<MemAccount>& current_account() {
     thread_local std::shared_ptr<MemAccount> acct;
     return acct;
+}
+
+std::shared_ptr<BlockCache>& current_cache() {
+    thread_local std::shared_ptr<BlockCache> cache;
+    return cache;
+}
+
+void BlockCache::release() {
+    std::lock_guard<std::mutex> g(mu);
+    const bool alive = stream_alive(stream);
+    for (auto& kv : free) {
+        if (alive) cudaFreeAsync(kv.second, stream);
+        else cudaFree(kv.second);
+    }
+    free.clear();
+    held = 0;
 }
 
 void Ctx::ensure_stage(size_t bytes) {
@@ -607,10 +713,18 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
     if (auto hit = ctx.plans->find(key)) { ctx.plan_hits++; return hit; }
     // plan tables outlive the solve that builds them (the cache is shared):
     // they are not charged to its memory account
+    // (nor taken from its block cache, which is emptied when the solve ends)
     struct Uncharged {
         std::shared_ptr<MemAccount> saved;
-        Uncharged() : saved(std::move(current_account())) { current_account().reset(); }
-        ~Uncharged() { current_account() = std::move(saved); }
+        std::shared_ptr<BlockCache> saved_cache;
+        Uncharged() : saved(std::move(current_account())), saved_cache(std::move(current_cache())) {
+            current_account().reset();
+            current_cache().reset();
+        }
+        ~Uncharged() {
+            current_account() = std::move(saved);
+            current_cache() = std::move(saved_cache);
+        }
     } uncharged;
 
     const int nA = A.nblocks(), nB = B.nblocks(), rA = A.rank(), rB = B.rank();

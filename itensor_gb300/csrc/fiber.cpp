@@ -20,8 +20,10 @@ void fiber_entry() {
 void resume(FiberScheduler& s, Fiber& f) {
     s.current = &f;
     current_account() = f.live_acct;  // as the fiber left it (a section may have suspended charging)
+    current_cache() = f.live_cache;
     if (swapcontext(&s.main_uc, &f.uc) != 0) throw Error(ERR_INTERNAL, "fiber: context switch failed");
     current_account().reset();
+    current_cache().reset();
     s.current = nullptr;
 }
 }  // namespace
@@ -56,6 +58,7 @@ void FiberScheduler::start(Fiber& f, std::function<void()> fn) {
     f.wait = nullptr;
     f.wait_status = cudaSuccess;
     f.live_acct = f.acct;
+    f.live_cache = f.cache;
     resume(*this, f);
 }
 
@@ -81,6 +84,7 @@ void fiber_wait_event(cudaEvent_t ev) {
     Fiber* f = s->current;
     f->wait = ev;
     f->live_acct = current_account();
+    f->live_cache = current_cache();
     if (swapcontext(&f->uc, &s->main_uc) != 0) throw Error(ERR_INTERNAL, "fiber: context switch failed");
     // resumed by poll() once the event completed (or reported an error)
     const cudaError_t e = f->wait_status;

@@ -21,6 +21,8 @@ struct Fiber {
     cudaError_t wait_status = cudaSuccess;
     std::shared_ptr<MemAccount> acct;       // the solve's account
     std::shared_ptr<MemAccount> live_acct;  // the thread's account when the fiber last yielded
+    std::shared_ptr<BlockCache> cache;      // the solve's block cache
+    std::shared_ptr<BlockCache> live_cache; // the thread's cache when the fiber last yielded
     Fiber();
     ~Fiber();
     Fiber(Fiber const&) = delete;

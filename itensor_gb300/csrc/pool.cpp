@@ -218,6 +218,7 @@ void SolverPool::worker_main(int w) {
                     rec->worker = w;
                     rec->slot = i;
                     s.fiber.acct = std::make_shared<MemAccount>();
+                    s.fiber.cache = std::make_shared<BlockCache>(s.ctx->stream);
                     Ctx* ctx = s.ctx.get();
                     SolveRecord* r = rec.get();
                     sched.start(s.fiber, [ctx, r, this] { run_solve(*ctx, *r, *this); });
@@ -231,6 +232,10 @@ void SolverPool::worker_main(int w) {
                 finish(s.rec);
                 s.rec.reset();
                 s.fiber.acct.reset();
+                s.fiber.live_acct.reset();
+                if (s.fiber.cache) s.fiber.cache->release();  // blocks still held by the context return later
+                s.fiber.cache.reset();
+                s.fiber.live_cache.reset();
             }
             busy += s.rec ? 1 : 0;
         }
