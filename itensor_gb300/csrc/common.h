@@ -50,9 +50,15 @@ struct Error : std::runtime_error {
 // Streams of live contexts. A buffer that outlives its context (a tensor
 // handle released after itg_destroy) is freed synchronously instead of on the
 // destroyed stream.
-void stream_register(cudaStream_t s);
+struct BlockCache;
+void stream_register(cudaStream_t s, std::shared_ptr<BlockCache> cache);
 void stream_unregister(cudaStream_t s);
 bool stream_alive(cudaStream_t s);
+// The block cache of the context that owns stream s (null: none).
+std::shared_ptr<BlockCache> stream_cache(cudaStream_t s);
+// Set while allocating buffers that outlive the current solve (shared plan
+// tables): they bypass every block cache.
+bool& cache_bypass();
 
 // Cooperative solve multiplexing (fiber.cpp). A solver-pool worker thread runs
 // several solves as fibers; a fiber that must wait for its stream yields to
@@ -120,7 +126,11 @@ struct DevBuf {
     DevBuf() = default;
     DevBuf(size_t n, cudaStream_t s) : bytes(n), stream(s) {
         if (n) {
-            auto const& c = current_cache();
+            std::shared_ptr<BlockCache> c;
+            if (!cache_bypass()) {
+                c = current_cache();                // a pool solve's own cache
+                if (!c || c->stream != s) c = stream_cache(s);  // else the stream's context cache
+            }
             if (c && c->stream == s) {
                 cache = c;
                 size_t got = 0;

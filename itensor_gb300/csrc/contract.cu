@@ -506,16 +506,16 @@ static void launch_skinny(Ctx& ctx, Plan const& p, double const* A, double const
 
 // ------------------------------------------------------------------ host side
 namespace {
-// every buffer free asks whether its stream is alive: many readers, rare writers
+// live streams and their contexts' block caches: many readers, rare writers
 std::shared_mutex g_streams_mu;
-std::unordered_set<cudaStream_t>& live_streams() {
-    static std::unordered_set<cudaStream_t> v;
+std::unordered_map<cudaStream_t, std::shared_ptr<BlockCache>>& live_streams() {
+    static std::unordered_map<cudaStream_t, std::shared_ptr<BlockCache>> v;
     return v;
 }
 }  // namespace
-void stream_register(cudaStream_t s) {
+void stream_register(cudaStream_t s, std::shared_ptr<BlockCache> cache) {
     std::unique_lock<std::shared_mutex> g(g_streams_mu);
-    live_streams().insert(s);
+    live_streams()[s] = std::move(cache);
 }
 void stream_unregister(cudaStream_t s) {
     std::unique_lock<std::shared_mutex> g(g_streams_mu);
@@ -525,11 +525,21 @@ bool stream_alive(cudaStream_t s) {
     std::shared_lock<std::shared_mutex> g(g_streams_mu);
     return live_streams().count(s) != 0;
 }
+std::shared_ptr<BlockCache> stream_cache(cudaStream_t s) {
+    std::shared_lock<std::shared_mutex> g(g_streams_mu);
+    auto it = live_streams().find(s);
+    return it == live_streams().end() ? nullptr : it->second;
+}
+bool& cache_bypass() {
+    thread_local bool bypass = false;
+    return bypass;
+}
 
 Ctx::Ctx(int dev) : device(dev) {
     ITG_CHECK_CUDA(cudaSetDevice(dev));
     ITG_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    stream_register(stream);
+    cache = std::make_shared<BlockCache>(stream);
+    stream_register(stream, cache);
     int sms = 0;
     ITG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     sm_count = sms;
@@ -550,6 +560,7 @@ Ctx::~Ctx() {
     if (stage) cudaFreeHost(stage);
     if (stream) {
         stream_unregister(stream);
+        if (cache) cache->release();  // while the stream lives
         cudaStreamDestroy(stream);
     }
 }
@@ -716,14 +727,14 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
     // (nor taken from its block cache, which is emptied when the solve ends)
     struct Uncharged {
         std::shared_ptr<MemAccount> saved;
-        std::shared_ptr<BlockCache> saved_cache;
-        Uncharged() : saved(std::move(current_account())), saved_cache(std::move(current_cache())) {
+        bool saved_bypass;
+        Uncharged() : saved(std::move(current_account())), saved_bypass(cache_bypass()) {
             current_account().reset();
-            current_cache().reset();
+            cache_bypass() = true;
         }
         ~Uncharged() {
             current_account() = std::move(saved);
-            current_cache() = std::move(saved_cache);
+            cache_bypass() = saved_bypass;
         }
     } uncharged;
 

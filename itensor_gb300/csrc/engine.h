@@ -139,6 +139,8 @@ struct Ctx {
     DevBufPtr split_scratch;
     // event used by sync() when the calling thread multiplexes solves
     cudaEvent_t sync_event = nullptr;
+    // freed buffers of this stream, reused by its next allocations
+    std::shared_ptr<BlockCache> cache;
     // partial sums + completion counter of the fused reductions (ops.cu)
     DevBufPtr reduce_buf;
     void ensure_reduce();

@@ -21,9 +21,11 @@ void resume(FiberScheduler& s, Fiber& f) {
     s.current = &f;
     current_account() = f.live_acct;  // as the fiber left it (a section may have suspended charging)
     current_cache() = f.live_cache;
+    cache_bypass() = f.live_bypass;
     if (swapcontext(&s.main_uc, &f.uc) != 0) throw Error(ERR_INTERNAL, "fiber: context switch failed");
     current_account().reset();
     current_cache().reset();
+    cache_bypass() = false;
     s.current = nullptr;
 }
 }  // namespace
@@ -59,6 +61,7 @@ void FiberScheduler::start(Fiber& f, std::function<void()> fn) {
     f.wait_status = cudaSuccess;
     f.live_acct = f.acct;
     f.live_cache = f.cache;
+    f.live_bypass = false;
     resume(*this, f);
 }
 
@@ -85,6 +88,7 @@ void fiber_wait_event(cudaEvent_t ev) {
     f->wait = ev;
     f->live_acct = current_account();
     f->live_cache = current_cache();
+    f->live_bypass = cache_bypass();
     if (swapcontext(&f->uc, &s->main_uc) != 0) throw Error(ERR_INTERNAL, "fiber: context switch failed");
     // resumed by poll() once the event completed (or reported an error)
     const cudaError_t e = f->wait_status;

@@ -23,6 +23,7 @@ struct Fiber {
     std::shared_ptr<MemAccount> live_acct;  // the thread's account when the fiber last yielded
     std::shared_ptr<BlockCache> cache;      // the solve's block cache
     std::shared_ptr<BlockCache> live_cache; // the thread's cache when the fiber last yielded
+    bool live_bypass = false;               // the thread's cache bypass when the fiber last yielded
     Fiber();
     ~Fiber();
     Fiber(Fiber const&) = delete;
