@@ -218,15 +218,33 @@ def diag_hermitian(rho: BSTensor, ai: Index, maxdim=None, mindim=1, cutoff=0.0, 
     return U, dind, probs, truncerr, kept
 
 
+def swap_prime01(T: BSTensor) -> BSTensor:
+    """swapTags(T, "0", "1"): prime levels 0 and 1 exchanged, data unchanged."""
+    inds = [I.prime(1) if I.plev == 0 else (I.prime(-1) if I.plev == 1 else I) for I in T.inds]
+    return BSTensor(inds, T.blocks, T.scalar)
+
+
+def block_trace(rho: BSTensor) -> float:
+    """delta(dag(ci), prime(ci)) * rho for a 2-index QN tensor (ci, ci')."""
+    return float(sum(np.trace(b) for c, b in rho.blocks.items() if c[0] == c[1]))
+
+
 def denmat_decomp(AA: BSTensor, A: BSTensor, B: BSTensor, fromleft: bool, maxdim, mindim, cutoff,
-                  respectDegenerate=True, normalize=True):
-    """denmatDecomp (noise 0) followed by the DoNormalize step of
-    MPS::svdBond (itensor/mps/mps_impl.h:73-78). Returns (A', B', probs, truncerr)."""
+                  respectDegenerate=True, normalize=True, noise=0.0, op=None):
+    """denmatDecomp (itensor/decomp.h:316-418), with the noise term
+    rho += noise * deltaRho and the trace normalisation (decomp.h:386-394)
+    when noise > 0, followed by the DoNormalize step of MPS::svdBond
+    (itensor/mps/mps_impl.h:73-78). Returns (A', B', probs, truncerr)."""
     to_orth, newoc = (A, B) if fromleft else (B, A)
     cinds = [I for I in to_orth.inds if newoc.find(I) < 0]
     cmb = Combiner(cinds)
     AAc = combine(AA, cmb)
     rho = contract(AAc, AAc.dag().prime(which={cmb.ci.id}))
+    if noise > 0 and op is not None:
+        rho = rho + op.delta_rho(AA, cmb, fromleft).scale(noise)
+        tr = block_trace(rho)
+        if tr > 1e-16:
+            rho = rho.scale(1.0 / tr)
     U, dind, probs, te, kept = diag_hermitian(rho, cmb.ci, maxdim=maxdim, mindim=mindim, cutoff=cutoff,
                                               respectDegenerate=respectDegenerate)
     Ud = U.dag()

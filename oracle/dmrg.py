@@ -13,7 +13,7 @@ from __future__ import annotations
 import numpy as np
 
 from .blocksparse import BSTensor, contract, dot
-from .decomp import denmat_decomp, svd_split
+from .decomp import denmat_decomp, svd_split, combine, swap_prime01
 
 
 class LocalOp:
@@ -34,6 +34,23 @@ class LocalOp:
             if self.R is not None:
                 p = contract(p, self.R)
         return p.noprime()
+
+    def delta_rho(self, AA: BSTensor, cmb, fromleft: bool) -> BSTensor:
+        """LocalOp::deltaRho (itensor/mps/localop.h:375-406): the noise term
+        of the density matrix, AA with the environment and MPO tensor of the
+        side being orthogonalised, combined and squared, Hermitian part."""
+        drho = AA
+        if fromleft:
+            if self.L is not None:
+                drho = contract(drho, self.L)
+            drho = contract(drho, self.W1)
+        else:
+            if self.R is not None:
+                drho = contract(drho, self.R)
+            drho = contract(drho, self.W2)
+        drho = combine(drho.noprime(), cmb)
+        drho = contract(drho, drho.dag().prime(which={cmb.ci.id}))
+        return (drho + swap_prime01(drho).dag()).scale(0.5)
 
     def size(self, phi: BSTensor) -> int:
         n = 1
@@ -183,14 +200,16 @@ def dmrg(W, psi, sweeps, record=None, usesvd=None):
             op = PH.position(b, psi)
             phi = contract(psi[b - 1], psi[b])
             energy, phi = davidson(op, phi, maxiter=s["niter"])
-            svd_route = usesvd if usesvd is not None else (s["cutoff"] < 1e-12)
+            noise = s.get("noise", 0.0)
+            # MPS::svdBond (itensor/mps/mps_impl.h:50): SVD when UseSVD or (noise == 0 and cutoff < 1e-12)
+            svd_route = usesvd if usesvd is not None else (noise == 0 and s["cutoff"] < 1e-12)
             if svd_route:
                 Uinds = [I for I in psi[b - 1].inds if psi[b].find(I) < 0]
                 A, B, probs, te = svd_split(phi, Uinds, s["maxdim"], s["mindim"], s["cutoff"],
                                             fromleft=(ha == 1))
             else:
                 A, B, probs, te = denmat_decomp(phi, psi[b - 1], psi[b], ha == 1, s["maxdim"], s["mindim"],
-                                                s["cutoff"])
+                                                s["cutoff"], noise=noise, op=op)
             psi[b - 1], psi[b] = A, B
             link = [I for I in A.inds if B.find(I) >= 0][0]
             recs.append((sw, ha, b, energy, te, link.dim))

@@ -205,13 +205,13 @@ def build_mpo(H: Hamiltonian, sites=None):
             ferm = a in st.fermionic
             # start a channel here
             if any(tt[1] == a and tt[2] == n for tt in H.two):
-                put(("start", 0), (a, 1), a)
+                put(("start", 0), (a, 1), a, _left_coef(H, a, n))
             for k in range(1, rng):
                 if any(tt[1] == a and tt[2] == n - k and tt[4] > n for tt in H.two):
                     put((a, k), (a, k + 1), "F" if ferm else "Id")
         for (c, a, i, b, j) in H.two:
             if j == n:
-                put((a, j - i), ("done", 0), b, c)
+                put((a, j - i), ("done", 0), b, c / _left_coef(H, a, i))
         T = BSTensor([sites[n - 1].dag(), sites[n - 1].prime(), links[n - 1].dag(), links[n]])
         for cs in BSTensor.allowed_blocks(T.inds, QN()):
             blk = np.zeros(T.block_shape(cs), order="F")
@@ -231,6 +231,19 @@ def build_mpo(H: Hamiltonian, sites=None):
     Ws[0] = _project(Ws[0], 2, sec_of[("start", 0)], off_in[("start", 0)])
     Ws[-1] = _project(Ws[-1], 3, sec_of[("done", 0)], off_in[("done", 0)])
     return sites, Ws, links
+
+
+def _left_coef(H: Hamiltonian, a, i):
+    """Coefficient carried by the starting operator a at site i: the common
+    coefficient of every two-site term that starts there, else 1 (the ending
+    operators carry the rest).  For the nearest-neighbour Heisenberg chain
+    this is the gauge of sample/Heisenberg.h:79-90 (J/2 and Jz on the left
+    operator, 1 on the right), which the noise term (a sum over MPO link
+    channels, itensor/mps/localop.h:375-406) depends on."""
+    cs = [tt[0] for tt in H.two if tt[1] == a and tt[2] == i]
+    if cs and all(c == cs[0] for c in cs) and cs[0] != 0.0:
+        return cs[0]
+    return 1.0
 
 
 def _project(T: BSTensor, axis, sec, off):

@@ -548,6 +548,12 @@ static void gen_dmrg(std::string const& dir) {
         MPO H = Heisenberg(sites);
         cs.push_back(run_dmrg("heis20", sites, H, neel_mps(sites, N), mksweeps({10, 20, 100, 100, 200}, 1e-10),
                               "{\"type\":\"heisenberg\",\"J\":1.0,\"Jz\":1.0}"));
+        // the same with the noise schedule of sample/dmrg.cc (1e-7, 1e-8, then 0)
+        auto swn = mksweeps({10, 20, 100, 100, 200}, 1e-10);
+        swn.setnoise(1, 1e-7);
+        swn.setnoise(2, 1e-8);
+        cs.push_back(run_dmrg("heis20_noise", sites, H, neel_mps(sites, N), swn,
+                              "{\"type\":\"heisenberg\",\"J\":1.0,\"Jz\":1.0}"));
     }
     {   // XXZ N=16, Delta=0.5
         int N = 16; double D = 0.5;

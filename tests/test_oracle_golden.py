@@ -87,7 +87,7 @@ def test_bond_split(golden):
         assert same and err < 1e-12 * max(1.0, np.abs(T(c["AA"]).flat()).max()), (c["name"], err)
 
 
-@pytest.mark.parametrize("name", ["heis20", "xxz16", "j1j2_16", "tfi16", "hubbard8", "hubbard4x2"])
+@pytest.mark.parametrize("name", ["heis20", "heis20_noise", "xxz16", "j1j2_16", "tfi16", "hubbard8", "hubbard4x2"])
 def test_dmrg_energies_and_structure(golden, name):
     c = [x for x in golden("dmrg")["cases"] if x["name"] == name][0]
     N = c["N"]
@@ -98,10 +98,17 @@ def test_dmrg_energies_and_structure(golden, name):
     assert abs(E - c["energy"]) < ENERGY_TOL
     ref = c["bonds"]
     assert len(recs) == len(ref)
+    # With noise on, rho's SU(2) multiplets are split only by noise*drho, so a
+    # rounding-level change of rho (1e-16) rotates the kept vectors inside a
+    # multiplet and moves the next bond's (2-iteration) Davidson energy by
+    # ~1e-9 and a truncation error by ~1e-12 (measured by rescaling the noise
+    # by 1+1e-9); the final energy and the kept dims stay tight.
+    noisy = any(s.get("noise", 0.0) > 0 for s in c["sweeps"])
+    bond_tol, trunc_tol = (1e-8, 1e-11) if noisy else (ENERGY_TOL, 1e-12)
     for a, b in zip(recs, ref):
         assert tuple(a[:3]) == tuple(b[:3])
-        assert abs(a[3] - b[3]) < ENERGY_TOL
-        assert abs(a[4] - b[4]) < 1e-12
+        assert abs(a[3] - b[3]) < bond_tol
+        assert abs(a[4] - b[4]) < trunc_tol
         assert a[5] == b[5]          # kept states: exact
     for b in range(N - 1):
         link = [I for I in psi2[b].inds if psi2[b + 1].find(I) >= 0][0]
