@@ -186,6 +186,17 @@ int itg_denmat_decomp(itg_ctx* ctx, const itg_tensor* AA, const itg_tensor* A, c
                       int precision, itg_tensor** A_out, itg_tensor** B_out, double* truncerr, double* eigs,
                       int32_t* neigs);
 
+/* denmatDecomp with the noise term: rho += noise * deltaRho (LocalOp::deltaRho,
+ * itensor/mps/localop.h:375-406) and rho /= trace(rho) (itensor/decomp.h:386-394)
+ * when noise > 0. L/W1 (fromleft) or R/W2 (from the right) are the local
+ * operator's environment and MPO tensors; L or R may be null at the chain's
+ * ends. With noise == 0 this is itg_denmat_decomp. */
+int itg_denmat_decomp_noise(itg_ctx* ctx, const itg_tensor* AA, const itg_tensor* A, const itg_tensor* B, int fromleft,
+                            const itg_tensor* L, const itg_tensor* W1, const itg_tensor* W2, const itg_tensor* R,
+                            double noise, double cutoff, int32_t maxdim, int32_t mindim, int respect_degenerate,
+                            int normalize, int precision, itg_tensor** A_out, itg_tensor** B_out, double* truncerr,
+                            double* eigs, int32_t* neigs);
+
 /* SVD route of the bond split: svd (itensor/decomp.cc:121-248) with svdImpl's
  * QN branch (itensor/svd.cc:169-401), as MPS::svdBond uses it with UseSVD or
  * cutoff < 1e-12 (itensor/mps/mps_impl.h:50-65). A's indices that B lacks go to
@@ -219,8 +230,9 @@ typedef struct {
     int32_t maxdim, mindim;
     double cutoff;
     int32_t niter;
-    double noise;    /* must be 0 */
-    int32_t use_svd; /* 1: SVD bond split; 0: SVD only when cutoff < 1e-12, else density matrix */
+    double noise;    /* >= 0: density-matrix noise term (LocalOp::deltaRho, itensor/mps/localop.h:375-406) */
+    int32_t use_svd; /* 1: SVD bond split (noise ignored); 0: SVD only when noise == 0 and cutoff < 1e-12,
+                        else density matrix */
 } itg_sweep_desc;
 
 int itg_dmrg_run(itg_ctx* ctx, const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps,

@@ -91,6 +91,10 @@ SIGNATURES = {
     "itg_denmat_decomp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int32,
                                     C.c_int32, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p),
                                     C.POINTER(C.c_void_p), _f64p, _f64p, _i32p]),
+    "itg_denmat_decomp_noise": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int32,
+                                          C.c_int32, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p),
+                                          C.POINTER(C.c_void_p), _f64p, _f64p, _i32p]),
     "itg_svd_split": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int32,
                                 C.c_int32, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p),
                                 C.POINTER(C.c_void_p), _f64p, _f64p, _i32p]),
@@ -441,15 +445,24 @@ class Context:
         return e.value, Tensor(self, out)
 
     def denmat_decomp(self, AA, A, B, fromleft, cutoff, maxdim, mindim=1, respect_degenerate=True, normalize=True,
-                      precision=-1):
+                      precision=-1, noise=0.0, op=None):
+        """op = (L, W1, W2, R) (L or R may be None) for the noise term."""
         ao, bo = C.c_void_p(), C.c_void_p()
         te = C.c_double()
         cap = 1 << 16
         eigs = np.zeros(cap)
         n = C.c_int32(cap)
-        self._ok(lib().itg_denmat_decomp(self.h, AA.h, A.h, B.h, int(fromleft), cutoff, maxdim, mindim,
-                                         int(respect_degenerate), int(normalize), precision, C.byref(ao),
-                                         C.byref(bo), C.byref(te), _p(eigs, C.c_double), C.byref(n)), self.h)
+        if noise > 0:
+            L, W1, W2, R = op
+            h = lambda t: t.h if t is not None else None
+            self._ok(lib().itg_denmat_decomp_noise(self.h, AA.h, A.h, B.h, int(fromleft), h(L), h(W1), h(W2), h(R),
+                                                   noise, cutoff, maxdim, mindim, int(respect_degenerate),
+                                                   int(normalize), precision, C.byref(ao), C.byref(bo),
+                                                   C.byref(te), _p(eigs, C.c_double), C.byref(n)), self.h)
+        else:
+            self._ok(lib().itg_denmat_decomp(self.h, AA.h, A.h, B.h, int(fromleft), cutoff, maxdim, mindim,
+                                             int(respect_degenerate), int(normalize), precision, C.byref(ao),
+                                             C.byref(bo), C.byref(te), _p(eigs, C.c_double), C.byref(n)), self.h)
         return Tensor(self, ao), Tensor(self, bo), eigs[:n.value].copy(), te.value
 
     def svd_split(self, AA, A, B, fromleft, cutoff, maxdim, mindim=1, respect_degenerate=True, normalize=True,

@@ -101,8 +101,14 @@ struct SplitResult {
 };
 // denmatDecomp (itensor/decomp.h:316-418) with diag_hermitian's QN branch
 // (itensor/hermitian.cc:180-426) and the DoNormalize step of MPS::svdBond.
+// With noise > 0 and op given, rho += noise * deltaRho (LocalOp::deltaRho,
+// itensor/mps/localop.h:375-406) and rho is divided by its trace.
 SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor const& B, bool fromleft,
-                          SplitArgs const& args, int prec);
+                          SplitArgs const& args, int prec, LocalOp const* op = nullptr, double noise = 0.0);
+// The noise term of the density matrix: AA times the environment and MPO
+// tensor of the side being orthogonalised, primes removed, combined with cmb
+// and squared over every index but cmb.ci: indices (ci, ci'). Not symmetrised.
+Tensor delta_rho(Ctx& ctx, LocalOp const& op, Tensor const& AA, Combiner const& cmb, bool fromleft);
 
 // svd route of MPS::svdBond (itensor/mps/mps_impl.h:50-65): svd
 // (itensor/decomp.cc:121-248) with svdImpl's QN branch (itensor/svd.cc:169-401);

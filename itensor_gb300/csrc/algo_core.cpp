@@ -507,8 +507,45 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
 }
 
 // ---------------------------------------------------------------- density-matrix bond split
+Tensor delta_rho(Ctx& ctx, LocalOp const& op, Tensor const& AA, Combiner const& cmb, bool fromleft) {
+    Tensor const* env = fromleft ? op.L : op.R;
+    Tensor const* W = fromleft ? op.W1 : op.W2;
+    ITG_REQUIRE(W, "delta_rho: missing MPO tensor");
+    Tensor X = env ? contract(ctx, AA, *env, PREC_F64) : AA;
+    X = contract(ctx, X, *W, PREC_F64);
+    X = relabel(X, noprime_all(X.inds()));
+    Tensor Xc = combine(ctx, X, cmb);
+    std::vector<Index> dinds = dag_all(Xc.inds());
+    dinds[0] = dinds[0].prime();
+    return contract(ctx, Xc, relabel(Xc, dinds), PREC_F64);
+}
+
+// rho + noise * (D + D^T)/2 on the union of both block structures, divided by
+// its trace (itensor/decomp.h:386-394; ITensor's += keeps every block of both).
+static Tensor noisy_rho(Ctx& ctx, Tensor const& rho, Tensor const& D, double noise) {
+    Layout const& RL = *rho.lay;
+    Layout const& DL = *D.lay;
+    std::vector<int32_t> coords(RL.coords);
+    coords.insert(coords.end(), DL.coords.begin(), DL.coords.end());
+    auto UL = std::make_shared<Layout>(make_layout(rho.inds(), coords));
+    Tensor out(UL, ctx.stream);
+    std::vector<NoiseBlock> blocks(UL->nblocks());
+    for (int b = 0; b < UL->nblocks(); ++b) {
+        int32_t const* c = UL->block(b);
+        ITG_REQUIRE(c[0] == c[1], "noisy_rho: density matrix block off the diagonal");
+        const int rb = RL.find_block(c), db = DL.find_block(c);
+        blocks[b].out_off = UL->offs[b];
+        blocks[b].rho_off = rb >= 0 ? RL.offs[rb] : -1;
+        blocks[b].d_off = db >= 0 ? DL.offs[db] : -1;
+        blocks[b].n = (int32_t)rho.inds()[0].bdim(c[0]);
+        blocks[b].pad = 0;
+    }
+    launch_noisy_rho(ctx, blocks, rho.data(), D.data(), out.data(), UL->size, noise);
+    return out;
+}
+
 SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor const& B, bool fromleft,
-                          SplitArgs const& args, int prec) {
+                          SplitArgs const& args, int prec, LocalOp const* op, double noise) {
     Tensor const& to_orth = fromleft ? A : B;
     Tensor const& newoc = fromleft ? B : A;
     std::vector<Index> cinds;
@@ -520,6 +557,7 @@ SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor co
     std::vector<Index> dinds = dag_all(AAc.inds());
     dinds[0] = dinds[0].prime();
     Tensor rho = contract(ctx, AAc, relabel(AAc, dinds), PREC_F64);
+    if (noise > 0 && op) rho = noisy_rho(ctx, rho, delta_rho(ctx, *op, AA, cmb, fromleft), noise);
     Layout const& RL = *rho.lay;
     // one eigenproblem per diagonal block, in storage order
     const int nb = RL.nblocks();

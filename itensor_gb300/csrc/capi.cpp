@@ -71,12 +71,13 @@ std::vector<SweepSpec> sweeps_from(itg_sweep_desc const* sweeps, int n) {
     ITG_REQUIRE(sweeps && n > 0, "dmrg: empty sweep schedule");
     std::vector<SweepSpec> sw(n);
     for (int s = 0; s < n; ++s) {
-        ITG_REQUIRE(sweeps[s].noise == 0.0, "dmrg: the noise term is not supported");
+        ITG_REQUIRE(sweeps[s].noise >= 0.0, "dmrg: the noise must be non-negative");
         ITG_REQUIRE(sweeps[s].maxdim >= 1 && sweeps[s].niter >= 1, "dmrg: maxdim and niter must be positive");
         sw[s].maxdim = sweeps[s].maxdim;
         sw[s].mindim = sweeps[s].mindim;
         sw[s].cutoff = sweeps[s].cutoff;
         sw[s].niter = sweeps[s].niter;
+        sw[s].noise = sweeps[s].noise;
         sw[s].use_svd = sweeps[s].use_svd != 0;
     }
     return sw;
@@ -413,15 +414,33 @@ int itg_denmat_decomp(itg_ctx* c, const itg_tensor* AA, const itg_tensor* A, con
                       double cutoff, int32_t maxdim, int32_t mindim, int respect_degenerate, int normalize,
                       int precision, itg_tensor** A_out, itg_tensor** B_out, double* truncerr, double* eigs,
                       int32_t* neigs) {
+    return itg_denmat_decomp_noise(c, AA, A, B, fromleft, nullptr, nullptr, nullptr, nullptr, 0.0, cutoff, maxdim,
+                                   mindim, respect_degenerate, normalize, precision, A_out, B_out, truncerr, eigs,
+                                   neigs);
+}
+
+int itg_denmat_decomp_noise(itg_ctx* c, const itg_tensor* AA, const itg_tensor* A, const itg_tensor* B, int fromleft,
+                            const itg_tensor* L, const itg_tensor* W1, const itg_tensor* W2, const itg_tensor* R,
+                            double noise, double cutoff, int32_t maxdim, int32_t mindim, int respect_degenerate,
+                            int normalize, int precision, itg_tensor** A_out, itg_tensor** B_out, double* truncerr,
+                            double* eigs, int32_t* neigs) {
     return guard(c, [&] {
         ITG_REQUIRE(AA && A && B && A_out && B_out, "denmat_decomp: null argument");
+        ITG_REQUIRE(noise >= 0.0, "denmat_decomp: the noise must be non-negative");
+        ITG_REQUIRE(noise == 0.0 || (fromleft ? W1 : W2), "denmat_decomp: the noise term needs the MPO tensor");
         SplitArgs sa;
         sa.cutoff = cutoff;
         sa.maxdim = maxdim;
         sa.mindim = mindim;
         sa.respect_degenerate = respect_degenerate != 0;
         sa.normalize = normalize != 0;
-        SplitResult r = denmat_decomp(c->ctx, AA->t, A->t, B->t, fromleft != 0, sa, precision);
+        LocalOp op;
+        op.L = opt(L);
+        op.W1 = opt(W1);
+        op.W2 = opt(W2);
+        op.R = opt(R);
+        SplitResult r = denmat_decomp(c->ctx, AA->t, A->t, B->t, fromleft != 0, sa, precision,
+                                      noise > 0 ? &op : nullptr, noise);
         *A_out = new itg_tensor{r.A};
         *B_out = new itg_tensor{r.B};
         if (truncerr) *truncerr = r.truncerr;

@@ -81,9 +81,10 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
             sa.respect_degenerate = true;
             sa.normalize = true;
             // MPS::svdBond: SVD when UseSVD or (noise == 0 and cutoff < 1e-12), else density matrix
-            const bool svd_route = s.use_svd || s.cutoff < 1e-12;
+            // with the noise term (the SVD route ignores noise, as the reference does)
+            const bool svd_route = s.use_svd || (s.noise == 0 && s.cutoff < 1e-12);
             SplitResult sr = svd_route ? svd_split(ctx, phi, A, B, ha == 1, sa, prec)
-                                       : denmat_decomp(ctx, phi, A, B, ha == 1, sa, prec);
+                                       : denmat_decomp(ctx, phi, A, B, ha == 1, sa, prec, &op, s.noise);
             psi[b - 1] = sr.A;
             psi[b] = sr.B;
             auto tp3 = clk::now();

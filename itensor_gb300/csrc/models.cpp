@@ -157,6 +157,23 @@ static QN op_flux(SiteType const& st, std::vector<double> const& O) {
     return QN();
 }
 
+// Coefficient carried by the starting operator a at site i: the common
+// coefficient of every two-site term starting there, else 1 (the ending
+// operator carries the rest). For the nearest-neighbour Heisenberg chain this
+// is the gauge of sample/Heisenberg.h:79-90 (J/2 and Jz on the left operator),
+// which the density-matrix noise term (a sum over MPO link channels,
+// itensor/mps/localop.h:375-406) depends on.
+static double left_coef(Hamiltonian const& H, std::string const& a, int i) {
+    double c0 = 0.0;
+    bool any = false;
+    for (auto const& t : H.two) {
+        if (t.a != a || t.i != i) continue;
+        if (!any) { c0 = t.c; any = true; }
+        else if (t.c != c0) return 1.0;
+    }
+    return (any && c0 != 0.0) ? c0 : 1.0;
+}
+
 int mpo_bond_dim(Hamiltonian const& H) {
     std::vector<std::string> lefts;
     int rng = 1;
@@ -215,7 +232,7 @@ MPO build_mpo(Ctx& ctx, Hamiltonian const& H) {
             bool ferm = std::find(st.fermionic.begin(), st.fermionic.end(), lefts[ai]) != st.fermionic.end();
             bool starts = false;
             for (auto const& t : H.two) if (t.a == lefts[ai] && t.i == n) starts = true;
-            if (starts) put(1, chan((int)ai, 1), lefts[ai], 1.0);
+            if (starts) put(1, chan((int)ai, 1), lefts[ai], left_coef(H, lefts[ai], n));
             for (int k = 1; k < rng; ++k) {
                 bool pass = false;
                 for (auto const& t : H.two) if (t.a == lefts[ai] && t.i == n - k && t.j > n) pass = true;
@@ -225,7 +242,7 @@ MPO build_mpo(Ctx& ctx, Hamiltonian const& H) {
         for (auto const& t : H.two)
             if (t.j == n) {
                 int ai = (int)(std::find(lefts.begin(), lefts.end(), t.a) - lefts.begin());
-                put(chan(ai, t.j - t.i), 0, t.b, t.c);
+                put(chan(ai, t.j - t.i), 0, t.b, t.c / left_coef(H, t.a, t.i));
             }
         // QN blocks of (dag(s), s', dag(row link), col link); first/last project the boundary
         const bool first = (n == 1), last = (n == N);

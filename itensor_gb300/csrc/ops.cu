@@ -296,6 +296,69 @@ void launch_gather(Ctx& ctx, GatherPlan const& g, double const* src, double* dst
     ctx.kernel_launches++;
 }
 
+// ------------------------------------------------------------------ noisy density matrix
+// rho + noise * deltaRho with deltaRho's Hermitian part (itensor/mps/localop.h:399-403):
+// one CTA per diagonal block.
+__global__ void noisy_rho_kernel(NoiseBlock const* __restrict__ blocks, double const* __restrict__ rho,
+                                 double const* __restrict__ d, double* __restrict__ out, double half_noise) {
+    const NoiseBlock bk = blocks[blockIdx.x];
+    const int64_t n = bk.n;
+    for (int64_t e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int64_t i = e % n, j = e / n;
+        double v = bk.rho_off >= 0 ? rho[bk.rho_off + e] : 0.0;
+        if (bk.d_off >= 0) v = fma(half_noise, d[bk.d_off + e] + d[bk.d_off + i * n + j], v);
+        out[bk.out_off + e] = v;
+    }
+}
+
+// Trace over every block's diagonal in a fixed order (one CTA, deterministic),
+// then the scale 1/tr applied by all CTAs when tr > 1e-16.
+constexpr int TRACE_THREADS = 256;
+__global__ void block_trace_kernel(NoiseBlock const* __restrict__ blocks, int nb, double const* __restrict__ out,
+                                   double* __restrict__ tr) {
+    __shared__ double part[TRACE_THREADS];
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) {
+        const NoiseBlock bk = blocks[b];
+        for (int64_t i = threadIdx.x; i < bk.n; i += blockDim.x) s += out[bk.out_off + i * (bk.n + 1)];
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = TRACE_THREADS / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *tr = part[0];
+}
+__global__ void trace_normalise_kernel(double* __restrict__ x, int64_t n, double const* __restrict__ tr) {
+    const double t = *tr;
+    if (!(t > 1e-16)) return;
+    const double inv = 1.0 / t;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] *= inv;
+}
+
+void launch_noisy_rho(Ctx& ctx, std::vector<NoiseBlock> const& blocks, double const* rho, double const* d,
+                      double* out, int64_t out_size, double noise) {
+    if (blocks.empty()) return;
+    const size_t bytes = sizeof(NoiseBlock) * blocks.size();
+    ctx.ensure_stage(bytes);
+    std::memcpy(ctx.stage, blocks.data(), bytes);
+    DevBuf tab(bytes + 16, ctx.stream);
+    ITG_CHECK_CUDA(cudaMemcpyAsync(tab.as<char>(), ctx.stage, bytes, cudaMemcpyHostToDevice, ctx.stream));
+    NoiseBlock const* dblocks = reinterpret_cast<NoiseBlock const*>(tab.as<char>());
+    double* dtr = reinterpret_cast<double*>(tab.as<char>() + bytes);
+    noisy_rho_kernel<<<(int)blocks.size(), 256, 0, ctx.stream>>>(dblocks, rho, d, out, 0.5 * noise);
+    ITG_CHECK_CUDA(cudaGetLastError());
+    block_trace_kernel<<<1, TRACE_THREADS, 0, ctx.stream>>>(dblocks, (int)blocks.size(), out, dtr);
+    ITG_CHECK_CUDA(cudaGetLastError());
+    trace_normalise_kernel<<<grid_for(ctx, out_size), 256, 0, ctx.stream>>>(out, out_size, dtr);
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches += 3;
+    // the staging buffer is reused by the next upload: wait until the copy has read it
+    ctx.sync();
+}
+
 // Deterministic pseudo-random fill in [0,1) (splitmix64 of the element index
 // and a seed); used when Davidson must replace a dependent vector.
 __global__ void random_kernel(double* x, int64_t n, uint64_t seed) {

@@ -26,6 +26,19 @@ struct GatherPlan {
     void upload(Ctx& ctx);
 };
 
+// One diagonal block of the noisy density matrix (denmat_decomp with noise):
+// out = rho + noise * (D + D^T) / 2 on an n x n block; rho_off or d_off < 0
+// when that term has no such block.
+struct NoiseBlock {
+    int64_t out_off, rho_off, d_off;
+    int32_t n, pad;
+};
+// Writes every block of `out` (blocks listed in storage order), then divides
+// out by its trace when the trace exceeds 1e-16 (itensor/decomp.h:386-394).
+// Device-side throughout: no host wait.
+void launch_noisy_rho(Ctx& ctx, std::vector<NoiseBlock> const& blocks, double const* rho, double const* d,
+                      double* out, int64_t out_size, double noise);
+
 // One symmetric n x n matrix (column-major) to diagonalise.
 struct EigItem {
     int64_t a_off;   // input matrix in the source buffer

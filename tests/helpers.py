@@ -94,3 +94,23 @@ def gpu_layout_matches(t, refj):
     same_blocks = coords.shape[0] == rb.shape[0] and np.array_equal(coords.reshape(rb.shape), rb) and \
         list(offs) == list(refj["offsets"])
     return same_inds, same_blocks
+
+
+def bst_json(X):
+    """An oracle tensor in the fixture format (for uploading through gpu_tensor)."""
+    inds = [dict(id=I.id, plev=I.plev, dir=I.dir, sectors=[[q.to_json(), d] for q, d in I.sectors])
+            for I in X.inds]
+    if not X.inds:
+        return dict(inds=[], data=[float(X.scalar or 0.0)])
+    blocks, offsets, data, off = [], [], [], 0
+    for c in X.sorted_coords():
+        b = X.blocks[c]
+        blocks.append(list(c))
+        offsets.append(off)
+        data.extend(np.asarray(b).reshape(-1, order="F").tolist())
+        off += b.size
+    return dict(inds=inds, blocks=blocks, offsets=offsets, data=data)
+
+
+def to_gpu(ctx, X, names):
+    return gpu_tensor(ctx, bst_json(X), names)

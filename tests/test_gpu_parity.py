@@ -165,7 +165,7 @@ def test_denmat_golden(ctx, golden):
                 assert np.max(np.abs(np.transpose(blk_ref, inds_map) - blk)) < 1e-11 * max(1, np.abs(ref.flat()).max())
 
 
-@pytest.mark.parametrize("name", ["heis20", "xxz16", "j1j2_16", "tfi16", "hubbard8", "hubbard4x2"])
+@pytest.mark.parametrize("name", ["heis20", "heis20_noise", "xxz16", "j1j2_16", "tfi16", "hubbard8", "hubbard4x2"])
 def test_dmrg_golden(ctx, golden, name):
     c = [x for x in golden("dmrg")["cases"] if x["name"] == name][0]
     m = c["model"]
@@ -180,10 +180,17 @@ def test_dmrg_golden(ctx, golden, name):
     res = ctx.dmrg(model, c["sweeps"], precision=0)
     assert abs(res.energy - c["energy"]) < ENERGY_TOL
     assert len(res.bonds) == len(c["bonds"])
+    # noise splits rho's SU(2) multiplets only by noise*drho, so rounding-level
+    # changes move the kept vectors inside a multiplet: in the first, noisiest
+    # sweep a bond's (2-iteration) Davidson energy moves by up to ~3e-8 between
+    # summation orders (the oracle moves 3e-9 when rho changes by 1e-14), and a
+    # truncation error by ~2e-12; the final energy and kept dims stay tight.
+    noisy = any(s.get("noise", 0.0) > 0 for s in c["sweeps"])
+    bond_tol, trunc_tol = (1e-7, 1e-11) if noisy else (ENERGY_TOL, 1e-12)
     for a, b in zip(res.bonds, c["bonds"]):
         assert tuple(a[:3]) == tuple(b[:3])
-        assert abs(a[3] - b[3]) < ENERGY_TOL, (a, b)
-        assert abs(a[4] - b[4]) < 1e-12
+        assert abs(a[3] - b[3]) < bond_tol, (a, b)
+        assert abs(a[4] - b[4]) < trunc_tol
         assert a[5] == b[5]
     for (dr, qn, dims), ref in zip(res.links, c["links"]):
         assert [int(x) for x in dims] == [d for _, d in ref["sectors"]]
@@ -248,3 +255,53 @@ def test_dmrg_svd_route_matches_oracle(ctx):
     for a, b in zip(res.bonds, recs):
         assert abs(a[3] - b[3]) < 1e-10
         assert a[5] == b[5]
+
+
+def test_dmrg_noise_matches_oracle(ctx):
+    """Noise term on a fermionic MPO (Hubbard 4x2, Jordan-Wigner strings in the
+    channels) against the CPU oracle's deltaRho."""
+    from oracle import models
+    from oracle.dmrg import dmrg as odmrg
+    sweeps = [dict(maxdim=m, mindim=1, cutoff=1e-9, niter=2, noise=nz)
+              for m, nz in ((8, 1e-5), (16, 1e-6), (24, 1e-7), (32, 0.0))]
+    res = ctx.dmrg(dict(type=2, Lx=4, Ly=2, t=1.0, U=4.0, yperiodic=0), sweeps, precision=0)
+    H = models.hubbard(4, 2, 1.0, 4.0)
+    sites, W, _ = models.build_mpo(H)
+    labels = ["Up" if i % 2 == 0 else "Dn" for i in range(8)]
+    psi = models.product_mps(sites, H.st, labels)
+    E, _, recs = odmrg(W, psi, sweeps)
+    assert abs(res.energy - E) < 1e-10
+    assert len(res.bonds) == len(recs)
+    for a, b in zip(res.bonds, recs):
+        assert tuple(a[:3]) == tuple(b[:3])
+        assert abs(a[3] - b[3]) < 1e-8, (a, b)
+        assert abs(a[4] - b[4]) < 1e-11
+        assert a[5] == b[5]
+
+
+def test_denmat_noise_single_bond(ctx):
+    """One noisy density-matrix split, from the left and from the right, against
+    the oracle: trace-normalised eigenvalues and truncation error."""
+    from oracle import models
+    from oracle.blocksparse import contract as ocontract
+    from oracle.dmrg import LocalMPO, dmrg as odmrg
+    from oracle.decomp import denmat_decomp as odenmat
+    from helpers import to_gpu
+    N = 6
+    H = models.heisenberg(N)
+    sites, W, _ = models.build_mpo(H)
+    psi = models.product_mps(sites, H.st, ["Up" if i % 2 == 0 else "Dn" for i in range(N)])
+    _, psi, _ = odmrg(W, psi, [dict(maxdim=4, mindim=1, cutoff=1e-12, niter=2)])
+    for b in (1, 3, 5):  # chain end (no L), middle, other end (no R)
+        op = LocalMPO(W).position(b, psi)
+        A, B = psi[b - 1], psi[b]
+        AA = ocontract(A, B)
+        names = ["Sz"]
+        g = lambda X: to_gpu(ctx, X, names) if X is not None else None
+        for fromleft in (True, False):
+            _, _, probs, te = odenmat(AA, A, B, fromleft, 3, 1, 1e-12, normalize=False, noise=1e-3, op=op)
+            _, _, eigs, gte = ctx.denmat_decomp(g(AA), g(A), g(B), fromleft, 1e-12, 3, 1, normalize=False,
+                                                noise=1e-3, op=(g(op.L), g(op.W1), g(op.W2), g(op.R)))
+            assert len(eigs) == len(probs), (b, fromleft)
+            assert np.max(np.abs(eigs - probs)) < 1e-13, (b, fromleft)
+            assert abs(gte - te) < 1e-13, (b, fromleft)
