@@ -407,6 +407,45 @@ def run_profile_dmrg(args):
     return 0
 
 
+def cylinder_sweeps(maxdim):
+    """The sweep table of the reference's 2D Hubbard sample (sample/hubbard_2d.cc:43-46):
+    maxdim 20, 60, 100, 100, 200, 400, 800, 2000, 3000 (capped at `maxdim`), noise
+    1e-7, 1e-8, 1e-10, then 0; cutoff 1e-9 and niter 2 as the cylinder workload states."""
+    mds = [m for m in (20, 60, 100, 100, 200, 400, 800, 2000, 3000) if m < maxdim] + [maxdim]
+    noise = [1e-7, 1e-8, 1e-10]
+    return [dict(maxdim=m, mindim=1, cutoff=1e-9, niter=2, noise=noise[i] if i < len(noise) else 0.0)
+            for i, m in enumerate(mds)]
+
+
+def run_cylinder(args):
+    """Hubbard model on a 4x16 cylinder (Nx=16, Ny=4 periodic in y, snaked into
+    the chain), t=1, U=4, half filling, (Nf, Sz) QN, Neel product start: DMRG in
+    the split precision and in plain FP64 on the same sweep table; reports both
+    energies, their difference, sweep times and the phase split."""
+    import itensor_gb300 as itg
+    ctx = itg.Context(0)
+    model = dict(type=2, Lx=16, Ly=4, t=1.0, U=4.0, yperiodic=1)
+    sw = cylinder_sweeps(args.cylinder)
+    out = {"workload": "hubbard_4x16_cylinder", "t": 1.0, "U": 4.0, "sweeps": sw}
+    runs = [(n, {"split": itg.PREC_OZAKI_BF16, "fp64": itg.PREC_F64}[n]) for n in args.cyl_runs.split(",")]
+    for name, prec in runs:
+        clk = ClockSampler(0)
+        clk.start()
+        t0 = time.perf_counter()
+        r = ctx.dmrg(model, sw, precision=prec)
+        el = time.perf_counter() - t0
+        out[name] = {"energy": r.energy, "seconds": el, "sweep_seconds": r.sweep_seconds,
+                     "phase_seconds": r.phase_seconds, "max_link_dim": max(sum(int(x) for x in d) for _, _, d in r.links),
+                     "last_sweep_truncerr_max": max(b[4] for b in r.bonds[-(2 * (64 - 1)):]),
+                     "clocks": clk.stop()}
+        print(json.dumps({name: out[name]}), flush=True)
+    if "fp64" in out:
+        out["energy_diff_split_vs_fp64"] = out["split"]["energy"] - out["fp64"]["energy"]
+    print(json.dumps(out))
+    ctx.close()
+    return 0
+
+
 def run_profile(args):
     """Short run of the same workload for ncu: for the split form and plain
     FP64, N prepared applies each (kernels launched one by one)."""
@@ -444,6 +483,9 @@ def main():
                     help="profiling run for ncu: one J1-J2 chain N=48, J2=0.3, maxdim 64/128/256, split precision")
     ap.add_argument("--profile", type=int, default=0,
                     help="profiling run for ncu: N prepared applies per arithmetic, no graph, no timing")
+    ap.add_argument("--cylinder", type=int, default=0,
+                    help="Hubbard 4x16 cylinder DMRG up to this maxdim (3000 in the workload), split and FP64")
+    ap.add_argument("--cyl-runs", default="split,fp64", help="with --cylinder: which arithmetics to run")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -451,6 +493,8 @@ def main():
         return run_profile(args)
     if args.profile_dmrg:
         return run_profile_dmrg(args)
+    if args.cylinder:
+        return run_cylinder(args)
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
 

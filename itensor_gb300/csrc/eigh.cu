@@ -25,7 +25,9 @@
 // sweep skips every pair. Sweeps are capped; a capped matrix still counts as
 // converged when its largest off-diagonal entry is below 1e-13 ||A||_F.
 #include "ops.h"
+#include "eigh_tri.h"
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -158,10 +160,11 @@ __device__ int jacobi_run(double* A, int lda, double* V, int ldv, double2* rlog,
 }
 
 // One block on the device: EigItem plus the offset of its rotation log
-// (double2 units; -1 when V is accumulated in the CTA).
+// (double2 units; -1 when V is accumulated in the CTA) and of its eigenvalue
+// ranks in this launch's rank array.
 struct EigJob {
     int64_t a_off, v_off, w_off, s_off, r_off;
-    int32_t n, pad;
+    int32_t n, k_off;
 };
 
 template <bool SMEM_A, bool SMEM_V>
@@ -224,7 +227,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigJob const* __res
         }
         wout[it.w_off + r] = di;
         rank[i] = r;
-        if (logv) ranks[it.w_off + i] = r;
+        if (logv) ranks[it.k_off + i] = r;
     }
     __syncthreads();
     if (V) {
@@ -259,7 +262,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigJob const* __res
 // every logged rotation in order (column pairs of a round are disjoint, so a
 // round is one parallel step), then written to vout in eigenvalue order.
 struct VJob {
-    int64_t v_off, r_off, w_off;
+    int64_t v_off, r_off, k_off;
     int32_t n, row0, rows, blk;
 };
 
@@ -297,7 +300,7 @@ __global__ void __launch_bounds__(EIG_THREADS) vapply_kernel(VJob const* __restr
     }
     for (int e = tid; e < R * n; e += nt) {
         const int r = e / n, col = e % n;
-        vout[j.v_off + (size_t)ranks[j.w_off + col] * n + j.row0 + r] = vr[e];
+        vout[j.v_off + (size_t)ranks[j.k_off + col] * n + j.row0 + r] = vr[e];
     }
 }
 
@@ -327,8 +330,8 @@ void launch_eig(Ctx& ctx, int njobs, size_t smem, EigJob const* d_jobs, double c
 }
 }  // namespace
 
-int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
-                 double* scratch) {
+static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
+                       double* scratch) {
     if (items.empty()) return 0;
     const int nb = (int)items.size();
     int nmax = 0;
@@ -355,15 +358,17 @@ int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src,
         while (rows > 1 && (size_t)rows * nmax * sizeof(double) > EIG_SMEM_LIMIT) rows /= 2;
     }
     size_t roff = 0;
+    int32_t koff = 0;  // ranks of this launch's items, packed in item order
     for (int b = 0; b < nb; ++b) {
         auto const& it = items[b];
         const int np = it.n + (it.n & 1);
-        jobs[b] = EigJob{it.a_off, it.v_off, it.w_off, it.s_off, logv ? (int64_t)roff : -1, it.n, 0};
+        jobs[b] = EigJob{it.a_off, it.v_off, it.w_off, it.s_off, logv ? (int64_t)roff : -1, it.n, koff};
         if (logv) {
             for (int r0 = 0; r0 < it.n; r0 += rows)
-                vjobs.push_back(VJob{it.v_off, (int64_t)roff, it.w_off, it.n, r0, std::min(rows, it.n - r0), b});
+                vjobs.push_back(VJob{it.v_off, (int64_t)roff, (int64_t)koff, it.n, r0, std::min(rows, it.n - r0), b});
             roff += (size_t)EIG_MAX_SWEEPS * std::max(np - 1, 0) * (np / 2);
         }
+        koff += it.n;
     }
     const bool sa = eig_smem_bytes(nmax, true, false) <= EIG_SMEM_LIMIT;
     const bool sv = !logv && sa && eig_smem_bytes(nmax, true, true) <= EIG_SMEM_LIMIT;
@@ -408,6 +413,33 @@ int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src,
         std::fprintf(stderr, "itg eigh:");
         for (int b = 0; b < nb; ++b) std::fprintf(stderr, " %d/%d", items[b].n, swv[b]);
         std::fprintf(stderr, "\n");
+    }
+    return bad;
+}
+
+// Small blocks: one-CTA Jacobi; large ones: the tridiagonal path (eigh_tri.cu).
+int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
+                 double* scratch) {
+    int tmin = TRI_MIN_N_DEFAULT;
+    if (char const* env = std::getenv("ITG_EIG_TRI_MIN")) tmin = std::max(1, std::atoi(env));
+    std::vector<EigItem> small, large;
+    for (auto const& it : items) (it.n >= tmin && it.n <= TRI_MAX_N ? large : small).push_back(it);
+    const bool timing = std::getenv("ITG_EIG_TIME") != nullptr;  // diagnostics: wall time of each path
+    auto now = [&] { ctx.sync(); return std::chrono::steady_clock::now(); };
+    auto t0 = timing ? now() : std::chrono::steady_clock::time_point{};
+    // Jacobi first: both paths stage uploads in the context's pinned buffer, and
+    // each is done with it when it returns
+    int bad = jacobi_eigh(ctx, small, src, vout, wout, scratch);
+    auto t1 = timing ? now() : t0;
+    bad += tri_eigh(ctx, large, src, vout, wout, scratch);
+    if (timing) {
+        auto t2 = now();
+        int nl = 0, ns = 0;
+        for (auto const& it : large) nl = std::max(nl, it.n);
+        for (auto const& it : small) ns = std::max(ns, it.n);
+        std::fprintf(stderr, "itg eigh-time: tri %zu blocks nmax %d %.3f ms | jacobi %zu blocks nmax %d %.3f ms\n",
+                     large.size(), nl, std::chrono::duration<double, std::milli>(t2 - t1).count(), small.size(), ns,
+                     std::chrono::duration<double, std::milli>(t1 - t0).count());
     }
     return bad;
 }

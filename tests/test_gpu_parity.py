@@ -305,3 +305,51 @@ def test_denmat_noise_single_bond(ctx):
             assert len(eigs) == len(probs), (b, fromleft)
             assert np.max(np.abs(eigs - probs)) < 1e-13, (b, fromleft)
             assert abs(gte - te) < 1e-13, (b, fromleft)
+
+
+def _big_split_problem(seed=3):
+    """A two-site tensor whose density-matrix blocks are several hundred wide."""
+    from oracle.blocksparse import BSTensor, Index, QN, OUT, IN
+    rng = np.random.default_rng(seed)
+    q = lambda v: QN(("Sz", v, 1))
+    l = Index([(q(-4), 90), (q(-2), 200), (q(0), 260), (q(2), 200), (q(4), 90)], dir=IN, tags="l")
+    s1 = Index([(q(1), 1), (q(-1), 1)], dir=OUT, tags="s1")
+    s2 = Index([(q(1), 1), (q(-1), 1)], dir=OUT, tags="s2")
+    r = Index([(q(-2), 30), (q(0), 60), (q(2), 30)], dir=OUT, tags="r")
+    a = Index([(q(0), 4), (q(2), 4), (q(-2), 4)], dir=OUT, tags="a")
+    AA = BSTensor.random([l, s1, s2, r], QN(("Sz", 0, 1)), rng)
+    # a decaying spectrum, as in a density matrix: scale the right index's columns
+    for c, b in AA.blocks.items():
+        b *= np.exp(-np.arange(b.shape[3]) / 6.0)[None, None, None, :]
+    A = BSTensor.random([l, s1, a], QN(("Sz", 0, 1)), rng)
+    B = BSTensor.random([a.dag(), s2, r], QN(("Sz", 0, 1)), rng)
+    return AA, A, B
+
+
+@pytest.mark.parametrize("tri_min", ["64", "300", "100000"])
+def test_denmat_large_blocks(ctx, tri_min, monkeypatch):
+    """Density-matrix blocks of 90..460 rows through the tridiagonal eigensolver
+    (and, for comparison, the Jacobi one) against the oracle's eigh."""
+    from oracle.decomp import denmat_decomp as odenmat
+    from helpers import to_gpu
+    monkeypatch.setenv("ITG_EIG_TRI_MIN", tri_min)
+    AA, A, B = _big_split_problem()
+    names = ["Sz"]
+    for fromleft in (True, False):
+        _, _, probs, te = odenmat(AA, A, B, fromleft, 400, 1, 1e-10, normalize=False)
+        gA, gB, eigs, gte = ctx.denmat_decomp(to_gpu(ctx, AA, names), to_gpu(ctx, A, names), to_gpu(ctx, B, names),
+                                              fromleft, 1e-10, 400, 1, normalize=False)
+        assert len(eigs) == len(probs), fromleft
+        assert np.max(np.abs(eigs - probs)) < 1e-12 * probs[0], fromleft
+        assert abs(gte - te) < 1e-12, fromleft
+        # A' B' reproduces the truncated product: compare norms of the kept weight
+        AB = ctx.contract(gA, gB)
+        nrm2 = float(np.sum(AB.numpy() ** 2))
+        assert abs(nrm2 - np.sum(probs)) < 1e-10 * np.sum(probs)
+
+
+@pytest.mark.parametrize("name", ["heis20", "hubbard4x2", "heis20_noise"])
+def test_dmrg_golden_tridiagonal_eigh(ctx, golden, name, monkeypatch):
+    """Every density-matrix block through the tridiagonal path (down to 1x1)."""
+    monkeypatch.setenv("ITG_EIG_TRI_MIN", "1")
+    test_dmrg_golden(ctx, golden, name)
