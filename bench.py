@@ -439,7 +439,7 @@ def run_cylinder(args):
                      "last_sweep_truncerr_max": max(b[4] for b in r.bonds[-(2 * (64 - 1)):]),
                      "clocks": clk.stop()}
         print(json.dumps({name: out[name]}), flush=True)
-    if "fp64" in out:
+    if "fp64" in out and "split" in out:
         out["energy_diff_split_vs_fp64"] = out["split"]["energy"] - out["fp64"]["energy"]
     print(json.dumps(out))
     ctx.close()
