@@ -11,6 +11,9 @@
 // through per-block offset tables (offset(m,k) = T_m[m] + T_k[k]), so arbitrary
 // index permutations cost nothing extra and no permuted copy is ever formed.
 #include "engine.h"
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cuda_bf16.h>
 #include <algorithm>
 #include <cstring>
@@ -268,6 +271,7 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
     constexpr int T = GEMM_TILE, TK = 16;
     __shared__ double As[TK][T + 1];
     __shared__ double Bs[TK][T + 1];
+    __shared__ int32_t rowA[T], colB[T], kA[TK], kB[TK];   // this tile's offsets
     const ItemRec it = items[blockIdx.x];
     const CBlockRec cb = cblk[it.c];
     const int tid = threadIdx.x;
@@ -277,13 +281,24 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
     double acc00 = 0, acc01 = 0, acc10 = 0, acc11 = 0;
     for (int p = it.p0; p < it.p1; ++p) {
         const PairRec pr = pairs[p];
+        if (tid < T) {
+            const int m = it.m0 + tid, n = it.n0 + tid;
+            rowA[tid] = m < cb.M ? tab_at(tab, pr.tam, m) : 0;
+            colB[tid] = n < cb.N ? tab_at(tab, pr.tbn, n) : 0;
+        }
         for (int k0 = 0; k0 < pr.K; k0 += TK) {
+            if (tid >= 64 && tid < 64 + TK) {
+                const int k = k0 + tid - 64;
+                kA[tid - 64] = k < pr.K ? tab_at(tab, pr.tak, k) : 0;
+                kB[tid - 64] = k < pr.K ? tab_at(tab, pr.tbk, k) : 0;
+            }
+            __syncthreads();
             for (int e = tid; e < TK * T; e += 256) {
                 int i = e % T, kk = e / T;
                 int m = it.m0 + i, k = k0 + kk;
-                As[kk][i] = (m < cb.M && k < pr.K) ? A[pr.aoff + tab[pr.tam + m] + tab[pr.tak + k]] : 0.0;
+                As[kk][i] = (m < cb.M && k < pr.K) ? A[pr.aoff + rowA[i] + kA[kk]] : 0.0;
                 int n = it.n0 + i;
-                Bs[kk][i] = (n < cb.N && k < pr.K) ? B[pr.boff + tab[pr.tbk + k] + tab[pr.tbn + n]] : 0.0;
+                Bs[kk][i] = (n < cb.N && k < pr.K) ? B[pr.boff + kB[kk] + colB[i]] : 0.0;
             }
             __syncthreads();
             if (warp_active) {
@@ -306,7 +321,7 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
     for (int r = 0; r < 2; ++r)
 #pragma unroll
         for (int s = 0; s < 2; ++s)
-            if (m + r < cb.M && n + s < cb.N) C[cb.coff + tab[cb.tcm + m + r] + tab[cb.tcn + n + s]] = accs[r][s];
+            if (m + r < cb.M && n + s < cb.N) C[cb.coff + tab_at(tab, cb.tcm, m + r) + tab_at(tab, cb.tcn, n + s)] = accs[r][s];
 }
 
 // ------------------------------------------------------------------ skinny FP64 block GEMM
@@ -339,17 +354,17 @@ __device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& 
         const PairRec pr = pairs[p];
         int arow[R];
 #pragma unroll
-        for (int j = 0; j < R; ++j) arow[j] = mrow[j] < cb.M ? tab[pr.tam + mrow[j]] : -1;
+        for (int j = 0; j < R; ++j) arow[j] = mrow[j] < cb.M ? tab_at(tab, pr.tam, mrow[j]) : -1;
         for (int k0 = 0; k0 < pr.K; k0 += SKINNY_K) {
             const int kn = min(SKINNY_K, pr.K - k0);
             __syncthreads();
             for (int e = threadIdx.x; e < kn * NN; e += blockDim.x) {
                 int k = e / NN, n = e % NN;
-                Bs[k][n] = B[pr.boff + tab[pr.tbk + k0 + k] + tab[pr.tbn + n]];
+                Bs[k][n] = B[pr.boff + tab_at(tab, pr.tbk, k0 + k) + tab_at(tab, pr.tbn, n)];
             }
             __syncthreads();
             for (int k = 0; k < kn; ++k) {
-                const int ko = tab[pr.tak + k0 + k];
+                const int ko = tab_at(tab, pr.tak, k0 + k);
                 double a[R];
 #pragma unroll
                 for (int j = 0; j < R; ++j) a[j] = arow[j] >= 0 ? A[pr.aoff + arow[j] + ko] : 0.0;
@@ -367,9 +382,9 @@ __device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& 
 #pragma unroll
     for (int j = 0; j < R; ++j) {
         if (mrow[j] < cb.M) {
-            const int64_t crow = cb.coff + tab[cb.tcm + mrow[j]];
+            const int64_t crow = cb.coff + tab_at(tab, cb.tcm, mrow[j]);
 #pragma unroll
-            for (int n = 0; n < NN; ++n) C[crow + tab[cb.tcn + n]] = acc[j][n];
+            for (int n = 0; n < NN; ++n) C[crow + tab_at(tab, cb.tcn, n)] = acc[j][n];
         }
     }
 }
@@ -396,12 +411,12 @@ __device__ __forceinline__ void skinny_item_direct(ItemRec const& it, CBlockRec 
         const PairRec pr = pairs[p];
         int arow[R];
 #pragma unroll
-        for (int j = 0; j < R; ++j) arow[j] = mrow[j] < cb.M ? tab[pr.tam + mrow[j]] : -1;
+        for (int j = 0; j < R; ++j) arow[j] = mrow[j] < cb.M ? tab_at(tab, pr.tam, mrow[j]) : -1;
 #pragma unroll
-        for (int n = 0; n < NN; ++n) bcol[n] = tab[pr.tbn + n];
+        for (int n = 0; n < NN; ++n) bcol[n] = tab_at(tab, pr.tbn, n);
         for (int k = 0; k < pr.K; ++k) {
-            const int ko = tab[pr.tak + k];
-            const int64_t bk = pr.boff + tab[pr.tbk + k];
+            const int ko = tab_at(tab, pr.tak, k);
+            const int64_t bk = pr.boff + tab_at(tab, pr.tbk, k);
             double a[R];
 #pragma unroll
             for (int j = 0; j < R; ++j) a[j] = arow[j] >= 0 ? A[pr.aoff + arow[j] + ko] : 0.0;
@@ -418,9 +433,9 @@ __device__ __forceinline__ void skinny_item_direct(ItemRec const& it, CBlockRec 
 #pragma unroll
     for (int j = 0; j < R; ++j) {
         if (mrow[j] < cb.M) {
-            const int64_t crow = cb.coff + tab[cb.tcm + mrow[j]];
+            const int64_t crow = cb.coff + tab_at(tab, cb.tcm, mrow[j]);
 #pragma unroll
-            for (int n = 0; n < NN; ++n) C[crow + tab[cb.tcn + n]] = acc[j][n];
+            for (int n = 0; n < NN; ++n) C[crow + tab_at(tab, cb.tcn, n)] = acc[j][n];
         }
     }
 }
@@ -570,7 +585,8 @@ void Ctx::ensure_pin(size_t bytes) {
     sync();
     if (pin) cudaFreeHost(pin);
     pin = nullptr;
-    size_t nb = std::max<size_t>(bytes, 1 << 20);
+    // geometric growth: pinning host memory costs milliseconds per call
+    size_t nb = std::max<size_t>({bytes, size_t(1) << 20, pin_bytes + pin_bytes / 2});
     ITG_CHECK_CUDA(cudaHostAlloc(&pin, nb, cudaHostAllocMapped));
     ITG_CHECK_CUDA(cudaHostGetDevicePointer(&pin_dev, pin, 0));
     pin_bytes = nb;
@@ -625,7 +641,7 @@ void Ctx::ensure_stage(size_t bytes) {
     sync();
     if (stage) cudaFreeHost(stage);
     stage = nullptr;
-    size_t nb = std::max<size_t>(bytes, 1 << 20);
+    size_t nb = std::max<size_t>({bytes, size_t(1) << 20, stage_bytes + stage_bytes / 2});
     ITG_CHECK_CUDA(cudaHostAlloc(&stage, nb, cudaHostAllocDefault));
     stage_bytes = nb;
 }
@@ -667,15 +683,27 @@ int bits_for(int n) {
     return b;
 }
 
+// Appends the offset table of a fused index with these dims and strides
+// (first dim fastest) in the two-level form read by tab_at.
 void enum_offsets(std::vector<int32_t>& tab, std::vector<int> const& dims, std::vector<int64_t> const& strides) {
-    int n = (int)dims.size();
+    const int n = (int)dims.size();
+    int64_t P = 1, s = 1;
+    int j = 0;
+    if (n > 0) {
+        s = strides[0];
+        P = dims[0];
+        j = 1;
+        while (j < n && strides[j] == s * P) P *= dims[j++];
+    }
+    tab.push_back((int32_t)P);
+    tab.push_back((int32_t)s);
     int64_t total = 1;
-    for (int d : dims) total *= d;
+    for (int k = j; k < n; ++k) total *= dims[k];
     std::vector<int> dig(n, 0);
     int64_t off = 0;
     for (int64_t t = 0; t < total; ++t) {
         tab.push_back((int32_t)off);
-        for (int k = 0; k < n; ++k) {
+        for (int k = j; k < n; ++k) {
             off += strides[k];
             if (++dig[k] < dims[k]) break;
             off -= strides[k] * dims[k];
@@ -759,6 +787,9 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
     const int cap = (int)cap_ll;
 
     auto plan = std::make_shared<Plan>();
+    // diagnostics (ITG_PLAN_TIME): planner kernel (with its copies) and host table time per plan
+    static const bool plan_timing = std::getenv("ITG_PLAN_TIME") != nullptr;
+    auto pt0 = std::chrono::steady_clock::now();
     if (nA > 0 && nB > 0) {
         // inputs -> device (one staged copy)
         size_t o_ac = 0, o_bc = align16(o_ac + sizeof(int32_t) * std::max<size_t>(1, A.coords.size()));
@@ -811,6 +842,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         int32_t const* cnt = reinterpret_cast<int32_t const*>(hp + p_cnt);
         if (cnt[2]) throw Error(ERR_INTERNAL, "contract planner: capacity overflow");
         const int np = cnt[0], nc = cnt[1];
+        auto pt1 = std::chrono::steady_clock::now();
         std::vector<int32_t> pa(reinterpret_cast<int32_t*>(hp + p_pa), reinterpret_cast<int32_t*>(hp + p_pa) + np);
         std::vector<int32_t> pb(reinterpret_cast<int32_t*>(hp + p_pb), reinterpret_cast<int32_t*>(hp + p_pb) + np);
         std::vector<int32_t> pc(reinterpret_cast<int32_t*>(hp + p_pc), reinterpret_cast<int32_t*>(hp + p_pc) + np);
@@ -1030,6 +1062,12 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->bytes_ab = bytes_ab;
         plan->maxK = maxK;
         plan->avgK = ncb ? sumK / ncb : 0;
+        if (plan_timing) {
+            auto pt2 = std::chrono::steady_clock::now();
+            std::fprintf(stderr, "itg plan: nA %d nB %d pairs %d C %d device %.3f ms host %.3f ms\n", nA, nB, np, nc,
+                         std::chrono::duration<double, std::milli>(pt1 - pt0).count(),
+                         std::chrono::duration<double, std::milli>(pt2 - pt1).count());
+        }
     } else {
         // an empty operand: the output has no blocks (or is the scalar 0)
         auto natural = std::make_shared<Layout>();
@@ -1046,9 +1084,8 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             CBlockRec r;
             r.coff = CL.offs[c];
             r.M = (int)CL.block_size(c); r.N = 1;
-            r.tcm = (int)tab.size();
-            for (int i = 0; i < r.M; ++i) tab.push_back(i);
-            r.tcn = (int)tab.size(); tab.push_back(0);
+            r.tcm = (int)tab.size(); enum_offsets(tab, {r.M}, {1});
+            r.tcn = (int)tab.size(); enum_offsets(tab, {}, {});
             cblk.push_back(r);
             for (int m0 = 0; m0 < r.M; m0 += GEMM_TILE) items.push_back(ItemRec{c, m0, 0, 0, 0});
         }

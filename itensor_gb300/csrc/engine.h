@@ -49,6 +49,21 @@ struct ItemRec {          // one output tile (TILE x TILE) of one output block
     int32_t c, m0, n0, p0, p1;
 };
 
+// Offset tables ("table positions" above): the element offsets of a block's
+// rows (or columns, or contracted positions) in enumeration order, stored as
+// tab[pos] = P, tab[pos+1] = s, then hi[0..]: entry m = (m mod P) * s + hi[m / P].
+// P covers the leading dimensions that are contiguous in units of s, so a
+// block whose fused dimensions are all contiguous has a single hi entry and a
+// table of three integers instead of one per element.
+#ifdef __CUDACC__
+__device__ __forceinline__ int32_t tab_at(const int32_t* __restrict__ tab, int32_t pos, int32_t m) {
+    const int32_t P = __ldg(tab + pos), s = __ldg(tab + pos + 1);
+    if (m < P) return m * s + __ldg(tab + pos + 2);
+    const int32_t q = m / P;
+    return (m - q * P) * s + __ldg(tab + pos + 2 + q);
+}
+#endif
+
 constexpr int GEMM_TILE = 32;
 constexpr int OZ_PREP_ROWS = 256;   // rows per split-precision prep item (at most)
 

@@ -44,20 +44,22 @@ __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restr
                                                          const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
                                                          int64_t plane, int32_t* __restrict__ exps) {
     __shared__ int rexp[OZ_PREP_ROWS];
+    __shared__ int32_t trow[OZ_PREP_ROWS];   // offsets of this item's rows
     const PrepItem pi = items[blockIdx.x];
     const OpBlockRec ob = ops[pi.op];
     const double* __restrict__ X = pi.which ? B : A;
     const int tid = threadIdx.x;
     const int rows = pi.r1 - pi.r0;
     const int n = rows * ob.K;
-    for (int r = tid; r < rows; r += blockDim.x) rexp[r] = 0;
+    for (int r = tid; r < rows; r += blockDim.x) {
+        rexp[r] = 0;
+        trow[r] = tab_at(tab, ob.trow, pi.r0 + r);
+    }
     __syncthreads();
     const double* base = X + ob.src;
-    const int32_t* trow = tab + ob.trow + pi.r0;
-    const int32_t* tcol = tab + ob.tcol;
     for (int e = tid; e < n; e += blockDim.x) {
         int r = e % rows, k = e / rows;
-        atomicMax(&rexp[r], exp_field(base[trow[r] + tcol[k]]));
+        atomicMax(&rexp[r], exp_field(base[trow[r] + tab_at(tab, ob.tcol, k)]));
     }
     __syncthreads();
     for (int r = tid; r < rows; r += blockDim.x) exps[ob.exp + pi.r0 + r] = rexp[r] - 1022;  // |x| < 2^(E-1022)
@@ -65,7 +67,7 @@ __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restr
     __nv_bfloat16* pan = panels + ob.panel + (int64_t)pi.r0 * ob.Kp;
     for (int e = tid; e < np; e += blockDim.x) {
         int k = e % ob.Kp, r = e / ob.Kp;
-        double x = (k < ob.K) ? base[trow[r] + tcol[k]] : 0.0;
+        double x = (k < ob.K) ? base[trow[r] + tab_at(tab, ob.tcol, k)] : 0.0;
         long long bits = __double_as_longlong(x);
         int ef = (int)((bits >> 52) & 0x7FF);
         unsigned long long Xf = 0;
@@ -273,7 +275,7 @@ __device__ __forceinline__ void oz_tile(ItemRec const& it, const PairRec* __rest
         for (int q = 0; q < 4; ++q) {
             const int m = it.m0 + wm + g + (q >= 2 ? 8 : 0);
             const int n = it.n0 + wn + j * 8 + tg * 2 + (q & 1);
-            if (m < cb.M && n < cb.N) C[cb.coff + tab[cb.tcm + m] + tab[cb.tcn + n]] = out[j][q];
+            if (m < cb.M && n < cb.N) C[cb.coff + tab_at(tab, cb.tcm, m) + tab_at(tab, cb.tcn, n)] = out[j][q];
         }
 }
 
