@@ -565,8 +565,34 @@ Ctx::Ctx(int dev) : device(dev) {
     ITG_CHECK_CUDA(cudaEventCreateWithFlags(&sync_event, cudaEventDisableTiming));
 }
 
+cudaStream_t Ctx::side_stream(int i) {
+    if (!side[i]) {
+        ITG_CHECK_CUDA(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking));
+        ITG_CHECK_CUDA(cudaEventCreateWithFlags(&side_done[i], cudaEventDisableTiming));
+    }
+    return side[i];
+}
+
+void Ctx::fork() {
+    if (!fork_event) ITG_CHECK_CUDA(cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming));
+    ITG_CHECK_CUDA(cudaEventRecord(fork_event, stream));
+    for (int i = 0; i < NSIDE; ++i) ITG_CHECK_CUDA(cudaStreamWaitEvent(side_stream(i), fork_event, 0));
+}
+
+void Ctx::join(int nused) {
+    for (int i = 0; i < nused; ++i) {
+        ITG_CHECK_CUDA(cudaEventRecord(side_done[i], side[i]));
+        ITG_CHECK_CUDA(cudaStreamWaitEvent(stream, side_done[i], 0));
+    }
+}
+
 Ctx::~Ctx() {
     if (stream) cudaStreamSynchronize(stream);
+    for (int i = 0; i < NSIDE; ++i) {
+        if (side[i]) { cudaStreamSynchronize(side[i]); cudaStreamDestroy(side[i]); }
+        if (side_done[i]) cudaEventDestroy(side_done[i]);
+    }
+    if (fork_event) cudaEventDestroy(fork_event);
     for (auto& r : prof) { cudaEventDestroy(r.start); cudaEventDestroy(r.stop); }
     plans.reset();
     split_scratch.reset();

@@ -19,7 +19,9 @@
 //      host core runs it in nanoseconds per operation. It only records the plane
 //      rotations, while the device forms Q;
 //   4. tri_rot_kernel: the recorded rotations applied to the rows of Q (rows
-//      transform independently: a tile of rows per CTA, in shared memory);
+//      transform independently: a tile of rows per CTA, in shared memory; the
+//      CTA's eight warps apply rotations of eight sweeps at once, on a
+//      lockstep schedule from the host that keeps them on disjoint columns);
 //   5. tri_out_kernel: eigenvalues sorted descending, eigenvector columns moved
 //      with them.
 // The FP64 work is ~n^3 FMA for the reduction, ~2n^3/3 for Q and ~n^2 rotations
@@ -44,6 +46,7 @@ namespace itg {
 namespace {
 constexpr int TRI_THREADS = 256;
 constexpr int TRI_FORMQ_WARPS = 4;
+constexpr int TRI_ROT_WARPS = 8;         // sweeps applied at once to one row tile
 constexpr size_t TRI_SMEM_LIMIT = 200 * 1024;
 
 struct TriJob {
@@ -222,52 +225,73 @@ struct QlOut {
     int64_t eig_off;   // eigenvalues (unsorted, doubles)
     int64_t hdr_off;   // sweeps (QlSweep = int4: l, m, rotation offset, 0)
     int64_t rot_off;   // rotations (QlRot = double2: c, s)
-    int32_t nsweeps, status;
+    int64_t sched_off; // TRI_ROT_WARPS + 1 entry offsets, then entries (QlStart = int2: start step, sweep)
+    int32_t nsweeps, status, nsteps, pad;
 };
 
-// The logged rotations applied to rows r0..r0+R-1 of Q (one thread per row;
-// the tile lives in shared memory as tile[col * R + row]). A QL sweep on
-// columns l..m runs i = m-1 down to l: (z_i, z_{i+1}) <- (c z_i - s z_{i+1}, s z_i + c z_{i+1}),
-// the updated z_i carried into the next rotation.
-__global__ void tri_rot_kernel(RowJob const* __restrict__ rjobs, TriJob const* __restrict__ jobs,
-                               double* __restrict__ scratch, QlOut const* __restrict__ qo,
-                               char const* __restrict__ blob) {
+// The recorded rotations applied to rows r0..r0+R-1 of Q (the tile lives in
+// shared memory as tile[col * R + row], lane = row). The CTA's warps apply
+// rotations of different QL sweeps at once, in lockstep: at step s a warp
+// applies rotation s - S of its current sweep (started at step S), and the
+// host's schedule keeps every sweep at least two columns behind the earlier
+// sweeps it shares columns with, so the rotations of one step touch disjoint
+// column pairs and each column sees its rotations in the recorded order.
+// Rotation i of a sweep: (z_i, z_{i+1}) <- (c z_i - s z_{i+1}, s z_i + c z_{i+1}).
+__global__ void __launch_bounds__(TRI_ROT_WARPS * 32) tri_rot_kernel(RowJob const* __restrict__ rjobs,
+                                                                     TriJob const* __restrict__ jobs,
+                                                                     double* __restrict__ scratch,
+                                                                     QlOut const* __restrict__ qo,
+                                                                     char const* __restrict__ blob, int R) {
     extern __shared__ double tile[];
     const RowJob rj = rjobs[blockIdx.x];
     const TriJob jb = jobs[rj.job];
     const QlOut o = qo[rj.job];
     if (o.status != 0) return;
-    const int n = jb.n, R = blockDim.x;
+    const int n = jb.n;
     const int rows = min(R, n - rj.r0);
     double* Q = scratch + jb.s_off + (size_t)n * n;
-    for (int idx = threadIdx.x; idx < n * R; idx += R) {
+    for (int idx = threadIdx.x; idx < n * R; idx += blockDim.x) {
         const int c = idx / R, r = idx % R;
         if (r < rows) tile[idx] = Q[(size_t)c * n + rj.r0 + r];
     }
     __syncthreads();
-    const int r = threadIdx.x;
-    if (r < rows) {
-        int4 const* hd = reinterpret_cast<int4 const*>(blob + o.hdr_off);
-        double2 const* lg = reinterpret_cast<double2 const*>(blob + o.rot_off);
-        for (int it = 0; it < o.nsweeps; ++it) {
-            const int4 h = __ldg(hd + it);
-            const int l = h.x, m = h.y;
-            double2 const* cs = lg + h.z;
-            double carry = tile[m * R + r];
-            // one dependent FMA per rotation: c z_i and s z_i do not wait for the carry
-#pragma unroll 4
-            for (int i = m - 1; i >= l; --i) {
-                const double2 q = __ldg(cs + (m - 1 - i));
-                const double zi = tile[i * R + r];
-                const double czi = q.x * zi, szi = q.y * zi;
-                tile[(i + 1) * R + r] = fma(q.x, carry, szi);
-                carry = fma(-q.y, carry, czi);
-            }
-            tile[l * R + r] = carry;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int4 const* hd = reinterpret_cast<int4 const*>(blob + o.hdr_off);
+    double2 const* lg = reinterpret_cast<double2 const*>(blob + o.rot_off);
+    int32_t const* woff = reinterpret_cast<int32_t const*>(blob + o.sched_off);
+    int2 const* ent = reinterpret_cast<int2 const*>(blob + o.sched_off + 8 * ((TRI_ROT_WARPS + 2) / 2));
+    int e = __ldg(woff + warp);
+    const int e_end = __ldg(woff + warp + 1);
+    int S = 0, len = 0, m = 0, off = 0;
+    bool have = false;
+    auto fetch = [&]() {
+        have = e < e_end;
+        if (have) {
+            const int2 x = __ldg(ent + e);
+            const int4 h = __ldg(hd + x.y);
+            S = x.x;
+            m = h.y;
+            len = h.y - h.x;
+            off = h.z;
         }
+    };
+    fetch();
+    const bool row_ok = lane < rows;
+    for (int s = 0; s < o.nsteps; ++s) {
+        if (have && s >= S + len) {
+            ++e;
+            fetch();
+        }
+        if (have && s >= S && row_ok) {
+            const int j = s - S, i = m - 1 - j;
+            const double2 q = __ldg(lg + off + j);
+            const double a = tile[i * R + lane], b = tile[(i + 1) * R + lane];
+            tile[(i + 1) * R + lane] = fma(q.y, a, q.x * b);
+            tile[i * R + lane] = fma(q.x, a, -q.y * b);
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < n * R; idx += R) {
+    for (int idx = threadIdx.x; idx < n * R; idx += blockDim.x) {
         const int c = idx / R, rr = idx % R;
         if (rr < rows) Q[(size_t)c * n + rj.r0 + rr] = tile[idx];
     }
@@ -320,10 +344,9 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
     int nmax = 0;
     for (auto const& it : items) nmax = std::max(nmax, it.n);
     ITG_REQUIRE(nmax <= TRI_MAX_N, "tri_eigh: block larger than the tridiagonal path supports");
-    // rows per tile of the rotation pass: a quarter warp (the FP64 pipe, not the
-    // lanes, bounds a tile; smaller tiles spread a block over more SMs), fewer
-    // when shared memory runs out
-    int R = 8;
+    // rows per tile of the rotation pass (lane = row): a full warp, fewer when
+    // shared memory runs out
+    int R = 32;
     if (char const* env = std::getenv("ITG_TRI_ROWS")) R = std::max(1, std::min(32, std::atoi(env)));
     while (R > 1 && sizeof(double) * (size_t)R * nmax > TRI_SMEM_LIMIT) R /= 2;
     std::vector<TriJob> jobs(nj);
@@ -377,7 +400,18 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
             ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_reduce_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem));
         ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_reduce_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-        int b = 0;
+        // one launch per cluster size; the launches are independent, so they
+        // run side by side on the context's side streams
+        int ngroups = 0;
+        for (int b = 0; b < nj;) {
+            int e = b;
+            while (e < nj && cluster_for(items[e].n) == cluster_for(items[b].n)) ++e;
+            ++ngroups;
+            b = e;
+        }
+        const bool fan = ngroups > 1;
+        if (fan) ctx.fork();
+        int g = 0, b = 0;
         while (b < nj) {
             const int C = cluster_for(items[b].n);
             int e = b;
@@ -386,7 +420,7 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
             cfg.gridDim = dim3((unsigned)((e - b) * C));
             cfg.blockDim = dim3(TRI_THREADS);
             cfg.dynamicSmemBytes = smem;
-            cfg.stream = ctx.stream;
+            cfg.stream = fan ? ctx.side_stream(g % Ctx::NSIDE) : ctx.stream;
             cudaLaunchAttribute attr[1];
             attr[0].id = cudaLaunchAttributeClusterDimension;
             attr[0].val.clusterDim.x = (unsigned)C;
@@ -397,7 +431,9 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
             ITG_CHECK_CUDA(cudaLaunchKernelEx(&cfg, tri_reduce_kernel, d_jobs + b, src, scratch, d_aux));
             ctx.kernel_launches++;
             b = e;
+            ++g;
         }
+        if (fan) ctx.join(std::min(ngroups, (int)Ctx::NSIDE));
     }
     // (d, e) of every block to the host; Q is formed on the device meanwhile
     const size_t aux_bytes = sizeof(double) * aux_tot;
@@ -432,12 +468,16 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
     // run one solve each) large passes use a few host threads
     std::vector<std::vector<QlSweep>> bsw(nj);
     std::vector<std::vector<QlRot>> brot(nj);
-    std::vector<int> bst(nj, 0);
+    std::vector<std::vector<int32_t>> bwoff(nj);
+    std::vector<std::vector<QlStart>> bent(nj);
+    std::vector<int> bst(nj, 0), bsteps(nj, 0);
     auto run_block = [&](int b) {
         const int n = items[b].n;
         double* d = de.data() + jobs[b].aux_off;
         bst[b] = tridiag_ql(n, d, d + n, bsw[b], brot[b]);
         eigs[b].assign(d, d + n);
+        if (bst[b] == 0) bsteps[b] = ql_schedule(n, bsw[b], TRI_ROT_WARPS, bwoff[b], bent[b]);
+        else bwoff[b].assign(TRI_ROT_WARPS + 1, 0);
     };
     double work = 0;
     for (auto const& it : items) work += (double)it.n * it.n;
@@ -454,14 +494,24 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
         for (int b = 0; b < nj; ++b) run_block(b);
     }
     int bad = 0;
+    std::vector<int32_t> sched;   // per block: woff (padded to 8 bytes), then entries as int pairs
     for (int b = 0; b < nj; ++b) {
         qo[b].status = bst[b];
         bad += (bst[b] != 0);
         qo[b].nsweeps = (int32_t)bsw[b].size();
+        qo[b].nsteps = bsteps[b];
+        qo[b].pad = 0;
         qo[b].hdr_off = (int64_t)sweeps.size();   // element offsets for now
         qo[b].rot_off = (int64_t)rots.size();
+        qo[b].sched_off = (int64_t)sched.size();
         sweeps.insert(sweeps.end(), bsw[b].begin(), bsw[b].end());
         rots.insert(rots.end(), brot[b].begin(), brot[b].end());
+        sched.insert(sched.end(), bwoff[b].begin(), bwoff[b].end());
+        for (int k = TRI_ROT_WARPS + 1; k < 2 * ((TRI_ROT_WARPS + 2) / 2); ++k) sched.push_back(0);
+        for (auto const& x : bent[b]) {
+            sched.push_back(x.step);
+            sched.push_back(x.sweep);
+        }
     }
     auto th1 = std::chrono::steady_clock::now();
     // blob: QlOut table | eigenvalues | sweeps | rotations
@@ -469,13 +519,15 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
     for (int b = 0; b < nj; ++b) eig_tot += items[b].n;
     const size_t b_qo = 0, b_eig = a16(sizeof(QlOut) * nj), b_hdr = a16(b_eig + sizeof(double) * eig_tot);
     const size_t b_rot = a16(b_hdr + sizeof(QlSweep) * sweeps.size());
-    const size_t blob_bytes = a16(b_rot + sizeof(QlRot) * rots.size());
+    const size_t b_sched = a16(b_rot + sizeof(QlRot) * rots.size());
+    const size_t blob_bytes = a16(b_sched + sizeof(int32_t) * sched.size());
     {
         int64_t eo = 0;
         for (int b = 0; b < nj; ++b) {
             qo[b].eig_off = (int64_t)(b_eig + sizeof(double) * eo);
             qo[b].hdr_off = (int64_t)(b_hdr + sizeof(QlSweep) * qo[b].hdr_off);
             qo[b].rot_off = (int64_t)(b_rot + sizeof(QlRot) * qo[b].rot_off);
+            qo[b].sched_off = (int64_t)(b_sched + sizeof(int32_t) * qo[b].sched_off);
             eo += items[b].n;
         }
     }
@@ -491,6 +543,7 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
     }
     if (!sweeps.empty()) std::memcpy(st + b_hdr, sweeps.data(), sizeof(QlSweep) * sweeps.size());
     if (!rots.empty()) std::memcpy(st + b_rot, rots.data(), sizeof(QlRot) * rots.size());
+    if (!sched.empty()) std::memcpy(st + b_sched, sched.data(), sizeof(int32_t) * sched.size());
     DevBuf blob(blob_bytes, ctx.stream);
     ITG_CHECK_CUDA(cudaMemcpyAsync(blob.p, st, blob_bytes, cudaMemcpyHostToDevice, ctx.stream));
     QlOut const* d_qo = reinterpret_cast<QlOut const*>(blob.as<char>() + b_qo);
@@ -500,7 +553,8 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
         const size_t smem = sizeof(double) * (size_t)R * nmax;
         if (smem > 48 * 1024)
             ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_rot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        tri_rot_kernel<<<(int)rjobs.size(), R, smem, ctx.stream>>>(d_rj, d_jobs, scratch, d_qo, blob.as<char>());
+        tri_rot_kernel<<<(int)rjobs.size(), TRI_ROT_WARPS * 32, smem, ctx.stream>>>(d_rj, d_jobs, scratch, d_qo,
+                                                                                   blob.as<char>(), R);
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;
     }

@@ -159,6 +159,16 @@ struct Ctx {
     // partial sums + completion counter of the fused reductions (ops.cu)
     DevBufPtr reduce_buf;
     void ensure_reduce();
+    // side streams for independent launches inside one operation (created on
+    // first use; work forked to them is joined back before the operation
+    // returns, and uses only buffers allocated on `stream` before the fork)
+    static constexpr int NSIDE = 4;
+    cudaStream_t side[NSIDE] = {};
+    cudaEvent_t side_done[NSIDE] = {};
+    cudaEvent_t fork_event = nullptr;
+    cudaStream_t side_stream(int i);
+    void fork();                 // side streams wait for the work enqueued on `stream` so far
+    void join(int nused);        // `stream` waits for side streams 0..nused-1
     // counters
     uint64_t kernel_launches = 0;
     uint64_t plans_built = 0, plan_hits = 0;

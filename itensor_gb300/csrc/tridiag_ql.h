@@ -17,4 +17,15 @@ struct QlRot { double c, s; };
 // eigenvalue needed more than 30 sweeps.
 int tridiag_ql(int n, double* d, double* e, std::vector<QlSweep>& sweeps, std::vector<QlRot>& rots);
 
+// Lockstep schedule for applying the recorded sweeps with `workers` workers
+// that each apply one rotation per step: every sweep starts at the earliest
+// step at which each of its rotations comes after all rotations of earlier
+// sweeps that share a column (rotations on disjoint column pairs commute), on
+// the worker that is free first. Fills the per-worker entry lists (start step,
+// sweep index), entries of worker w at [woff[w], woff[w+1]), and returns the
+// number of steps.
+struct QlStart { int32_t step, sweep; };
+int ql_schedule(int n, std::vector<QlSweep> const& sweeps, int workers, std::vector<int32_t>& woff,
+                std::vector<QlStart>& entries);
+
 }  // namespace itg
