@@ -423,12 +423,12 @@ def run_cylinder(args):
     the split precision and in plain FP64 on the same sweep table; reports both
     energies, their difference, sweep times and the phase split."""
     import itensor_gb300 as itg
-    ctx = itg.Context(0)
     model = dict(type=2, Lx=16, Ly=4, t=1.0, U=4.0, yperiodic=1)
     sw = cylinder_sweeps(args.cylinder)
     out = {"workload": "hubbard_4x16_cylinder", "t": 1.0, "U": 4.0, "sweeps": sw}
     runs = [(n, {"split": itg.PREC_OZAKI_BF16, "fp64": itg.PREC_F64}[n]) for n in args.cyl_runs.split(",")]
     for name, prec in runs:
+        ctx = itg.Context(0)   # a fresh context each: no contraction plans carried over
         clk = ClockSampler(0)
         clk.start()
         t0 = time.perf_counter()
@@ -438,11 +438,11 @@ def run_cylinder(args):
                      "phase_seconds": r.phase_seconds, "max_link_dim": max(sum(int(x) for x in d) for _, _, d in r.links),
                      "last_sweep_truncerr_max": max(b[4] for b in r.bonds[-(2 * (64 - 1)):]),
                      "clocks": clk.stop()}
+        ctx.close()
         print(json.dumps({name: out[name]}), flush=True)
     if "fp64" in out and "split" in out:
         out["energy_diff_split_vs_fp64"] = out["split"]["energy"] - out["fp64"]["energy"]
     print(json.dumps(out))
-    ctx.close()
     return 0
 
 
