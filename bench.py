@@ -446,6 +446,21 @@ def run_cylinder(args):
     return 0
 
 
+def run_profile_cylinder(args):
+    """One cylinder solve for ncu's launch list: the Hubbard 4x16 cylinder on
+    the sweep table of run_cylinder up to maxdim `--profile-cylinder`, split
+    precision, one context."""
+    import itensor_gb300 as itg
+    ctx = itg.Context(0)
+    t0 = time.perf_counter()
+    r = ctx.dmrg(dict(type=2, Lx=16, Ly=4, t=1.0, U=4.0, yperiodic=1), cylinder_sweeps(args.profile_cylinder),
+                 precision=itg.PREC_OZAKI_BF16)
+    print(json.dumps({"energy": r.energy, "bond_steps": len(r.bonds), "seconds": time.perf_counter() - t0,
+                      "phase_seconds": r.phase_seconds, "stats": ctx.stats()}))
+    ctx.close()
+    return 0
+
+
 def run_profile(args):
     """Short run of the same workload for ncu: for the split form and plain
     FP64, N prepared applies each (kernels launched one by one)."""
@@ -486,6 +501,8 @@ def main():
     ap.add_argument("--cylinder", type=int, default=0,
                     help="Hubbard 4x16 cylinder DMRG up to this maxdim (3000 in the workload), split and FP64")
     ap.add_argument("--cyl-runs", default="split,fp64", help="with --cylinder: which arithmetics to run")
+    ap.add_argument("--profile-cylinder", type=int, default=0,
+                    help="profiling run for ncu: one cylinder solve up to this maxdim, split precision")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -495,6 +512,8 @@ def main():
         return run_profile_dmrg(args)
     if args.cylinder:
         return run_cylinder(args)
+    if args.profile_cylinder:
+        return run_profile_cylinder(args)
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
 
