@@ -47,6 +47,7 @@ namespace {
 constexpr int TRI_THREADS = 256;
 constexpr int TRI_FORMQ_WARPS = 4;
 constexpr int TRI_ROT_WARPS = 8;         // sweeps applied at once to one row tile
+constexpr int TRI_ROT_WINDOW = 4;        // lockstep steps between barriers
 constexpr size_t TRI_SMEM_LIMIT = 200 * 1024;
 
 struct TriJob {
@@ -67,33 +68,43 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Sum over the CTA (fixed order: lanes, then warps in order); every thread gets it.
+// Sum over the CTA (a fixed tree: lanes, then the warps' sums); every thread
+// gets the same value. The warps' sums are combined by shuffles, not by a
+// serial loop in every warp: each FP64 instruction costs a warp tens of cycles.
 __device__ double cta_sum(double v, double* red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     v = warp_sum(v);
     __syncthreads();
     if (lane == 0) red[warp] = v;
     __syncthreads();
-    double s = 0.0;
-    for (int w = 0; w < nw; ++w) s += red[w];
-    return s;
+    double s = lane < nw ? red[lane] : 0.0;
+    for (int o = 4; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);   // nw <= 8
+    return __shfl_sync(0xffffffffu, s, 0);
 }
 
 // Householder reflector for column k (rows k+1..n-1), dlarfg's convention:
 // H = I - tau v v^T with v[k+1] = 1 and H [alpha; x] = [beta; 0]. Run by every
 // thread of the owning CTA.
 __device__ void tri_reflector(int k, int n, double* A, double* d, double* e, double* tau, double* vg, double* red) {
+    __shared__ double sc[3];   // beta, tau, 1 / (alpha - beta): computed once, by thread 0
     double* col = A + (size_t)k * n;
     const double alpha = col[k + 1];
     double ss = 0.0;
     for (int i = k + 2 + threadIdx.x; i < n; i += blockDim.x) ss = fma(col[i], col[i], ss);
     ss = cta_sum(ss, red);
-    double t = 0.0, beta = alpha, scal = 0.0;
-    if (ss > 0.0) {
-        beta = -copysign(sqrt(fma(alpha, alpha, ss)), alpha);
-        t = (beta - alpha) / beta;
-        scal = 1.0 / (alpha - beta);
+    if (threadIdx.x == 0) {
+        double t = 0.0, beta = alpha, scal = 0.0;
+        if (ss > 0.0) {
+            beta = -copysign(sqrt(fma(alpha, alpha, ss)), alpha);
+            t = (beta - alpha) / beta;
+            scal = 1.0 / (alpha - beta);
+        }
+        sc[0] = beta;
+        sc[1] = t;
+        sc[2] = scal;
     }
+    __syncthreads();
+    const double beta = sc[0], t = sc[1], scal = sc[2];
     for (int i = k + 2 + threadIdx.x; i < n; i += blockDim.x) {
         const double v = col[i] * scal;
         col[i] = v;
@@ -157,9 +168,10 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_reduce_kernel(TriJob const* _
         if (threadIdx.x == 0) __stcg(part + rank, psum);
         cl.sync();
         if (tk != 0.0) {
-            double K = 0.0;
-            for (int r = 0; r < C; ++r) K += __ldcg(part + r);
-            K *= -0.5 * tk;
+            // sum of the C partial dot products, as a shuffle tree (C <= 16)
+            double K = lane < C ? __ldcg(part + lane) : 0.0;
+            for (int o = 8; o > 0; o >>= 1) K += __shfl_xor_sync(0xffffffffu, K, o);
+            K = __shfl_sync(0xffffffffu, K, 0) * (-0.5 * tk);
             for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) ws[i] = fma(K, vs[i], __ldcg(pg + i));
             __syncthreads();
             for (int j = j0 + warp * C; j < n; j += nw * C) {
@@ -232,10 +244,10 @@ struct QlOut {
 // The recorded rotations applied to rows r0..r0+R-1 of Q (the tile lives in
 // shared memory as tile[col * R + row], lane = row). The CTA's warps apply
 // rotations of different QL sweeps at once, in lockstep: at step s a warp
-// applies rotation s - S of its current sweep (started at step S), and the
-// host's schedule keeps every sweep at least two columns behind the earlier
-// sweeps it shares columns with, so the rotations of one step touch disjoint
-// column pairs and each column sees its rotations in the recorded order.
+// applies rotation s - S of its current sweep (started at step S), with a
+// barrier every TRI_ROT_WINDOW steps; the host's schedule keeps the sweeps
+// far enough apart that the warps of one window touch disjoint columns, so
+// each column sees its rotations in the recorded order.
 // Rotation i of a sweep: (z_i, z_{i+1}) <- (c z_i - s z_{i+1}, s z_i + c z_{i+1}).
 __global__ void __launch_bounds__(TRI_ROT_WARPS * 32) tri_rot_kernel(RowJob const* __restrict__ rjobs,
                                                                      TriJob const* __restrict__ jobs,
@@ -277,17 +289,23 @@ __global__ void __launch_bounds__(TRI_ROT_WARPS * 32) tri_rot_kernel(RowJob cons
     };
     fetch();
     const bool row_ok = lane < rows;
-    for (int s = 0; s < o.nsteps; ++s) {
-        if (have && s >= S + len) {
-            ++e;
-            fetch();
-        }
-        if (have && s >= S && row_ok) {
-            const int j = s - S, i = m - 1 - j;
-            const double2 q = __ldg(lg + off + j);
-            const double a = tile[i * R + lane], b = tile[(i + 1) * R + lane];
-            tile[(i + 1) * R + lane] = fma(q.y, a, q.x * b);
-            tile[i * R + lane] = fma(q.x, a, -q.y * b);
+    // TRI_ROT_WINDOW steps between barriers: the schedule puts every rotation in
+    // a later window than the other warps' earlier rotations on its columns
+    for (int s0 = 0; s0 < o.nsteps; s0 += TRI_ROT_WINDOW) {
+#pragma unroll
+        for (int u = 0; u < TRI_ROT_WINDOW; ++u) {
+            const int s = s0 + u;
+            if (have && s >= S + len) {
+                ++e;
+                fetch();
+            }
+            if (have && s >= S && row_ok) {
+                const int j = s - S, i = m - 1 - j;
+                const double2 q = __ldg(lg + off + j);
+                const double a = tile[i * R + lane], b = tile[(i + 1) * R + lane];
+                tile[(i + 1) * R + lane] = fma(q.y, a, q.x * b);
+                tile[i * R + lane] = fma(q.x, a, -q.y * b);
+            }
         }
         __syncthreads();
     }
@@ -476,7 +494,7 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
         double* d = de.data() + jobs[b].aux_off;
         bst[b] = tridiag_ql(n, d, d + n, bsw[b], brot[b]);
         eigs[b].assign(d, d + n);
-        if (bst[b] == 0) bsteps[b] = ql_schedule(n, bsw[b], TRI_ROT_WARPS, bwoff[b], bent[b]);
+        if (bst[b] == 0) bsteps[b] = ql_schedule(n, bsw[b], TRI_ROT_WARPS, TRI_ROT_WINDOW, bwoff[b], bent[b]);
         else bwoff[b].assign(TRI_ROT_WARPS + 1, 0);
     };
     double work = 0;

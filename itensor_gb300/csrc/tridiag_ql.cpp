@@ -70,26 +70,33 @@ int tridiag_ql(int n, double* d, double* e, std::vector<QlSweep>& sweeps, std::v
     return 0;
 }
 
-int ql_schedule(int n, std::vector<QlSweep> const& sweeps, int workers, std::vector<int32_t>& woff,
+int ql_schedule(int n, std::vector<QlSweep> const& sweeps, int workers, int window, std::vector<int32_t>& woff,
                 std::vector<QlStart>& entries) {
-    // last[c]: last step at which column c is rotated (-1: never)
-    std::vector<int64_t> last(std::max(n, 1) + 1, -1);
+    // per column: window of its last rotation and the worker that applied it
+    std::vector<int64_t> last_win(std::max(n, 1) + 1, -1);
+    std::vector<int> last_worker(std::max(n, 1) + 1, -1);
     std::vector<int64_t> free_at(workers, 0);
     std::vector<std::vector<QlStart>> per(workers);
     int64_t nsteps = 0;
     for (size_t t = 0; t < sweeps.size(); ++t) {
         const int l = sweeps[t].l, m = sweeps[t].m;
-        // rotation i (columns i, i+1) runs at step S + (m - 1 - i)
-        int64_t S = 0;
-        for (int i = l; i < m; ++i) S = std::max(S, std::max(last[i], last[i + 1]) + 1 - (m - 1 - i));
         int w = 0;
         for (int k = 1; k < workers; ++k)
             if (free_at[k] < free_at[w]) w = k;
-        S = std::max(S, free_at[w]);
+        // rotation i (columns i, i+1) runs at step S + (m - 1 - i); it must fall in
+        // a later window than the last rotation on either column by another worker
+        // (a worker's own rotations are ordered by its program)
+        int64_t S = free_at[w];
+        for (int i = l; i < m; ++i)
+            for (int c = i; c <= i + 1; ++c)
+                if (last_worker[c] >= 0 && last_worker[c] != w)
+                    S = std::max(S, (last_win[c] + 1) * window - (m - 1 - i));
         for (int i = m - 1; i >= l; --i) {
-            const int64_t step = S + (m - 1 - i);
-            last[i] = std::max(last[i], step);
-            last[i + 1] = std::max(last[i + 1], step);
+            const int64_t win = (S + (m - 1 - i)) / window;
+            for (int c = i; c <= i + 1; ++c) {
+                last_win[c] = std::max(last_win[c], win);
+                last_worker[c] = w;
+            }
         }
         free_at[w] = S + (m - l);
         nsteps = std::max(nsteps, free_at[w]);
@@ -102,7 +109,7 @@ int ql_schedule(int n, std::vector<QlSweep> const& sweeps, int workers, std::vec
         entries.insert(entries.end(), per[w].begin(), per[w].end());
     }
     woff[workers] = (int32_t)entries.size();
-    return (int)nsteps;
+    return (int)((nsteps + window - 1) / window * window);
 }
 
 }  // namespace itg

@@ -18,14 +18,15 @@ struct QlRot { double c, s; };
 int tridiag_ql(int n, double* d, double* e, std::vector<QlSweep>& sweeps, std::vector<QlRot>& rots);
 
 // Lockstep schedule for applying the recorded sweeps with `workers` workers
-// that each apply one rotation per step: every sweep starts at the earliest
-// step at which each of its rotations comes after all rotations of earlier
-// sweeps that share a column (rotations on disjoint column pairs commute), on
-// the worker that is free first. Fills the per-worker entry lists (start step,
-// sweep index), entries of worker w at [woff[w], woff[w+1]), and returns the
-// number of steps.
+// that each apply one rotation per step, with a barrier after every `window`
+// steps: every sweep starts at the earliest step at which each of its
+// rotations falls in a later window than all rotations of earlier sweeps on
+// another worker that share a column (rotations on disjoint column pairs
+// commute), on the worker that is free first. Fills the per-worker entry
+// lists (start step, sweep index), entries of worker w at
+// [woff[w], woff[w+1]), and returns the number of steps (a whole number of windows).
 struct QlStart { int32_t step, sweep; };
-int ql_schedule(int n, std::vector<QlSweep> const& sweeps, int workers, std::vector<int32_t>& woff,
+int ql_schedule(int n, std::vector<QlSweep> const& sweeps, int workers, int window, std::vector<int32_t>& woff,
                 std::vector<QlStart>& entries);
 
 }  // namespace itg
