@@ -7,6 +7,9 @@ Restates:
   * LocalMPO position/makeL/makeR itensor/mps/localmpo.h:443-470, 542-618
   * MPS::svdBond                  itensor/mps/mps_impl.h:21-99
   * DMRGWorker / sweepnext        itensor/mps/dmrg.h:336-467, itensor/mps/sweeps.h:489-503
+  * LocalMPO of an MPS, LocalMPO_MPS (excited states)
+                                  itensor/mps/localmpo.h:340-349, 389-421, 543-594;
+                                  itensor/mps/localmpo_mps.h:98-156; itensor/mps/dmrg.h:245-266
 """
 from __future__ import annotations
 
@@ -180,6 +183,77 @@ class LocalMPO:
         return LocalOp(self.W[b - 1], self.W[b], L, R)
 
 
+class LocalMPS:
+    """LocalMPO built from a previously found state psi_j: environments of
+    <psi_j|psi> (makeL/makeR with dag(prime(psi_j(k), "Link"))) and, at bond b,
+    the projection of phi onto psi_j's two-site tensor: phip = dag(othr) (othr * phi)."""
+
+    def __init__(self, psij, site_ids):
+        self.P = list(psij)
+        self.N = len(psij)
+        self.sites = set(site_ids)
+        self.PH = [None] * (self.N + 2)
+        self.LHlim = 0
+        self.RHlim = self.N + 1
+        self.b = None
+
+    def _dagp(self, k):
+        """dag(prime(psi_j(k), "Link")) for site k (1-based): every index but the site primed."""
+        A = self.P[k - 1]
+        return A.dag().prime(which={I.id for I in A.inds if I.id not in self.sites})
+
+    def makeL(self, psi, k):
+        while self.LHlim < k:
+            ll = self.LHlim
+            E = psi[ll] if self.PH[ll] is None else contract(self.PH[ll], psi[ll])
+            self.PH[ll + 1] = contract(E, self._dagp(ll + 1))
+            self.LHlim = ll + 1
+
+    def makeR(self, psi, k):
+        while self.RHlim > k:
+            rl = self.RHlim
+            E = psi[rl - 2] if self.PH[rl] is None else contract(self.PH[rl], psi[rl - 2])
+            self.PH[rl - 1] = contract(E, self._dagp(rl - 1))
+            self.RHlim = rl - 1
+
+    def position(self, b, psi):
+        self.makeL(psi, b - 1)
+        self.makeR(psi, b + 2)
+        self.LHlim, self.RHlim, self.b = b - 1, b + 2, b
+
+    def othr(self):
+        b = self.b
+        L = self.PH[b - 1] if b - 1 >= 1 else None
+        R = self.PH[b + 2] if b + 2 <= self.N else None
+        o = self._dagp(b) if L is None else contract(L, self._dagp(b))
+        return contract(o, self._dagp(b + 1) if R is None else contract(R, self._dagp(b + 1)))
+
+    def product(self, phi):
+        o = self.othr()
+        z = contract(o, phi).scalar
+        return o.dag().scale(z)
+
+
+class ProjectedOp:
+    """LocalMPO_MPS::product: H phi + weight * sum_j P_j phi; deltaRho and size
+    from the MPO part (itensor/mps/localmpo_mps.h:65-72, 137-150)."""
+
+    def __init__(self, op, projs, weight):
+        self.op, self.projs, self.weight = op, projs, weight
+
+    def product(self, phi):
+        p = self.op.product(phi)
+        for M in self.projs:
+            p = p + M.product(phi).scale(self.weight)
+        return p
+
+    def delta_rho(self, AA, cmb, fromleft):
+        return self.op.delta_rho(AA, cmb, fromleft)
+
+    def size(self, phi):
+        return self.op.size(phi)
+
+
 def sweep_bonds(N):
     """(b, half-sweep) sequence of sweepnext: b=1..N-1 then N-1..1."""
     out = [(b, 1) for b in range(1, N)]
@@ -187,17 +261,24 @@ def sweep_bonds(N):
     return out
 
 
-def dmrg(W, psi, sweeps, record=None, usesvd=None):
+def dmrg(W, psi, sweeps, record=None, usesvd=None, psis=None, weight=1.0, site_ids=None):
     """sweeps: list of dicts {maxdim, mindim, cutoff, niter}. psi: list of
-    site tensors (modified copy returned). Returns (energy, psi, records)."""
+    site tensors (modified copy returned). Returns (energy, psi, records).
+    psis: previously found states to stay orthogonal to (H + weight sum_j
+    |psi_j><psi_j|, itensor/mps/dmrg.h:245-266); site_ids: ids of the site indices."""
     psi = list(psi)
     N = len(psi)
     PH = LocalMPO(W)
+    projs = [LocalMPS(p, site_ids) for p in (psis or [])]
     energy = np.nan
     recs = []
     for sw, s in enumerate(sweeps, start=1):
         for b, ha in sweep_bonds(N):
             op = PH.position(b, psi)
+            if projs:
+                for M in projs:
+                    M.position(b, psi)
+                op = ProjectedOp(op, projs, weight)
             phi = contract(psi[b - 1], psi[b])
             energy, phi = davidson(op, phi, maxiter=s["niter"])
             noise = s.get("noise", 0.0)

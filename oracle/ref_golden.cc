@@ -528,6 +528,41 @@ static std::string run_dmrg(std::string const& name, SitesT const& sites, MPO co
     return o.str();
 }
 
+// Excited-state DMRG (itensor/mps/dmrg.h:245-266, LocalMPO_MPS of
+// itensor/mps/localmpo_mps.h): the ground state from `sw0`, then the state
+// that minimises H + weight |psi0><psi0| from psi_start on `sw`; records the
+// second run like run_dmrg, plus the ground run's energy and the overlap.
+template <typename SitesT>
+static std::string run_dmrg_excited(std::string const& name, SitesT const& sites, MPO const& H, MPS const& psi_start,
+                                    Sweeps const& sw0, Sweeps const& sw, double weight, std::string const& model) {
+    auto [E0, psi0] = dmrg(H, psi_start, sw0, {"Quiet", true, "Silent", true});
+    Recorder obs(psi_start);
+    auto [E, psi] = dmrg(H, std::vector<MPS>{psi0}, psi_start, sw, obs,
+                         {"Quiet", true, "Silent", true, "Weight", weight});
+    auto sweeps_json = [](Sweeps const& w) {
+        std::ostringstream o;
+        o << "[";
+        for (int s = 1; s <= w.nsweep(); ++s) {
+            if (s > 1) o << ",";
+            o << "{\"maxdim\":" << w.maxdim(s) << ",\"mindim\":" << w.mindim(s) << ",\"cutoff\":" << num(w.cutoff(s))
+              << ",\"niter\":" << w.niter(s) << ",\"noise\":" << num(w.noise(s)) << "}";
+        }
+        o << "]";
+        return o.str();
+    };
+    std::ostringstream o;
+    o << "{\"name\":\"" << name << "\",\"model\":" << model << ",\"N\":" << length(psi)
+      << ",\"ground_sweeps\":" << sweeps_json(sw0) << ",\"ground_energy\":" << num(E0) << ",\"weight\":" << num(weight)
+      << ",\"sweeps\":" << sweeps_json(sw) << ",\"energy\":" << num(E)
+      << ",\"overlap_with_ground\":" << num(inner(psi0, psi)) << ",\"bonds\":[" << obs.rec.str() << "],\"links\":[";
+    for (int b = 1; b < length(psi); ++b) { if (b > 1) o << ","; o << jindex(linkIndex(psi, b)); }
+    o << "],\"sites\":[";
+    for (int j = 1; j <= length(psi); ++j) { if (j > 1) o << ","; o << jindex(sites(j)); }
+    o << "]}";
+    std::printf("  %s: E0=%.15f E1=%.15f <0|1>=%.3e\n", name.c_str(), E0, E, inner(psi0, psi));
+    return o.str();
+}
+
 static Sweeps mksweeps(std::vector<int> maxdims, double cutoff, int niter = 2) {
     auto sw = Sweeps((int)maxdims.size());
     for (int s = 1; s <= (int)maxdims.size(); ++s) {
@@ -554,6 +589,14 @@ static void gen_dmrg(std::string const& dir) {
         swn.setnoise(2, 1e-8);
         cs.push_back(run_dmrg("heis20_noise", sites, H, neel_mps(sites, N), swn,
                               "{\"type\":\"heisenberg\",\"J\":1.0,\"Jz\":1.0}"));
+    }
+    {   // first excited state of the Heisenberg chain N=12 (Sz = 0 triplet member), weight 20
+        int N = 12;
+        auto sites = SpinHalf(N);
+        MPO H = Heisenberg(sites);
+        cs.push_back(run_dmrg_excited("heis12_excited", sites, H, neel_mps(sites, N), mksweeps({10, 20, 40, 40, 40}, 1e-10),
+                                      mksweeps({10, 20, 40, 40, 40, 40}, 1e-10), 20.0,
+                                      "{\"type\":\"heisenberg\",\"J\":1.0,\"Jz\":1.0}"));
     }
     {   // XXZ N=16, Delta=0.5
         int N = 16; double D = 0.5;

@@ -114,3 +114,23 @@ def test_dmrg_energies_and_structure(golden, name):
         link = [I for I in psi2[b].inds if psi2[b + 1].find(I) >= 0][0]
         assert link_sectors(link) == json_sectors(c["links"][b])
         assert link.dir == c["links"][b]["dir"]
+
+
+def test_dmrg_excited_state(golden):
+    """Excited-state DMRG (H + weight |psi0><psi0|, itensor/mps/dmrg.h:245-266):
+    the ground state, then the first excited state against the reference."""
+    c = [x for x in golden("dmrg")["cases"] if x["name"] == "heis12_excited"][0]
+    N = c["N"]
+    H, labels = model_from_json(c["model"], N)
+    sites, W, _ = models.build_mpo(H)
+    psi = models.product_mps(sites, H.st, labels)
+    E0, psi0, _ = dmrg(W, psi, c["ground_sweeps"])
+    assert abs(E0 - c["ground_energy"]) < ENERGY_TOL
+    E1, psi1, recs = dmrg(W, psi, c["sweeps"], psis=[psi0], weight=c["weight"], site_ids=[I.id for I in sites])
+    assert abs(E1 - c["energy"]) < ENERGY_TOL
+    assert len(recs) == len(c["bonds"])
+    for a, b in zip(recs, c["bonds"]):
+        assert tuple(a[:3]) == tuple(b[:3])
+        assert abs(a[3] - b[3]) < ENERGY_TOL
+        assert abs(a[4] - b[4]) < 1e-12
+        assert a[5] == b[5]
