@@ -237,6 +237,14 @@ typedef struct {
 
 int itg_dmrg_run(itg_ctx* ctx, const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps,
                  int precision, itg_dmrg_result** out);
+/* Excited states: dmrg(H, psis, psi0, sweeps, {"Weight", weight}) of
+ * itensor/mps/dmrg.h:245-266 with LocalMPO_MPS (itensor/mps/localmpo_mps.h),
+ * chained. State 0 is the ground state from the model's default product
+ * state on sweeps[0]; state k >= 1 minimises H + weight * sum_{j<k} |psi_j><psi_j|
+ * from the same product state on sweeps[k]. out receives nstates results
+ * (each freed with itg_dmrg_free). */
+int itg_dmrg_run_states(itg_ctx* ctx, const itg_model_desc* model, int32_t nstates, const itg_sweep_desc* const* sweeps,
+                        const int32_t* nsweeps, double weight, int precision, itg_dmrg_result** out);
 int itg_dmrg_energy(const itg_dmrg_result* r, double* energy);
 int itg_dmrg_nbonds(const itg_dmrg_result* r, int32_t* nbonds);
 int itg_dmrg_bonds(const itg_dmrg_result* r, int32_t* sweep, int32_t* halfsweep, int32_t* bond, double* energy,

@@ -100,6 +100,8 @@ SIGNATURES = {
                                 C.POINTER(C.c_void_p), _f64p, _f64p, _i32p]),
     "itg_truncate": (C.c_int, [_f64p, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int, C.c_int, C.c_int, _f64p,
                                _i32p, _f64p, _f64p, _f64p, _i32p]),
+    "itg_dmrg_run_states": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.c_int32, C.POINTER(C.POINTER(SweepDesc)),
+                                      _i32p, C.c_double, C.c_int, C.POINTER(C.c_void_p)]),
     "itg_dmrg_run": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.POINTER(SweepDesc), C.c_int32, C.c_int,
                                C.POINTER(C.c_void_p)]),
     "itg_dmrg_energy": (C.c_int, [C.c_void_p, _f64p]),
@@ -485,6 +487,20 @@ class Context:
         out = C.c_void_p()
         self._ok(lib().itg_dmrg_run(self.h, C.byref(md), sw, len(sweeps), precision, C.byref(out)), self.h)
         return _take_dmrg_result(out)
+
+    def dmrg_states(self, model, sweeps_per_state, weight, precision=-1):
+        """Ground state, then excited states: state k minimises H + weight * sum_{j<k}
+        |psi_j><psi_j| (dmrg(H, psis, psi0, sweeps, {"Weight", weight})), each from
+        the model's default product state on its own sweep table. Returns a list of DmrgResult."""
+        md = _model_desc(model)
+        k = len(sweeps_per_state)
+        tables = [_sweep_descs(sw) for sw in sweeps_per_state]
+        ptrs = (C.POINTER(SweepDesc) * k)(*[C.cast(t, C.POINTER(SweepDesc)) for t in tables])
+        ns = np.array([len(sw) for sw in sweeps_per_state], np.int32)
+        outs = (C.c_void_p * k)()
+        self._ok(lib().itg_dmrg_run_states(self.h, C.byref(md), k, ptrs, _p(ns, C.c_int32), float(weight), precision,
+                                           outs), self.h)
+        return [_take_dmrg_result(C.c_void_p(o)) for o in outs]
 
 
 def _model_desc(model):

@@ -45,6 +45,10 @@ struct LocalOp {
     Tensor const* W1 = nullptr;
     Tensor const* W2 = nullptr;
     Tensor const* R = nullptr;
+    // Excited states (LocalMPO_MPS, itensor/mps/localmpo_mps.h:137-150): the
+    // apply adds proj_weight * sum_j P_j (P_j . phi), P_j stored in phi's layout.
+    std::vector<Tensor> const* proj = nullptr;
+    double proj_weight = 0.0;
 };
 // H_eff * phi written in phi's layout (phi must hold every block of its divergence).
 // into_phi_layout=false returns the reference's own output structure instead.
@@ -172,6 +176,7 @@ struct SweepSpec {
 struct BondRecord { int sweep, halfsweep, bond; double energy, truncerr; long dim; };
 struct DmrgResult {
     double energy = 0;
+    std::vector<Tensor> psi;   // the final MPS
     std::vector<BondRecord> bonds;
     std::vector<Index> links;
     std::vector<double> sweep_seconds;
@@ -181,6 +186,10 @@ struct DmrgResult {
 };
 // DMRGWorker (itensor/mps/dmrg.h:336-467) with LocalMPO environments
 // (itensor/mps/localmpo.h:443-618).
-DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<SweepSpec> const& sweeps, int prec);
+// With `prev`, the state that minimises H + weight sum_j |psi_j><psi_j| (the
+// excited-state dmrg of itensor/mps/dmrg.h:245-266, LocalMPO_MPS of
+// itensor/mps/localmpo_mps.h): prev holds earlier results' MPS in the same QN sector.
+DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<SweepSpec> const& sweeps, int prec,
+                std::vector<std::vector<Tensor>> const* prev = nullptr, double weight = 1.0);
 
 }  // namespace itg

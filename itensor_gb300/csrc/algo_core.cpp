@@ -423,9 +423,24 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
     auto Mat = [&](int i, int j) -> double& { return M[(size_t)j * msz + i]; };
     // one prepared program for every apply of this call (plans resolved once)
     auto prog = heff_prepare(ctx, op, phi.lay, prec, true, false);
+    const int nproj = op.proj ? (int)op.proj->size() : 0;
+    ITG_REQUIRE(nproj <= VecList::MAX, "davidson: too many projected states");
+    std::vector<double const*> pptr(nproj);
+    for (int j = 0; j < nproj; ++j) {
+        ITG_REQUIRE((*op.proj)[j].lay->size == n, "davidson: projector not in phi's layout");
+        pptr[j] = (*op.proj)[j].data();
+    }
+    std::vector<double> pz(std::max(nproj, 1));
     auto apply = [&](Tensor const& x) {
         Tensor y(phi.lay, ctx.stream);
         prog->run(ctx, x.data(), y.data());
+        if (nproj) {
+            // y += w sum_j P_j (P_j . x)
+            dots(ctx, pptr.data(), nproj, x.data(), n, pz.data());
+            VecList X;
+            for (int j = 0; j < nproj; ++j) X.add(pptr[j], op.proj_weight * pz[j]);
+            combo(ctx, y.data(), 1.0, X, n, false);
+        }
         ++napply;
         return y;
     };

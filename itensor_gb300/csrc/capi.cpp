@@ -504,11 +504,41 @@ int itg_dmrg_run(itg_ctx* c, const itg_model_desc* model, const itg_sweep_desc* 
         auto* res = new itg_dmrg_result;
         try {
             res->r = dmrg(c->ctx, mpo, psi, sw, precision);
+            res->r.psi.clear();
         } catch (...) {
             delete res;
             throw;
         }
         *out = res;
+    });
+}
+
+int itg_dmrg_run_states(itg_ctx* c, const itg_model_desc* model, int32_t nstates, const itg_sweep_desc* const* sweeps,
+                        const int32_t* nsweeps, double weight, int precision, itg_dmrg_result** out) {
+    return guard(c, [&] {
+        ITG_REQUIRE(model && nstates >= 1 && sweeps && nsweeps && out, "dmrg_run_states: bad arguments");
+        ITG_REQUIRE(weight > 0, "dmrg_run_states: the weight must be positive");
+        ModelSpec m = model_from(*model);
+        Hamiltonian H = make_hamiltonian(m);
+        ITG_REQUIRE(H.N >= 2, "dmrg_run_states: need at least two sites");
+        MPO mpo = build_mpo(c->ctx, H);
+        std::vector<std::vector<Tensor>> prev;
+        std::vector<itg_dmrg_result*> made;
+        try {
+            for (int k = 0; k < nstates; ++k) {
+                auto psi = product_mps(c->ctx, mpo, H.st, default_state(m));
+                std::vector<SweepSpec> sw = sweeps_from(sweeps[k], nsweeps[k]);
+                auto* res = new itg_dmrg_result;
+                made.push_back(res);
+                res->r = dmrg(c->ctx, mpo, psi, sw, precision, k ? &prev : nullptr, weight);
+                prev.push_back(res->r.psi);
+                res->r.psi.clear();
+            }
+        } catch (...) {
+            for (auto* r : made) delete r;
+            throw;
+        }
+        for (int k = 0; k < nstates; ++k) out[k] = made[k];
     });
 }
 

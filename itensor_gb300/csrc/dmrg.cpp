@@ -46,12 +46,68 @@ struct Environments {
         return op;
     }
 };
+// LocalMPO built from an earlier state psi_j (itensor/mps/localmpo.h:340-349,
+// makeL/makeR :543-594, product :389-421): environments of <psi_j|psi> with
+// dag(prime(psi_j(k), "Link")), and at bond b the projector
+// P_j = dag(L_j psi_j(b)' psi_j(b+1)' R_j) in the layout of phi.
+struct MpsEnvironments {
+    std::vector<Tensor> const* P;
+    std::vector<Index> const* sites;
+    std::vector<Tensor> PH;
+    int N, LHlim, RHlim;
+    MpsEnvironments(std::vector<Tensor> const& p, std::vector<Index> const& s)
+        : P(&p), sites(&s), PH(p.size() + 2), N((int)p.size()), LHlim(0), RHlim((int)p.size() + 1) {}
+
+    // dag(prime(psi_j(k), "Link")): every index of the site tensor but the site primed
+    Tensor dagp(int k) const {
+        Tensor const& A = (*P)[k - 1];
+        std::vector<Index> inds = dag_all(A.inds());
+        for (auto& I : inds)
+            if (!I.same((*sites)[k - 1])) I = I.prime();
+        return relabel(A, inds);
+    }
+    void makeL(Ctx& ctx, std::vector<Tensor> const& psi, int k, int prec) {
+        while (LHlim < k) {
+            int ll = LHlim;
+            Tensor E = PH[ll].valid() ? contract(ctx, PH[ll], psi[ll], prec) : psi[ll];
+            PH[ll + 1] = contract(ctx, E, dagp(ll + 1), prec);
+            LHlim = ll + 1;
+        }
+    }
+    void makeR(Ctx& ctx, std::vector<Tensor> const& psi, int k, int prec) {
+        while (RHlim > k) {
+            int rl = RHlim;
+            Tensor E = PH[rl].valid() ? contract(ctx, PH[rl], psi[rl - 2], prec) : psi[rl - 2];
+            PH[rl - 1] = contract(ctx, E, dagp(rl - 1), prec);
+            RHlim = rl - 1;
+        }
+    }
+    Tensor projector(Ctx& ctx, int b, std::vector<Tensor> const& psi, std::shared_ptr<Layout> phi_layout, int prec) {
+        makeL(ctx, psi, b - 1, prec);
+        makeR(ctx, psi, b + 2, prec);
+        LHlim = b - 1;
+        RHlim = b + 2;
+        Tensor o = (b - 1 >= 1) ? contract(ctx, PH[b - 1], dagp(b), prec) : dagp(b);
+        Tensor r = (b + 2 <= N) ? contract(ctx, PH[b + 2], dagp(b + 1), prec) : dagp(b + 1);
+        // dag(othr) has phi's indices (same ids and primes, arrows flipped): for real
+        // data it is the same numbers, written straight into phi's layout
+        return contract(ctx, o, r, prec, phi_layout);
+    }
+};
 }  // namespace
 
-DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<SweepSpec> const& sweeps, int prec) {
+DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<SweepSpec> const& sweeps, int prec,
+                std::vector<std::vector<Tensor>> const* prev, double weight) {
     const int N = (int)psi.size();
     ITG_REQUIRE(N >= 2 && (int)H.W.size() == N, "dmrg: MPO and MPS lengths differ");
     Environments env(H.W);
+    std::vector<MpsEnvironments> penv;
+    if (prev)
+        for (auto const& p : *prev) {
+            ITG_REQUIRE((int)p.size() == N, "dmrg: an earlier state has another length");
+            penv.emplace_back(p, H.sites);
+        }
+    std::vector<Tensor> proj(penv.size());
     DmrgResult res;
     double energy = 0;
     for (size_t sw = 0; sw < sweeps.size(); ++sw) {
@@ -71,6 +127,11 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
             for (int j : mt.b_unc) pinds.push_back(B.inds()[j]);
             auto full = std::make_shared<Layout>(allowed_layout(pinds, tensor_div(A) + tensor_div(B)));
             Tensor phi = contract(ctx, A, B, prec, full);
+            if (!penv.empty()) {
+                for (size_t j = 0; j < penv.size(); ++j) proj[j] = penv[j].projector(ctx, b, psi, full, PREC_F64);
+                op.proj = &proj;
+                op.proj_weight = weight;
+            }
             auto tp1 = clk::now();
             energy = davidson(ctx, op, phi, s.niter, 1e-14, 1, prec, &res.heff_applies);
             auto tp2 = clk::now();
@@ -110,6 +171,7 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
         ITG_REQUIRE(!mt.a_con.empty(), "dmrg: neighbouring tensors share no link");
         res.links.push_back(psi[b].inds()[mt.a_con[0]]);
     }
+    res.psi = std::move(psi);
     return res;
 }
 

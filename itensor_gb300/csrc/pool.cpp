@@ -163,6 +163,7 @@ void run_solve(Ctx& ctx, SolveRecord& rec, SolverPool const& pool) {
         MPO mpo = build_mpo(ctx, H);
         auto psi = product_mps(ctx, mpo, H.st, default_state(rec.req.model));
         rec.result = dmrg(ctx, mpo, std::move(psi), rec.req.sweeps, rec.req.prec);
+        rec.result.psi.clear();   // the record keeps energies and links, not the state
         rec.status = 0;
     } catch (Error const& e) {
         rec.status = e.code;

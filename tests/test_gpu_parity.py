@@ -353,3 +353,25 @@ def test_dmrg_golden_tridiagonal_eigh(ctx, golden, name, monkeypatch):
     """Every density-matrix block through the tridiagonal path (down to 1x1)."""
     monkeypatch.setenv("ITG_EIG_TRI_MIN", "1")
     test_dmrg_golden(ctx, golden, name)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_dmrg_excited_golden(ctx, golden, prec):
+    """Excited-state DMRG through the C-ABI (ground state, then H + 20 |psi0><psi0|)
+    against the reference's N=12 Heisenberg fixture; FP64 to 1e-10 per bond, the
+    split form to 1e-9 on the energies."""
+    c = [x for x in golden("dmrg")["cases"] if x["name"] == "heis12_excited"][0]
+    res = ctx.dmrg_states(dict(type=0, N=c["N"], J=1.0, Jz=1.0), [c["ground_sweeps"], c["sweeps"]], c["weight"],
+                          precision=prec)
+    tol = ENERGY_TOL if prec == 0 else 1e-9
+    assert abs(res[0].energy - c["ground_energy"]) < tol
+    assert abs(res[1].energy - c["energy"]) < tol
+    if prec == 0:
+        assert len(res[1].bonds) == len(c["bonds"])
+        for a, b in zip(res[1].bonds, c["bonds"]):
+            assert tuple(a[:3]) == tuple(b[:3])
+            assert abs(a[3] - b[3]) < ENERGY_TOL, (a, b)
+            assert abs(a[4] - b[4]) < 1e-12
+            assert a[5] == b[5]
+        for (dr, qn, dims), ref in zip(res[1].links, c["links"]):
+            assert [int(x) for x in dims] == [d for _, d in ref["sectors"]]
