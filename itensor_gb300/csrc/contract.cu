@@ -325,6 +325,12 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
 }
 
 // ------------------------------------------------------------------ skinny FP64 block GEMM
+// b != 0 (either sign of zero excluded) tested on the bit pattern: an FP64
+// compare issues on the FP64 pipe, which bounds these kernels.
+__device__ __forceinline__ bool nonzero_bits(double b) {
+    return (__double_as_longlong(b) & 0x7FFFFFFFFFFFFFFFll) != 0;
+}
+
 // For contractions whose output blocks are at most SKINNY_N columns wide (the
 // MPO-tensor steps of the H_eff apply: N = (s', w') <= 3, K = (s, w) <= 3).
 // One thread per output row keeps all N sums in registers; the B block
@@ -371,7 +377,7 @@ __device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& 
 #pragma unroll
                 for (int n = 0; n < NN; ++n) {
                     const double b = Bs[k][n];
-                    if (b != 0.0) {
+                    if (nonzero_bits(b)) {
 #pragma unroll
                         for (int j = 0; j < R; ++j) acc[j][n] = fma(a[j], b, acc[j][n]);
                     }
@@ -423,7 +429,7 @@ __device__ __forceinline__ void skinny_item_direct(ItemRec const& it, CBlockRec 
 #pragma unroll
             for (int n = 0; n < NN; ++n) {
                 const double b = __ldg(B + bk + bcol[n]);
-                if (b != 0.0) {
+                if (nonzero_bits(b)) {
 #pragma unroll
                     for (int j = 0; j < R; ++j) acc[j][n] = fma(a[j], b, acc[j][n]);
                 }
@@ -991,7 +997,10 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         std::vector<PrepItem> prep;
         for (int o = 0; o < (int)ops.size(); ++o) {
             const int rows = ops[o].rows, Kp = std::max(ops[o].Kp, 1);
-            const int chunk = std::max(1, std::min(OZ_PREP_ROWS, 2048 / Kp));
+            // eight rows per item: the prep kernel gives each row a warp, and many
+            // rows in flight hide the load latency
+            (void)Kp;
+            const int chunk = OZ_PREP_ITEM_ROWS;
             for (int r0 = 0; r0 < rows; r0 += chunk)
                 prep.push_back(PrepItem{o, r0, std::min(rows, r0 + chunk), o < nopsA ? 0 : 1});
         }

@@ -65,7 +65,7 @@ __device__ __forceinline__ int32_t tab_at(const int32_t* __restrict__ tab, int32
 #endif
 
 constexpr int GEMM_TILE = 32;
-constexpr int OZ_PREP_ROWS = 256;   // rows per split-precision prep item (at most)
+constexpr int OZ_PREP_ITEM_ROWS = 8; // rows per prep item: one warp each
 
 struct Plan {
     std::shared_ptr<Layout> C;       // output layout

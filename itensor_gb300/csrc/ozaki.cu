@@ -20,8 +20,9 @@
 // of the row/column maxima. Slicing and
 // folding are integer work: FP64 issue slots on this part are ~1/60 of FP32.
 //
-// prep: one CTA per item of whole rows (~2048 elements) writes the row
-//       exponents and the S digit planes, k-contiguous, K padded to 16.
+// prep: one CTA per item of whole rows (~2048 elements), one warp per row,
+//       writes the row exponents and the S digit planes, k-contiguous, K
+//       padded to 16.
 // gemm: output tiles of 32 x 32 (4 warps of 16 x 16) or 64 x 32 (8 warps),
 //       one CTA per tile or persistent CTAs over the tile list; the variant
 //       is chosen per plan by autotune_ozaki. Digit panels are staged with
@@ -38,62 +39,72 @@ __device__ __forceinline__ int exp_field(double x) {
     return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
 }
 
+// The S balanced digits of x against the row exponent field emax, written to
+// dst[s * plane] (BF16-exact integers).
+template <int S>
+__device__ __forceinline__ void oz_digits(double x, int emax, __nv_bfloat16* dst, int64_t plane) {
+    long long bits = __double_as_longlong(x);
+    int ef = (int)((bits >> 52) & 0x7FF);
+    unsigned long long Xf = 0;
+    if (ef != 0) {
+        unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+        int sh = ef - 1075 + 7 * S - (emax - 1022);  // <= 7S - 53 < 0 for S <= 7
+        // rounded to nearest, not truncated: truncation shrinks every entry's
+        // magnitude and the bias adds up coherently in the products
+        if (sh >= 0) Xf = mant << sh;
+        else if (sh > -64) Xf = (mant >> (-sh)) + ((mant >> (-sh - 1)) & 1ull);
+    }
+    // balanced digits: d_1..d_{S-1} in [-64, 63], d_0 in [-128, 128] (BF16-exact).
+    // Their signs are independent of the entry's sign, so the digit products
+    // left out (s + t >= S) average to zero instead of always shrinking |x y|.
+    long long X = bits < 0 ? -(long long)Xf : (long long)Xf;
+    int dig[S];
+#pragma unroll
+    for (int s = S - 1; s >= 1; --s) {
+        const long long d = ((X + 64) & 127) - 64;
+        dig[s] = (int)d;
+        X = (X - d) >> 7;
+    }
+    dig[0] = (int)X;
+#pragma unroll
+    for (int s = 0; s < S; ++s) dst[s * plane] = __float2bfloat16_rn((float)dig[s]);
+}
+
+// One warp per row: the row's entries are read once into registers (rows of
+// up to 32 * OZ_PREP_REGS entries; longer rows are read a second time), the
+// exponent is a warp max, and the digits are written k-contiguous.
+constexpr int OZ_PREP_REGS = 8;
 template <int S>
 __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restrict__ items, const OpBlockRec* __restrict__ ops,
                                                          const int32_t* __restrict__ tab, const double* __restrict__ A,
                                                          const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
                                                          int64_t plane, int32_t* __restrict__ exps) {
-    __shared__ int rexp[OZ_PREP_ROWS];
-    __shared__ int32_t trow[OZ_PREP_ROWS];   // offsets of this item's rows
     const PrepItem pi = items[blockIdx.x];
     const OpBlockRec ob = ops[pi.op];
-    const double* __restrict__ X = pi.which ? B : A;
-    const int tid = threadIdx.x;
-    const int rows = pi.r1 - pi.r0;
-    const int n = rows * ob.K;
-    for (int r = tid; r < rows; r += blockDim.x) {
-        rexp[r] = 0;
-        trow[r] = tab_at(tab, ob.trow, pi.r0 + r);
-    }
-    __syncthreads();
-    const double* base = X + ob.src;
-    for (int e = tid; e < n; e += blockDim.x) {
-        int r = e % rows, k = e / rows;
-        atomicMax(&rexp[r], exp_field(base[trow[r] + tab_at(tab, ob.tcol, k)]));
-    }
-    __syncthreads();
-    for (int r = tid; r < rows; r += blockDim.x) exps[ob.exp + pi.r0 + r] = rexp[r] - 1022;  // |x| < 2^(E-1022)
-    const int np = rows * ob.Kp;
-    __nv_bfloat16* pan = panels + ob.panel + (int64_t)pi.r0 * ob.Kp;
-    for (int e = tid; e < np; e += blockDim.x) {
-        int k = e % ob.Kp, r = e / ob.Kp;
-        double x = (k < ob.K) ? base[trow[r] + tab_at(tab, ob.tcol, k)] : 0.0;
-        long long bits = __double_as_longlong(x);
-        int ef = (int)((bits >> 52) & 0x7FF);
-        unsigned long long Xf = 0;
-        if (ef != 0) {
-            unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-            int sh = ef - 1075 + 7 * S - (rexp[r] - 1022);  // <= 7S - 53 < 0 for S <= 7
-            // rounded to nearest, not truncated: truncation shrinks every entry's
-            // magnitude and the bias adds up coherently in the products
-            if (sh >= 0) Xf = mant << sh;
-            else if (sh > -64) Xf = (mant >> (-sh)) + ((mant >> (-sh - 1)) & 1ull);
-        }
-        // balanced digits: d_1..d_{S-1} in [-64, 63], d_0 in [-128, 128] (BF16-exact).
-        // Their signs are independent of the entry's sign, so the digit products
-        // left out (s + t >= S) average to zero instead of always shrinking |x y|.
-        long long X = bits < 0 ? -(long long)Xf : (long long)Xf;
-        int dig[S];
+    const double* __restrict__ base = (pi.which ? B : A) + ob.src;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int r = pi.r0 + warp; r < pi.r1; r += nw) {
+        const int32_t ro = tab_at(tab, ob.trow, r);
+        double xr[OZ_PREP_REGS];
+        int emax = 0;
 #pragma unroll
-        for (int s = S - 1; s >= 1; --s) {
-            const long long d = ((X + 64) & 127) - 64;
-            dig[s] = (int)d;
-            X = (X - d) >> 7;
+        for (int j = 0; j < OZ_PREP_REGS; ++j) {
+            const int k = lane + 32 * j;
+            xr[j] = k < ob.K ? base[ro + tab_at(tab, ob.tcol, k)] : 0.0;
+            emax = max(emax, exp_field(xr[j]));
         }
-        dig[0] = (int)X;
-        __nv_bfloat16* dst = pan + e;
+        for (int k = lane + 32 * OZ_PREP_REGS; k < ob.K; k += 32)
+            emax = max(emax, exp_field(base[ro + tab_at(tab, ob.tcol, k)]));
+        emax = __reduce_max_sync(0xffffffffu, emax);
+        if (lane == 0) exps[ob.exp + r] = emax - 1022;  // |x| < 2^(E-1022)
+        __nv_bfloat16* pan = panels + ob.panel + (int64_t)r * ob.Kp;
 #pragma unroll
-        for (int s = 0; s < S; ++s) dst[s * plane] = __float2bfloat16_rn((float)dig[s]);
+        for (int j = 0; j < OZ_PREP_REGS; ++j) {
+            const int k = lane + 32 * j;
+            if (k < ob.Kp) oz_digits<S>(xr[j], emax, pan + k, plane);
+        }
+        for (int k = lane + 32 * OZ_PREP_REGS; k < ob.Kp; k += 32)
+            oz_digits<S>(k < ob.K ? base[ro + tab_at(tab, ob.tcol, k)] : 0.0, emax, pan + k, plane);
     }
 }
 
