@@ -3,6 +3,7 @@
 // host keeps block metadata, the (niter+2)-sized Rayleigh-Ritz matrix and the
 // truncation decisions.
 #include "algo.h"
+#include "eigh_tri.h"
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -593,8 +594,10 @@ SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor co
     DevBuf vbuf(sizeof(double) * std::max<int64_t>(vtot, 1), ctx.stream);
     DevBuf wbuf(sizeof(double) * std::max<int64_t>(wtot, 1), ctx.stream);
     DevBuf sbuf(sizeof(double) * std::max<int64_t>(stot, 1), ctx.stream);
-    int bad = batched_eigh(ctx, items, rho.data(), vbuf.as<double>(), wbuf.as<double>(), sbuf.as<double>());
-    if (bad) throw Error(ERR_NOCONV, "denmat_decomp: eigensolver hit its sweep cap");
+    // eigenvalues first; the eigenvectors of the large blocks only for the kept states
+    EighPending eig = batched_eigh_begin(ctx, items, rho.data(), vbuf.as<double>(), wbuf.as<double>(),
+                                         sbuf.as<double>());
+    if (eig.bad) throw Error(ERR_NOCONV, "denmat_decomp: eigensolver hit its sweep cap");
     std::vector<double> w(std::max<int64_t>(wtot, 1));
     if (wtot) {
         ctx.d2h(w.data(), wbuf.as<double>(), sizeof(double) * wtot);
@@ -616,6 +619,7 @@ SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor co
         }
         keep[b] = this_m;
     }
+    batched_eigh_finish(ctx, eig, keep, vbuf.as<double>(), sbuf.as<double>());
     std::vector<QN> dq;
     std::vector<int32_t> dd;
     for (int b = 0; b < nb; ++b) if (keep[b] > 0) { dq.push_back(ci.qn(bsec[b])); dd.push_back(keep[b]); }

@@ -993,14 +993,22 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         for (int bb = 0; bb < nB; ++bb)
             if (tbkB[bb] >= 0) ib_of[bb] = add_op(B.offs[bb], rows_of(B, bb, mt.b_unc), rows_of(B, bb, mt.b_con), tbnB[bb], tbkB[bb]);
         const int nopsB = (int)ops.size() - nopsA;
-        // prep items: ~2048 elements each, whole rows (exponents complete per row)
+        // prep items of whole rows (exponents complete per row). Short rows: one
+        // warp each, the item size chosen so that the items fill the GPU about 16
+        // times over (8 to 128 rows: small operands keep every row in flight,
+        // large ones do not pay for hundreds of thousands of tiny CTAs); long
+        // rows: ~2048 entries per item.
         std::vector<PrepItem> prep;
+        int64_t short_rows = 0;
+        for (auto const& o : ops)
+            if (o.Kp <= 32 * OZ_PREP_REGS) short_rows += o.rows;
+        int short_chunk = (int)std::min<int64_t>(128, std::max<int64_t>(OZ_PREP_ITEM_ROWS,
+                                                                       short_rows / (16 * (int64_t)ctx.sm_count)));
+        short_chunk = (short_chunk + 7) / 8 * 8;
         for (int o = 0; o < (int)ops.size(); ++o) {
             const int rows = ops[o].rows, Kp = std::max(ops[o].Kp, 1);
-            // eight rows per item: the prep kernel gives each row a warp, and many
-            // rows in flight hide the load latency
-            (void)Kp;
-            const int chunk = OZ_PREP_ITEM_ROWS;
+            const int chunk = Kp <= 32 * OZ_PREP_REGS ? short_chunk
+                                                      : std::max(1, std::min(OZ_PREP_LONG_ROWS, 2048 / Kp));
             for (int r0 = 0; r0 < rows; r0 += chunk)
                 prep.push_back(PrepItem{o, r0, std::min(rows, r0 + chunk), o < nopsA ? 0 : 1});
         }

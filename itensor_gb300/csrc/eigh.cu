@@ -418,20 +418,32 @@ static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const
 }
 
 // Small blocks: one-CTA Jacobi; large ones: the tridiagonal path (eigh_tri.cu).
-int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
-                 double* scratch) {
+EighPending batched_eigh_begin(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout,
+                               double* wout, double* scratch) {
     int tmin = TRI_MIN_N_DEFAULT;
     if (char const* env = std::getenv("ITG_EIG_TRI_MIN")) tmin = std::max(1, std::atoi(env));
     std::vector<EigItem> small, large;
-    for (auto const& it : items) (it.n >= tmin && it.n <= TRI_MAX_N ? large : small).push_back(it);
+    std::vector<int> large_ids;
+    for (int i = 0; i < (int)items.size(); ++i) {
+        auto const& it = items[i];
+        if (it.n >= tmin && it.n <= TRI_MAX_N) {
+            large.push_back(it);
+            large_ids.push_back(i);
+        } else {
+            small.push_back(it);
+        }
+    }
     const bool timing = std::getenv("ITG_EIG_TIME") != nullptr;  // diagnostics: wall time of each path
     auto now = [&] { ctx.sync(); return std::chrono::steady_clock::now(); };
     auto t0 = timing ? now() : std::chrono::steady_clock::time_point{};
     // Jacobi first: both paths stage uploads in the context's pinned buffer, and
     // each is done with it when it returns
-    int bad = jacobi_eigh(ctx, small, src, vout, wout, scratch);
+    EighPending p;
+    p.bad = jacobi_eigh(ctx, small, src, vout, wout, scratch);
     auto t1 = timing ? now() : t0;
-    bad += tri_eigh(ctx, large, src, vout, wout, scratch);
+    int bad_tri = 0;
+    p.tri = tri_eigh_begin(ctx, large, large_ids, src, wout, scratch, &bad_tri);
+    p.bad += bad_tri;
     if (timing) {
         auto t2 = now();
         int nl = 0, ns = 0;
@@ -441,7 +453,21 @@ int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src,
                      large.size(), nl, std::chrono::duration<double, std::milli>(t2 - t1).count(), small.size(), ns,
                      std::chrono::duration<double, std::milli>(t1 - t0).count());
     }
-    return bad;
+    return p;
+}
+
+void batched_eigh_finish(Ctx& ctx, EighPending& p, std::vector<int> const& keep, double* vout, double* scratch) {
+    if (p.tri) tri_eigh_finish(ctx, *p.tri, keep, vout, scratch);
+}
+
+int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
+                 double* scratch) {
+    EighPending p = batched_eigh_begin(ctx, items, src, vout, wout, scratch);
+    if (p.bad) return p.bad;
+    std::vector<int> all(items.size());
+    for (size_t i = 0; i < items.size(); ++i) all[i] = items[i].n;
+    batched_eigh_finish(ctx, p, all, vout, scratch);
+    return 0;
 }
 
 }  // namespace itg

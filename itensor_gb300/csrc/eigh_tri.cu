@@ -9,24 +9,21 @@
 //      owner builds the reflector, all CTAs form p = tau A v over their columns,
 //      then apply the rank-2 update A -= v w^T + w v^T with w = p - (tau/2)(p.v) v;
 //      two cluster barriers per column). Reflectors are kept below the subdiagonal.
-//   2. tri_formq_kernel: Q = H_0 H_1 ... H_{n-3} formed column by column (one warp
-//      per column, columns independent, spread over the whole GPU).
-//   3. the implicit QL recurrence on (d, e) (tridiag_ql.cpp): a chain of
+//   2. the implicit QL recurrence on (d, e) (tridiag_ql.cpp): a chain of
 //      dependent scalar FP64 operations, ~n^2 rotations per block with a square
 //      root and two divisions each. On this part an SM issues ~2 FP64 FMAs per
 //      clock, so one thread's dependent FP64 chain advances by one operation
 //      every few tens of cycles (measured: ~1.7 us per rotation on the SM); the
-//      host core runs it in nanoseconds per operation. It only records the plane
-//      rotations, while the device forms Q;
-//   4. tri_rot_kernel: the recorded rotations applied to the rows of Q (rows
-//      transform independently: a tile of rows per CTA, in shared memory; the
-//      CTA's eight warps apply rotations of eight sweeps at once, on a
-//      lockstep schedule from the host that keeps them on disjoint columns);
-//   5. tri_out_kernel: eigenvalues sorted descending, eigenvector columns moved
-//      with them.
-// The FP64 work is ~n^3 FMA for the reduction, ~2n^3/3 for Q and ~n^2 rotations
-// x n rows for the accumulation, against ~4n^3 per Jacobi sweep; every O(n^3)
-// stage spreads one block over many SMs.
+//      host core runs it in nanoseconds per operation. It records the plane
+//      rotations; the eigenvalues go back to the caller, which truncates;
+//   3. tri_rot_kernel: only the kept eigenvectors of the tridiagonal matrices:
+//      the recorded rotations applied in reverse to unit vectors, a tile of
+//      vectors per CTA in shared memory, the CTA's eight warps applying
+//      rotations of eight sweeps at once on a lockstep schedule from the host;
+//   4. tri_applyq_kernel: the Householder reflectors applied to each kept
+//      vector (one warp per vector), written to the output in eigenvalue order.
+// The FP64 work is ~n^3 FMA for the reduction, then ~n^2 rotations and ~2n^2
+// reflector FMAs per kept vector, against ~4n^3 per Jacobi sweep for every vector.
 #include "ops.h"
 #include "eigh_tri.h"
 #include "tridiag_ql.h"
@@ -37,6 +34,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <numeric>
 #include <thread>
 
 namespace cg = cooperative_groups;
@@ -56,7 +54,7 @@ struct TriJob {
     int64_t w_off;     // eigenvalues (descending) in wout
     int64_t s_off;     // 2 n^2 doubles: reduced matrix + reflectors, then Q
     int64_t aux_off;   // tri_aux_doubles(n) doubles in aux: d, e, tau, v, p, partial sums
-    int32_t n, pad;
+    int32_t n, keep;   // keep: eigenvectors wanted (the largest eigenvalues), set before the vector stage
 };
 struct ColJob { int32_t job, c0; };
 struct RowJob { int32_t job, r0; };
@@ -198,29 +196,32 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_reduce_kernel(TriJob const* _
     }
 }
 
-// Q e_j = H_0 (H_1 (... H_{n-3} e_j)); H_k acts on rows k+1..n-1, so only
-// reflectors k < j touch column j.
-__global__ void __launch_bounds__(TRI_FORMQ_WARPS * 32) tri_formq_kernel(ColJob const* __restrict__ cjobs,
-                                                                         TriJob const* __restrict__ jobs,
-                                                                         double* __restrict__ scratch,
-                                                                         double const* __restrict__ aux, int nmax) {
+// z = H_0 (H_1 (... H_{n-3} y)) for the kept columns y of Y (n x k, column-major,
+// in the second half of the block's scratch): the eigenvectors of the block,
+// written to vout in eigenvalue order. One warp per column; H_k acts on rows
+// k+1..n-1 with v[k+1] = 1 and v[i] stored below the subdiagonal of column k.
+__global__ void __launch_bounds__(TRI_FORMQ_WARPS * 32) tri_applyq_kernel(ColJob const* __restrict__ cjobs,
+                                                                          TriJob const* __restrict__ jobs,
+                                                                          double const* __restrict__ scratch,
+                                                                          double const* __restrict__ aux,
+                                                                          double* __restrict__ vout, int nmax) {
     extern __shared__ double sm[];
     const ColJob cj = cjobs[blockIdx.x];
     const TriJob jb = jobs[cj.job];
     const int n = jb.n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = cj.c0 + warp;
-    if (j >= n) return;
-    double const* R = scratch + jb.s_off;               // reflectors below the subdiagonal
-    double* Q = scratch + jb.s_off + (size_t)n * n;
+    if (j >= jb.keep) return;
+    double const* Rf = scratch + jb.s_off;               // reflectors below the subdiagonal
+    double const* Y = scratch + jb.s_off + (size_t)n * n;
     double const* tau = aux + jb.aux_off + 2 * (size_t)n;
     double* y = sm + (size_t)warp * nmax;
-    for (int i = lane; i < n; i += 32) y[i] = (i == j) ? 1.0 : 0.0;
+    for (int i = lane; i < n; i += 32) y[i] = Y[(size_t)j * n + i];
     __syncwarp();
-    for (int k = min(j - 1, n - 3); k >= 0; --k) {
+    for (int k = n - 3; k >= 0; --k) {
         const double t = tau[k];
         if (t == 0.0) continue;
-        double const* v = R + (size_t)k * n;
+        double const* v = Rf + (size_t)k * n;
         double acc = 0.0;
         for (int i = k + 2 + lane; i < n; i += 32) acc = fma(v[i], y[i], acc);
         const double dt = t * (warp_sum(acc) + y[k + 1]);
@@ -229,26 +230,29 @@ __global__ void __launch_bounds__(TRI_FORMQ_WARPS * 32) tri_formq_kernel(ColJob 
         for (int i = k + 2 + lane; i < n; i += 32) y[i] = fma(-dt, v[i], y[i]);
         __syncwarp();
     }
-    for (int i = lane; i < n; i += 32) Q[(size_t)j * n + i] = y[i];
+    for (int i = lane; i < n; i += 32) vout[jb.v_off + (size_t)j * n + i] = y[i];
 }
 
-// What the host's QL pass hands back per block (offsets into the uploaded blob).
+// The vector stage's per-block records (offsets into the uploaded blob).
 struct QlOut {
-    int64_t eig_off;   // eigenvalues (unsorted, doubles)
-    int64_t hdr_off;   // sweeps (QlSweep = int4: l, m, rotation offset, 0)
-    int64_t rot_off;   // rotations (QlRot = double2: c, s)
+    int64_t hdr_off;   // sweeps (QlSweep = int4: l, m, rotation offset, 0), mirrored and reversed
+    int64_t rot_off;   // rotations (QlRot = double2: c, s) in that order
     int64_t sched_off; // TRI_ROT_WARPS + 1 entry offsets, then entries (QlStart = int2: start step, sweep)
-    int32_t nsweeps, status, nsteps, pad;
+    int64_t sel_off;   // kept eigenvalues' positions in the QL output (int32), descending eigenvalue order
+    int32_t nsweeps, nsteps;
 };
 
-// The recorded rotations applied to rows r0..r0+R-1 of Q (the tile lives in
-// shared memory as tile[col * R + row], lane = row). The CTA's warps apply
-// rotations of different QL sweeps at once, in lockstep: at step s a warp
-// applies rotation s - S of its current sweep (started at step S), with a
-// barrier every TRI_ROT_WINDOW steps; the host's schedule keeps the sweeps
-// far enough apart that the warps of one window touch disjoint columns, so
-// each column sees its rotations in the recorded order.
-// Rotation i of a sweep: (z_i, z_{i+1}) <- (c z_i - s z_{i+1}, s z_i + c z_{i+1}).
+// Kept eigenvectors of the tridiagonal matrix: rows r0..r0+R-1 of Y^T, row r
+// starting as the unit vector of the r-th kept eigenvalue, times the QL
+// rotations in reverse order (G e_j = G_1 (G_2 (... G_T e_j))). In mirrored
+// column order (column c holds component n-1-c) the reversed sequence is again
+// a series of sweeps that run down the columns with the recorded (c, s), so the
+// same lockstep schedule applies: the CTA's warps apply rotations of different
+// sweeps at once, a barrier every TRI_ROT_WINDOW steps, and the host's schedule
+// keeps the warps of one window on disjoint columns. Rotation at column i:
+// (z_i, z_{i+1}) <- (c z_i - s z_{i+1}, s z_i + c z_{i+1}). The tile lives in
+// shared memory as tile[col * R + row], lane = row; Y (n x keep) is written to
+// the second half of the block's scratch.
 __global__ void __launch_bounds__(TRI_ROT_WARPS * 32) tri_rot_kernel(RowJob const* __restrict__ rjobs,
                                                                      TriJob const* __restrict__ jobs,
                                                                      double* __restrict__ scratch,
@@ -258,13 +262,12 @@ __global__ void __launch_bounds__(TRI_ROT_WARPS * 32) tri_rot_kernel(RowJob cons
     const RowJob rj = rjobs[blockIdx.x];
     const TriJob jb = jobs[rj.job];
     const QlOut o = qo[rj.job];
-    if (o.status != 0) return;
     const int n = jb.n;
-    const int rows = min(R, n - rj.r0);
-    double* Q = scratch + jb.s_off + (size_t)n * n;
+    const int rows = min(R, jb.keep - rj.r0);
+    int32_t const* sel = reinterpret_cast<int32_t const*>(blob + o.sel_off);
     for (int idx = threadIdx.x; idx < n * R; idx += blockDim.x) {
         const int c = idx / R, r = idx % R;
-        if (r < rows) tile[idx] = Q[(size_t)c * n + rj.r0 + r];
+        tile[idx] = (r < rows && c == n - 1 - __ldg(sel + rj.r0 + r)) ? 1.0 : 0.0;
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -289,8 +292,6 @@ __global__ void __launch_bounds__(TRI_ROT_WARPS * 32) tri_rot_kernel(RowJob cons
     };
     fetch();
     const bool row_ok = lane < rows;
-    // TRI_ROT_WINDOW steps between barriers: the schedule puts every rotation in
-    // a later window than the other warps' earlier rotations on its columns
     for (int s0 = 0; s0 < o.nsteps; s0 += TRI_ROT_WINDOW) {
 #pragma unroll
         for (int u = 0; u < TRI_ROT_WINDOW; ++u) {
@@ -309,35 +310,19 @@ __global__ void __launch_bounds__(TRI_ROT_WARPS * 32) tri_rot_kernel(RowJob cons
         }
         __syncthreads();
     }
+    double* Y = scratch + jb.s_off + (size_t)n * n;
     for (int idx = threadIdx.x; idx < n * R; idx += blockDim.x) {
-        const int c = idx / R, rr = idx % R;
-        if (rr < rows) Q[(size_t)c * n + rj.r0 + rr] = tile[idx];
+        const int c = idx / R, r = idx % R;
+        if (r < rows) Y[(size_t)(rj.r0 + r) * n + (n - 1 - c)] = tile[idx];
     }
 }
 
-// Eigenvalues descending (ties by position) with their columns; one warp per column.
-__global__ void tri_out_kernel(ColJob const* __restrict__ cjobs, TriJob const* __restrict__ jobs,
-                               double const* __restrict__ scratch, QlOut const* __restrict__ qo,
-                               char const* __restrict__ blob, double* __restrict__ vout, double* __restrict__ wout) {
-    const ColJob cj = cjobs[blockIdx.x];
-    const TriJob jb = jobs[cj.job];
-    const QlOut o = qo[cj.job];
-    if (o.status != 0) return;
-    const int n = jb.n;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int j = cj.c0 + warp;
-    if (j >= n) return;
-    double const* d = reinterpret_cast<double const*>(blob + o.eig_off);
-    const double dj = d[j];
-    int cnt = 0;
-    for (int i = lane; i < n; i += 32) {
-        const double di = d[i];
-        cnt += (di > dj || (di == dj && i < j)) ? 1 : 0;
-    }
-    for (int o2 = 16; o2 > 0; o2 >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o2);
-    double const* Q = scratch + jb.s_off + (size_t)n * n;
-    if (lane == 0) wout[jb.w_off + cnt] = dj;
-    for (int i = lane; i < n; i += 32) vout[jb.v_off + (size_t)cnt * n + i] = Q[(size_t)j * n + i];
+// Sorted eigenvalues of every block to wout (one CTA per block).
+__global__ void tri_wout_kernel(TriJob const* __restrict__ jobs, double const* __restrict__ sorted,
+                                int64_t const* __restrict__ soff, double* __restrict__ wout) {
+    const TriJob jb = jobs[blockIdx.x];
+    const int64_t o = soff[blockIdx.x];
+    for (int i = threadIdx.x; i < jb.n; i += blockDim.x) wout[jb.w_off + i] = sorted[o + i];
 }
 
 // CTAs per block in the reduction: 16-32 columns each, at most 16 (a
@@ -351,75 +336,94 @@ int cluster_for(int n) {
 }
 }  // namespace
 
-int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, double* vout, double* wout,
-             double* scratch) {
-    if (items_in.empty()) return 0;
-    // jobs ordered by cluster size (largest first), so that each size is one launch
-    std::vector<EigItem> items(items_in);
-    std::stable_sort(items.begin(), items.end(),
-                     [](EigItem const& a, EigItem const& b) { return cluster_for(a.n) > cluster_for(b.n); });
-    const int nj = (int)items.size();
+struct TriPending {
+    std::vector<EigItem> items;   // ordered by cluster size, largest first
+    std::vector<int> ids;         // the caller's id of each item
+    std::vector<TriJob> jobs;
+    DevBufPtr buf;                // jobs table | aux (d, e, tau, v, p, partials)
+    size_t o_aux = 0;
     int nmax = 0;
-    for (auto const& it : items) nmax = std::max(nmax, it.n);
-    ITG_REQUIRE(nmax <= TRI_MAX_N, "tri_eigh: block larger than the tridiagonal path supports");
-    // rows per tile of the rotation pass (lane = row): a full warp, fewer when
-    // shared memory runs out
-    int R = 32;
-    if (char const* env = std::getenv("ITG_TRI_ROWS")) R = std::max(1, std::min(32, std::atoi(env)));
-    while (R > 1 && sizeof(double) * (size_t)R * nmax > TRI_SMEM_LIMIT) R /= 2;
-    std::vector<TriJob> jobs(nj);
-    std::vector<ColJob> cjobs;
-    std::vector<RowJob> rjobs;
+    std::vector<std::vector<QlSweep>> sweeps;   // QL sweeps and rotations per block
+    std::vector<std::vector<QlRot>> rots;
+    std::vector<std::vector<int32_t>> order;    // eigenvalue positions, descending (ties by position)
+    std::vector<int> status;
+};
+void TriPendingFree::operator()(TriPending* p) const { delete p; }
+
+namespace {
+// Runs f(b) for b < n on the calling thread, or on up to 8 host threads when the
+// work is large and the caller is not a solver-pool fiber (whose workers already
+// run one solve each).
+template <typename F>
+void for_blocks(int n, double work, F const& f) {
+    const int nthreads = (!fiber_active() && work > 2e5) ? std::min<int>(n, 8) : 1;
+    if (nthreads > 1) {
+        std::atomic<int> next{0};
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthreads; ++t)
+            pool.emplace_back([&] {
+                for (int b; (b = next.fetch_add(1)) < n;) f(b);
+            });
+        for (auto& t : pool) t.join();
+    } else {
+        for (int b = 0; b < n; ++b) f(b);
+    }
+}
+size_t a16(size_t x) { return (x + 15) / 16 * 16; }
+}  // namespace
+
+TriPendingPtr tri_eigh_begin(Ctx& ctx, std::vector<EigItem> const& items_in, std::vector<int> const& ids_in,
+                             double const* src, double* wout, double* scratch, int* bad) {
+    *bad = 0;
+    TriPendingPtr P(new TriPending);
+    if (items_in.empty()) return P;
+    // items ordered by cluster size (largest first), so that each size is one launch
+    std::vector<int> ord(items_in.size());
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int x, int y) { return cluster_for(items_in[x].n) > cluster_for(items_in[y].n); });
+    for (int i : ord) {
+        P->items.push_back(items_in[i]);
+        P->ids.push_back(ids_in[i]);
+    }
+    auto const& items = P->items;
+    const int nj = (int)items.size();
+    for (auto const& it : items) P->nmax = std::max(P->nmax, it.n);
+    ITG_REQUIRE(P->nmax <= TRI_MAX_N, "tri_eigh: block larger than the tridiagonal path supports");
+    P->jobs.resize(nj);
     int64_t aux_tot = 0;
     for (int b = 0; b < nj; ++b) {
-        auto const& it = items[b];
-        TriJob& j = jobs[b];
+        TriJob& j = P->jobs[b];
         j = TriJob{};
-        j.a_off = it.a_off;
-        j.v_off = it.v_off;
-        j.w_off = it.w_off;
-        j.s_off = it.s_off;
+        j.a_off = items[b].a_off;
+        j.v_off = items[b].v_off;
+        j.w_off = items[b].w_off;
+        j.s_off = items[b].s_off;
         j.aux_off = aux_tot;
-        aux_tot += tri_aux_doubles(it.n);
-        j.n = it.n;
-        for (int c0 = 0; c0 < it.n; c0 += TRI_FORMQ_WARPS) cjobs.push_back(ColJob{b, c0});
-        for (int r0 = 0; r0 < it.n; r0 += R) rjobs.push_back(RowJob{b, r0});
+        aux_tot += tri_aux_doubles(items[b].n);
+        j.n = items[b].n;
+        j.keep = 0;
     }
-    auto a16 = [](size_t x) { return (x + 15) / 16 * 16; };
-    const size_t o_jobs = 0, o_cj = a16(sizeof(TriJob) * nj), o_rj = a16(o_cj + sizeof(ColJob) * cjobs.size());
-    const size_t up = a16(o_rj + sizeof(RowJob) * rjobs.size());
-    const size_t o_aux = up;
-    const size_t total = o_aux + sizeof(double) * aux_tot;
-    DevBuf buf(total, ctx.stream);
+    const size_t up = a16(sizeof(TriJob) * nj);
+    P->o_aux = up;
+    P->buf = dev_alloc(up + sizeof(double) * aux_tot, ctx.stream);
     ctx.ensure_stage(up);
-    char* st = static_cast<char*>(ctx.stage);
-    std::memcpy(st + o_jobs, jobs.data(), sizeof(TriJob) * nj);
-    std::memcpy(st + o_cj, cjobs.data(), sizeof(ColJob) * cjobs.size());
-    std::memcpy(st + o_rj, rjobs.data(), sizeof(RowJob) * rjobs.size());
-    char* db = buf.as<char>();
-    ITG_CHECK_CUDA(cudaMemcpyAsync(db, st, up, cudaMemcpyHostToDevice, ctx.stream));
-    TriJob const* d_jobs = reinterpret_cast<TriJob const*>(db + o_jobs);
-    ColJob const* d_cj = reinterpret_cast<ColJob const*>(db + o_cj);
-    RowJob const* d_rj = reinterpret_cast<RowJob const*>(db + o_rj);
-    double* d_aux = reinterpret_cast<double*>(db + o_aux);
-
-    // diagnostics (ITG_EIG_TIME): device time of the reduction and of Q, host
-    // time of the QL pass, device time of the rotations and the output
+    std::memcpy(ctx.stage, P->jobs.data(), sizeof(TriJob) * nj);
+    char* db = P->buf->as<char>();
+    ITG_CHECK_CUDA(cudaMemcpyAsync(db, ctx.stage, up, cudaMemcpyHostToDevice, ctx.stream));
+    TriJob const* d_jobs = reinterpret_cast<TriJob const*>(db);
+    double* d_aux = reinterpret_cast<double*>(db + P->o_aux);
     const bool timing = std::getenv("ITG_EIG_TIME") != nullptr;
-    cudaEvent_t ev[5] = {};
-    if (timing) {
-        for (auto& x : ev) ITG_CHECK_CUDA(cudaEventCreate(&x));
-        ITG_CHECK_CUDA(cudaEventRecord(ev[0], ctx.stream));
-    }
-    // 1. reduction: one launch per run of jobs with the same cluster size
+    auto t0 = std::chrono::steady_clock::now();
+
+    // 1. reduction: one launch per cluster size; the launches are independent,
+    //    so they run side by side on the context's side streams
     {
-        const size_t smem = sizeof(double) * 2 * (size_t)nmax;
+        const size_t smem = sizeof(double) * 2 * (size_t)P->nmax;
         if (smem > 48 * 1024)
             ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_reduce_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem));
         ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_reduce_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-        // one launch per cluster size; the launches are independent, so they
-        // run side by side on the context's side streams
         int ngroups = 0;
         for (int b = 0; b < nj;) {
             int e = b;
@@ -453,150 +457,197 @@ int tri_eigh(Ctx& ctx, std::vector<EigItem> const& items_in, double const* src, 
         }
         if (fan) ctx.join(std::min(ngroups, (int)Ctx::NSIDE));
     }
-    // (d, e) of every block to the host; Q is formed on the device meanwhile
+    // 2. (d, e) of every block to the host; QL there
     const size_t aux_bytes = sizeof(double) * aux_tot;
     ctx.ensure_pin(aux_bytes);
     ITG_CHECK_CUDA(cudaMemcpyAsync(ctx.pin, d_aux, aux_bytes, cudaMemcpyDeviceToHost, ctx.stream));
-    cudaEvent_t de_ready;
-    ITG_CHECK_CUDA(cudaEventCreateWithFlags(&de_ready, cudaEventDisableTiming));
-    ITG_CHECK_CUDA(cudaEventRecord(de_ready, ctx.stream));
-    if (timing) ITG_CHECK_CUDA(cudaEventRecord(ev[1], ctx.stream));
-    {
-        const size_t smem = sizeof(double) * TRI_FORMQ_WARPS * (size_t)nmax;
-        if (smem > 48 * 1024)
-            ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_formq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)smem));
-        tri_formq_kernel<<<(int)cjobs.size(), TRI_FORMQ_WARPS * 32, smem, ctx.stream>>>(d_cj, d_jobs, scratch, d_aux,
-                                                                                       nmax);
-        ITG_CHECK_CUDA(cudaGetLastError());
-        ctx.kernel_launches++;
-    }
-    if (timing) ITG_CHECK_CUDA(cudaEventRecord(ev[2], ctx.stream));
-    // 2. QL recurrences on the host, as soon as (d, e) arrived
-    if (fiber_active()) fiber_wait_event(de_ready);
-    else ITG_CHECK_CUDA(cudaEventSynchronize(de_ready));
-    cudaEventDestroy(de_ready);
-    auto th0 = std::chrono::steady_clock::now();
+    ctx.sync();
+    auto t1 = std::chrono::steady_clock::now();
     std::vector<double> de(static_cast<double*>(ctx.pin), static_cast<double*>(ctx.pin) + aux_tot);
-    std::vector<QlOut> qo(nj);
-    std::vector<QlSweep> sweeps;
-    std::vector<QlRot> rots;
-    std::vector<std::vector<double>> eigs(nj);
-    // blocks are independent: outside the solver pool (whose workers already
-    // run one solve each) large passes use a few host threads
-    std::vector<std::vector<QlSweep>> bsw(nj);
-    std::vector<std::vector<QlRot>> brot(nj);
-    std::vector<std::vector<int32_t>> bwoff(nj);
-    std::vector<std::vector<QlStart>> bent(nj);
-    std::vector<int> bst(nj, 0), bsteps(nj, 0);
-    auto run_block = [&](int b) {
-        const int n = items[b].n;
-        double* d = de.data() + jobs[b].aux_off;
-        bst[b] = tridiag_ql(n, d, d + n, bsw[b], brot[b]);
-        eigs[b].assign(d, d + n);
-        if (bst[b] == 0) bsteps[b] = ql_schedule(n, bsw[b], TRI_ROT_WARPS, TRI_ROT_WINDOW, bwoff[b], bent[b]);
-        else bwoff[b].assign(TRI_ROT_WARPS + 1, 0);
-    };
+    P->sweeps.resize(nj);
+    P->rots.resize(nj);
+    P->order.resize(nj);
+    P->status.assign(nj, 0);
+    std::vector<std::vector<double>> sorted(nj);
     double work = 0;
     for (auto const& it : items) work += (double)it.n * it.n;
-    const int nthreads = (!fiber_active() && work > 2e5) ? std::min<int>(nj, 8) : 1;
-    if (nthreads > 1) {
-        std::atomic<int> next{0};
-        std::vector<std::thread> pool;
-        for (int t = 0; t < nthreads; ++t)
-            pool.emplace_back([&] {
-                for (int b; (b = next.fetch_add(1)) < nj;) run_block(b);
-            });
-        for (auto& t : pool) t.join();
-    } else {
-        for (int b = 0; b < nj; ++b) run_block(b);
-    }
-    int bad = 0;
-    std::vector<int32_t> sched;   // per block: woff (padded to 8 bytes), then entries as int pairs
-    for (int b = 0; b < nj; ++b) {
-        qo[b].status = bst[b];
-        bad += (bst[b] != 0);
-        qo[b].nsweeps = (int32_t)bsw[b].size();
-        qo[b].nsteps = bsteps[b];
-        qo[b].pad = 0;
-        qo[b].hdr_off = (int64_t)sweeps.size();   // element offsets for now
-        qo[b].rot_off = (int64_t)rots.size();
-        qo[b].sched_off = (int64_t)sched.size();
-        sweeps.insert(sweeps.end(), bsw[b].begin(), bsw[b].end());
-        rots.insert(rots.end(), brot[b].begin(), brot[b].end());
-        sched.insert(sched.end(), bwoff[b].begin(), bwoff[b].end());
-        for (int k = TRI_ROT_WARPS + 1; k < 2 * ((TRI_ROT_WARPS + 2) / 2); ++k) sched.push_back(0);
-        for (auto const& x : bent[b]) {
-            sched.push_back(x.step);
-            sched.push_back(x.sweep);
-        }
-    }
-    auto th1 = std::chrono::steady_clock::now();
-    // blob: QlOut table | eigenvalues | sweeps | rotations
-    int64_t eig_tot = 0;
-    for (int b = 0; b < nj; ++b) eig_tot += items[b].n;
-    const size_t b_qo = 0, b_eig = a16(sizeof(QlOut) * nj), b_hdr = a16(b_eig + sizeof(double) * eig_tot);
-    const size_t b_rot = a16(b_hdr + sizeof(QlSweep) * sweeps.size());
-    const size_t b_sched = a16(b_rot + sizeof(QlRot) * rots.size());
-    const size_t blob_bytes = a16(b_sched + sizeof(int32_t) * sched.size());
+    for_blocks(nj, work, [&](int b) {
+        const int n = items[b].n;
+        double* d = de.data() + P->jobs[b].aux_off;
+        P->status[b] = tridiag_ql(n, d, d + n, P->sweeps[b], P->rots[b]);
+        auto& o = P->order[b];
+        o.resize(n);
+        std::iota(o.begin(), o.end(), 0);
+        std::stable_sort(o.begin(), o.end(), [&](int x, int y) { return d[x] > d[y]; });
+        sorted[b].resize(n);
+        for (int i = 0; i < n; ++i) sorted[b][i] = d[o[i]];
+    });
+    for (int b = 0; b < nj; ++b) *bad += (P->status[b] != 0);
+    auto t2 = std::chrono::steady_clock::now();
+    // 3. sorted eigenvalues to wout
     {
-        int64_t eo = 0;
-        for (int b = 0; b < nj; ++b) {
-            qo[b].eig_off = (int64_t)(b_eig + sizeof(double) * eo);
-            qo[b].hdr_off = (int64_t)(b_hdr + sizeof(QlSweep) * qo[b].hdr_off);
-            qo[b].rot_off = (int64_t)(b_rot + sizeof(QlRot) * qo[b].rot_off);
-            qo[b].sched_off = (int64_t)(b_sched + sizeof(int32_t) * qo[b].sched_off);
-            eo += items[b].n;
-        }
-    }
-    if (ctx.stage_bytes < blob_bytes) ctx.ensure_stage(blob_bytes + blob_bytes / 2);
-    st = static_cast<char*>(ctx.stage);
-    std::memcpy(st + b_qo, qo.data(), sizeof(QlOut) * nj);
-    {
-        int64_t eo = 0;
-        for (int b = 0; b < nj; ++b) {
-            std::memcpy(st + b_eig + sizeof(double) * eo, eigs[b].data(), sizeof(double) * items[b].n);
-            eo += items[b].n;
-        }
-    }
-    if (!sweeps.empty()) std::memcpy(st + b_hdr, sweeps.data(), sizeof(QlSweep) * sweeps.size());
-    if (!rots.empty()) std::memcpy(st + b_rot, rots.data(), sizeof(QlRot) * rots.size());
-    if (!sched.empty()) std::memcpy(st + b_sched, sched.data(), sizeof(int32_t) * sched.size());
-    DevBuf blob(blob_bytes, ctx.stream);
-    ITG_CHECK_CUDA(cudaMemcpyAsync(blob.p, st, blob_bytes, cudaMemcpyHostToDevice, ctx.stream));
-    QlOut const* d_qo = reinterpret_cast<QlOut const*>(blob.as<char>() + b_qo);
-    if (timing) ITG_CHECK_CUDA(cudaEventRecord(ev[3], ctx.stream));
-    // 3. rotations applied to Q's rows
-    {
-        const size_t smem = sizeof(double) * (size_t)R * nmax;
-        if (smem > 48 * 1024)
-            ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_rot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        tri_rot_kernel<<<(int)rjobs.size(), TRI_ROT_WARPS * 32, smem, ctx.stream>>>(d_rj, d_jobs, scratch, d_qo,
-                                                                                   blob.as<char>(), R);
+        int64_t tot = 0;
+        std::vector<int64_t> soff(nj);
+        for (int b = 0; b < nj; ++b) { soff[b] = tot; tot += items[b].n; }
+        const size_t o_s = a16(sizeof(int64_t) * nj), bytes = o_s + sizeof(double) * tot;
+        ctx.ensure_stage(bytes);
+        char* st = static_cast<char*>(ctx.stage);
+        std::memcpy(st, soff.data(), sizeof(int64_t) * nj);
+        for (int b = 0; b < nj; ++b)
+            std::memcpy(st + o_s + sizeof(double) * soff[b], sorted[b].data(), sizeof(double) * items[b].n);
+        DevBuf wb(bytes, ctx.stream);
+        ITG_CHECK_CUDA(cudaMemcpyAsync(wb.p, st, bytes, cudaMemcpyHostToDevice, ctx.stream));
+        tri_wout_kernel<<<nj, 128, 0, ctx.stream>>>(d_jobs, reinterpret_cast<double const*>(wb.as<char>() + o_s),
+                                                     wb.as<int64_t>(), wout);
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;
     }
-    // 4. sorted output
-    tri_out_kernel<<<(int)cjobs.size(), TRI_FORMQ_WARPS * 32, 0, ctx.stream>>>(d_cj, d_jobs, scratch, d_qo,
-                                                                              blob.as<char>(), vout, wout);
-    ITG_CHECK_CUDA(cudaGetLastError());
-    ctx.kernel_launches++;
-    if (timing) ITG_CHECK_CUDA(cudaEventRecord(ev[4], ctx.stream));
-    // the staging buffer holds the blob until its copy has run
-    ctx.sync();
     if (timing) {
-        float ms[4];
-        for (int i = 0; i < 4; ++i) ITG_CHECK_CUDA(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
-        std::fprintf(stderr,
-                     "itg tri stages (ms): reduce %.3f formq %.3f wait+ql+upload %.3f rot+out %.3f; host ql %.3f; "
-                     "rotations %zu; n:",
-                     ms[0], ms[1], ms[2], ms[3], std::chrono::duration<double, std::milli>(th1 - th0).count(),
-                     rots.size());
+        std::fprintf(stderr, "itg tri begin (ms): reduce+copy %.3f host ql %.3f; n:",
+                     std::chrono::duration<double, std::milli>(t1 - t0).count(),
+                     std::chrono::duration<double, std::milli>(t2 - t1).count());
         for (int b = 0; b < nj; ++b) std::fprintf(stderr, " %d", items[b].n);
         std::fprintf(stderr, "\n");
-        for (auto& x : ev) cudaEventDestroy(x);
     }
-    return bad;
+    return P;
+}
+
+void tri_eigh_finish(Ctx& ctx, TriPending& P, std::vector<int> const& keep, double* vout, double* scratch) {
+    const int nj = (int)P.items.size();
+    if (nj == 0) return;
+    auto const& items = P.items;
+    int kmax = 0;
+    for (int b = 0; b < nj; ++b) {
+        const int k = P.status[b] == 0 ? std::max(0, std::min(keep.at(P.ids[b]), items[b].n)) : 0;
+        P.jobs[b].keep = k;
+        kmax = std::max(kmax, k);
+    }
+    if (kmax == 0) return;
+    const bool timing = std::getenv("ITG_EIG_TIME") != nullptr;
+    auto t0 = std::chrono::steady_clock::now();
+    // rows per tile of the rotation pass (lane = row): a full warp, fewer when
+    // shared memory runs out
+    int R = 32;
+    while (R > 1 && sizeof(double) * (size_t)R * P.nmax > TRI_SMEM_LIMIT) R /= 2;
+    // host: the reversed rotation sequence in mirrored columns, its lockstep
+    // schedule, and the kept eigenvalues' positions
+    std::vector<std::vector<QlSweep>> msw(nj);
+    std::vector<std::vector<QlRot>> mrot(nj);
+    std::vector<std::vector<int32_t>> woff(nj);
+    std::vector<std::vector<QlStart>> ent(nj);
+    std::vector<int> steps(nj, 0);
+    double work = 0;
+    for (int b = 0; b < nj; ++b) work += (double)P.rots[b].size() * (P.jobs[b].keep > 0);
+    for_blocks(nj, work * 8, [&](int b) {
+        const int n = items[b].n;
+        if (P.jobs[b].keep == 0) return;
+        auto const& sw = P.sweeps[b];
+        auto const& rt = P.rots[b];
+        msw[b].reserve(sw.size());
+        mrot[b].reserve(rt.size());
+        for (int t = (int)sw.size() - 1; t >= 0; --t) {
+            const int l = sw[t].l, m = sw[t].m, len = m - l;
+            msw[b].push_back(QlSweep{n - 1 - m, n - 1 - l, (int32_t)mrot[b].size(), 0});
+            for (int j = 0; j < len; ++j) mrot[b].push_back(rt[sw[t].off + (len - 1 - j)]);
+        }
+        steps[b] = ql_schedule(n, msw[b], TRI_ROT_WARPS, TRI_ROT_WINDOW, woff[b], ent[b]);
+    });
+    // blob: QlOut table | sweeps | rotations | schedules | kept positions
+    std::vector<QlOut> qo(nj);
+    size_t n_sw = 0, n_rot = 0, n_sched = 0, n_sel = 0;
+    for (int b = 0; b < nj; ++b) {
+        n_sw += msw[b].size();
+        n_rot += mrot[b].size();
+        n_sched += 2 * ((TRI_ROT_WARPS + 2) / 2) + 2 * ent[b].size();
+        n_sel += P.jobs[b].keep;
+    }
+    const size_t b_hdr = a16(sizeof(QlOut) * nj), b_rot = a16(b_hdr + sizeof(QlSweep) * n_sw);
+    const size_t b_sched = a16(b_rot + sizeof(QlRot) * n_rot), b_sel = a16(b_sched + sizeof(int32_t) * n_sched);
+    const size_t blob_bytes = a16(b_sel + sizeof(int32_t) * n_sel);
+    if (ctx.stage_bytes < blob_bytes) ctx.ensure_stage(blob_bytes + blob_bytes / 2);
+    char* st = static_cast<char*>(ctx.stage);
+    {
+        size_t o_sw = b_hdr, o_rot = b_rot, o_sc = b_sched, o_sel = b_sel;
+        for (int b = 0; b < nj; ++b) {
+            qo[b] = QlOut{};
+            if (P.jobs[b].keep == 0) continue;
+            qo[b].hdr_off = (int64_t)o_sw;
+            qo[b].rot_off = (int64_t)o_rot;
+            qo[b].sched_off = (int64_t)o_sc;
+            qo[b].sel_off = (int64_t)o_sel;
+            qo[b].nsweeps = (int32_t)msw[b].size();
+            qo[b].nsteps = steps[b];
+            std::memcpy(st + o_sw, msw[b].data(), sizeof(QlSweep) * msw[b].size());
+            o_sw += sizeof(QlSweep) * msw[b].size();
+            std::memcpy(st + o_rot, mrot[b].data(), sizeof(QlRot) * mrot[b].size());
+            o_rot += sizeof(QlRot) * mrot[b].size();
+            std::vector<int32_t> sc(woff[b]);
+            sc.resize(2 * ((TRI_ROT_WARPS + 2) / 2), 0);
+            for (auto const& x : ent[b]) { sc.push_back(x.step); sc.push_back(x.sweep); }
+            std::memcpy(st + o_sc, sc.data(), sizeof(int32_t) * sc.size());
+            o_sc += sizeof(int32_t) * sc.size();
+            std::memcpy(st + o_sel, P.order[b].data(), sizeof(int32_t) * P.jobs[b].keep);
+            o_sel += sizeof(int32_t) * P.jobs[b].keep;
+        }
+        std::memcpy(st, qo.data(), sizeof(QlOut) * nj);
+    }
+    DevBuf blob(blob_bytes, ctx.stream);
+    ITG_CHECK_CUDA(cudaMemcpyAsync(blob.p, st, blob_bytes, cudaMemcpyHostToDevice, ctx.stream));
+    // the jobs table again (now with the kept counts) and the tile lists, staged
+    // once the blob's copy has read the stage
+    std::vector<RowJob> rjobs;
+    std::vector<ColJob> cjobs;
+    for (int b = 0; b < nj; ++b) {
+        for (int r0 = 0; r0 < P.jobs[b].keep; r0 += R) rjobs.push_back(RowJob{b, r0});
+        for (int c0 = 0; c0 < P.jobs[b].keep; c0 += TRI_FORMQ_WARPS) cjobs.push_back(ColJob{b, c0});
+    }
+    const size_t jbytes = sizeof(TriJob) * nj, o_rj = a16(jbytes), o_cj = a16(o_rj + sizeof(RowJob) * rjobs.size());
+    const size_t tbytes = o_cj + sizeof(ColJob) * cjobs.size();
+    ctx.sync();
+    ctx.ensure_stage(tbytes);
+    st = static_cast<char*>(ctx.stage);
+    std::memcpy(st, P.jobs.data(), jbytes);
+    std::memcpy(st + o_rj, rjobs.data(), sizeof(RowJob) * rjobs.size());
+    std::memcpy(st + o_cj, cjobs.data(), sizeof(ColJob) * cjobs.size());
+    char* db = P.buf->as<char>();
+    ITG_CHECK_CUDA(cudaMemcpyAsync(db, st, jbytes, cudaMemcpyHostToDevice, ctx.stream));
+    DevBuf tabs(tbytes - o_rj + 16, ctx.stream);
+    ITG_CHECK_CUDA(cudaMemcpyAsync(tabs.p, st + o_rj, tbytes - o_rj, cudaMemcpyHostToDevice, ctx.stream));
+    TriJob const* d_jobs = reinterpret_cast<TriJob const*>(db);
+    double const* d_aux = reinterpret_cast<double const*>(db + P.o_aux);
+    RowJob const* d_rj = reinterpret_cast<RowJob const*>(tabs.as<char>());
+    ColJob const* d_cj = reinterpret_cast<ColJob const*>(tabs.as<char>() + (o_cj - o_rj));
+    auto t1 = std::chrono::steady_clock::now();
+    // 1. kept eigenvectors of the tridiagonal matrices (reversed rotations on unit vectors)
+    {
+        const size_t smem = sizeof(double) * (size_t)R * P.nmax;
+        if (smem > 48 * 1024)
+            ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_rot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        tri_rot_kernel<<<(int)rjobs.size(), TRI_ROT_WARPS * 32, smem, ctx.stream>>>(
+            d_rj, d_jobs, scratch, reinterpret_cast<QlOut const*>(blob.as<char>()), blob.as<char>(), R);
+        ITG_CHECK_CUDA(cudaGetLastError());
+        ctx.kernel_launches++;
+    }
+    // 2. back to the block's basis: the Householder reflectors applied to each kept column
+    {
+        const size_t smem = sizeof(double) * TRI_FORMQ_WARPS * (size_t)P.nmax;
+        if (smem > 48 * 1024)
+            ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_applyq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem));
+        tri_applyq_kernel<<<(int)cjobs.size(), TRI_FORMQ_WARPS * 32, smem, ctx.stream>>>(d_cj, d_jobs, scratch, d_aux,
+                                                                                        vout, P.nmax);
+        ITG_CHECK_CUDA(cudaGetLastError());
+        ctx.kernel_launches++;
+    }
+    ctx.sync();   // the stage and the blob are released
+    if (timing) {
+        auto t2 = std::chrono::steady_clock::now();
+        size_t kept = 0, tot = 0;
+        for (int b = 0; b < nj; ++b) { kept += P.jobs[b].keep; tot += items[b].n; }
+        std::fprintf(stderr, "itg tri finish (ms): host %.3f device %.3f; kept %zu of %zu\n",
+                     std::chrono::duration<double, std::milli>(t1 - t0).count(),
+                     std::chrono::duration<double, std::milli>(t2 - t1).count(), kept, tot);
+    }
 }
 
 }  // namespace itg

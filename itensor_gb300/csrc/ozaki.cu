@@ -70,10 +70,10 @@ __device__ __forceinline__ void oz_digits(double x, int emax, __nv_bfloat16* dst
     for (int s = 0; s < S; ++s) dst[s * plane] = __float2bfloat16_rn((float)dig[s]);
 }
 
-// One warp per row: the row's entries are read once into registers (rows of
-// up to 32 * OZ_PREP_REGS entries; longer rows are read a second time), the
-// exponent is a warp max, and the digits are written k-contiguous.
-constexpr int OZ_PREP_REGS = 8;
+// Rows of up to 32 * OZ_PREP_REGS entries: one warp per row, the row read once
+// into registers, the exponent a warp max, the digits written k-contiguous
+// (items of OZ_PREP_ITEM_ROWS rows, all rows in flight at once). Longer rows:
+// items of a few rows whose rows x K entries are spread over the whole CTA.
 template <int S>
 __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restrict__ items, const OpBlockRec* __restrict__ ops,
                                                          const int32_t* __restrict__ tab, const double* __restrict__ A,
@@ -83,6 +83,31 @@ __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restr
     const OpBlockRec ob = ops[pi.op];
     const double* __restrict__ base = (pi.which ? B : A) + ob.src;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (ob.Kp > 32 * OZ_PREP_REGS) {
+        // long rows: the item's rows x K entries spread over the CTA (a few rows per item)
+        __shared__ int rexp[OZ_PREP_LONG_ROWS];
+        __shared__ int32_t trow[OZ_PREP_LONG_ROWS];
+        const int rows = pi.r1 - pi.r0;
+        const int n = rows * ob.K;
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+            rexp[r] = 0;
+            trow[r] = tab_at(tab, ob.trow, pi.r0 + r);
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const int r = e % rows, k = e / rows;
+            atomicMax(&rexp[r], exp_field(base[trow[r] + tab_at(tab, ob.tcol, k)]));
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) exps[ob.exp + pi.r0 + r] = rexp[r] - 1022;
+        const int np = rows * ob.Kp;
+        __nv_bfloat16* pan = panels + ob.panel + (int64_t)pi.r0 * ob.Kp;
+        for (int e = threadIdx.x; e < np; e += blockDim.x) {
+            const int k = e % ob.Kp, r = e / ob.Kp;
+            oz_digits<S>(k < ob.K ? base[trow[r] + tab_at(tab, ob.tcol, k)] : 0.0, rexp[r], pan + e, plane);
+        }
+        return;
+    }
     for (int r = pi.r0 + warp; r < pi.r1; r += nw) {
         const int32_t ro = tab_at(tab, ob.trow, r);
         double xr[OZ_PREP_REGS];
