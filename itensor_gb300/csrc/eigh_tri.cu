@@ -43,7 +43,7 @@ namespace itg {
 
 namespace {
 constexpr int TRI_THREADS = 256;
-constexpr int TRI_FORMQ_WARPS = 4;
+constexpr int TRI_APPLYQ_WARPS = 4;       // kept vectors per CTA in the reflector stage (one warp each)
 constexpr int TRI_ROT_WARPS = 8;         // sweeps applied at once to one row tile
 constexpr int TRI_ROT_WINDOW = 4;        // lockstep steps between barriers
 constexpr size_t TRI_SMEM_LIMIT = 200 * 1024;
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_reduce_kernel(TriJob const* _
 // in the second half of the block's scratch): the eigenvectors of the block,
 // written to vout in eigenvalue order. One warp per column; H_k acts on rows
 // k+1..n-1 with v[k+1] = 1 and v[i] stored below the subdiagonal of column k.
-__global__ void __launch_bounds__(TRI_FORMQ_WARPS * 32) tri_applyq_kernel(ColJob const* __restrict__ cjobs,
+__global__ void __launch_bounds__(TRI_APPLYQ_WARPS * 32) tri_applyq_kernel(ColJob const* __restrict__ cjobs,
                                                                           TriJob const* __restrict__ jobs,
                                                                           double const* __restrict__ scratch,
                                                                           double const* __restrict__ aux,
@@ -599,7 +599,7 @@ void tri_eigh_finish(Ctx& ctx, TriPending& P, std::vector<int> const& keep, doub
     std::vector<ColJob> cjobs;
     for (int b = 0; b < nj; ++b) {
         for (int r0 = 0; r0 < P.jobs[b].keep; r0 += R) rjobs.push_back(RowJob{b, r0});
-        for (int c0 = 0; c0 < P.jobs[b].keep; c0 += TRI_FORMQ_WARPS) cjobs.push_back(ColJob{b, c0});
+        for (int c0 = 0; c0 < P.jobs[b].keep; c0 += TRI_APPLYQ_WARPS) cjobs.push_back(ColJob{b, c0});
     }
     const size_t jbytes = sizeof(TriJob) * nj, o_rj = a16(jbytes), o_cj = a16(o_rj + sizeof(RowJob) * rjobs.size());
     const size_t tbytes = o_cj + sizeof(ColJob) * cjobs.size();
@@ -630,11 +630,11 @@ void tri_eigh_finish(Ctx& ctx, TriPending& P, std::vector<int> const& keep, doub
     }
     // 2. back to the block's basis: the Householder reflectors applied to each kept column
     {
-        const size_t smem = sizeof(double) * TRI_FORMQ_WARPS * (size_t)P.nmax;
+        const size_t smem = sizeof(double) * TRI_APPLYQ_WARPS * (size_t)P.nmax;
         if (smem > 48 * 1024)
             ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_applyq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem));
-        tri_applyq_kernel<<<(int)cjobs.size(), TRI_FORMQ_WARPS * 32, smem, ctx.stream>>>(d_cj, d_jobs, scratch, d_aux,
+        tri_applyq_kernel<<<(int)cjobs.size(), TRI_APPLYQ_WARPS * 32, smem, ctx.stream>>>(d_cj, d_jobs, scratch, d_aux,
                                                                                         vout, P.nmax);
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;
