@@ -7,6 +7,7 @@ Restates:
   * LocalMPO position/makeL/makeR itensor/mps/localmpo.h:443-470, 542-618
   * MPS::svdBond                  itensor/mps/mps_impl.h:21-99
   * DMRGWorker / sweepnext        itensor/mps/dmrg.h:336-467, itensor/mps/sweeps.h:489-503
+  * LocalMPOSet (sums of MPOs)   itensor/mps/localmposet.h:140-176
   * LocalMPO of an MPS, LocalMPO_MPS (excited states)
                                   itensor/mps/localmpo.h:340-349, 389-421, 543-594;
                                   itensor/mps/localmpo_mps.h:98-156; itensor/mps/dmrg.h:245-266
@@ -234,6 +235,29 @@ class LocalMPS:
         return o.dag().scale(z)
 
 
+class OpSum:
+    """LocalMPOSet::product (itensor/mps/localmposet.h:140-152): the sum of the
+    local products of several MPOs on the same sites; deltaRho summed (:166-176)."""
+
+    def __init__(self, ops):
+        self.ops = ops
+
+    def product(self, phi):
+        p = self.ops[0].product(phi)
+        for op in self.ops[1:]:
+            p = p + op.product(phi)
+        return p
+
+    def delta_rho(self, AA, cmb, fromleft):
+        d = self.ops[0].delta_rho(AA, cmb, fromleft)
+        for op in self.ops[1:]:
+            d = d + op.delta_rho(AA, cmb, fromleft)
+        return d
+
+    def size(self, phi):
+        return self.ops[0].size(phi)
+
+
 class ProjectedOp:
     """LocalMPO_MPS::product: H phi + weight * sum_j P_j phi; deltaRho and size
     from the MPO part (itensor/mps/localmpo_mps.h:65-72, 137-150)."""
@@ -268,13 +292,17 @@ def dmrg(W, psi, sweeps, record=None, usesvd=None, psis=None, weight=1.0, site_i
     |psi_j><psi_j|, itensor/mps/dmrg.h:245-266); site_ids: ids of the site indices."""
     psi = list(psi)
     N = len(psi)
-    PH = LocalMPO(W)
+    # W: one MPO (list of site tensors) or a list of MPOs whose sum is H
+    # (dmrg(psi, {H1, H2, ...}, sweeps), itensor/mps/dmrg.h:181-230)
+    Wset = W if isinstance(W[0], list) else [W]
+    PHs = [LocalMPO(w) for w in Wset]
     projs = [LocalMPS(p, site_ids) for p in (psis or [])]
     energy = np.nan
     recs = []
     for sw, s in enumerate(sweeps, start=1):
         for b, ha in sweep_bonds(N):
-            op = PH.position(b, psi)
+            ops = [P.position(b, psi) for P in PHs]
+            op = ops[0] if len(ops) == 1 else OpSum(ops)
             if projs:
                 for M in projs:
                     M.position(b, psi)

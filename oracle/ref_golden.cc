@@ -563,6 +563,27 @@ static std::string run_dmrg_excited(std::string const& name, SitesT const& sites
     return o.str();
 }
 
+// dmrg with a sum of MPOs (itensor/mps/dmrg.h:209-230, LocalMPOSet of
+// itensor/mps/localmposet.h), recorded like run_dmrg.
+template <typename SitesT>
+static std::string run_dmrg_set(std::string const& name, SitesT const& sites, std::vector<MPO> const& Hs,
+                                MPS const& psi0, Sweeps const& sw, std::string const& model) {
+    Recorder obs(psi0);
+    auto [E, psi] = dmrg(Hs, psi0, sw, obs, {"Quiet", true, "Silent", true});
+    std::ostringstream o;
+    o << "{\"name\":\"" << name << "\",\"model\":" << model << ",\"N\":" << length(psi) << ",\"sweeps\":[";
+    for (int s = 1; s <= sw.nsweep(); ++s) {
+        if (s > 1) o << ",";
+        o << "{\"maxdim\":" << sw.maxdim(s) << ",\"mindim\":" << sw.mindim(s) << ",\"cutoff\":" << num(sw.cutoff(s))
+          << ",\"niter\":" << sw.niter(s) << ",\"noise\":" << num(sw.noise(s)) << "}";
+    }
+    o << "],\"energy\":" << num(E) << ",\"bonds\":[" << obs.rec.str() << "],\"links\":[";
+    for (int b = 1; b < length(psi); ++b) { if (b > 1) o << ","; o << jindex(linkIndex(psi, b)); }
+    o << "]}";
+    std::printf("  %s: E=%.15f maxlink=%ld\n", name.c_str(), E, maxLinkDim(psi));
+    return o.str();
+}
+
 static Sweeps mksweeps(std::vector<int> maxdims, double cutoff, int niter = 2) {
     auto sw = Sweeps((int)maxdims.size());
     for (int s = 1; s <= (int)maxdims.size(); ++s) {
@@ -628,6 +649,20 @@ static void gen_dmrg(std::string const& dir) {
         auto H = toMPO(ampo);
         cs.push_back(run_dmrg("j1j2_16", sites, H, neel_mps(sites, N), mksweeps({10, 20, 40, 60}, 1e-10),
                               "{\"type\":\"j1j2\",\"J2\":0.3}"));
+        // the same Hamiltonian as a sum of two MPOs: nearest and next-nearest neighbours
+        auto a1 = AutoMPO(sites), a2 = AutoMPO(sites);
+        for (int j = 1; j < N; ++j) {
+            a1 += 0.5, "S+", j, "S-", j + 1;
+            a1 += 0.5, "S-", j, "S+", j + 1;
+            a1 += "Sz", j, "Sz", j + 1;
+        }
+        for (int j = 1; j < N - 1; ++j) {
+            a2 += 0.5 * J2, "S+", j, "S-", j + 2;
+            a2 += 0.5 * J2, "S-", j, "S+", j + 2;
+            a2 += J2, "Sz", j, "Sz", j + 2;
+        }
+        cs.push_back(run_dmrg_set("j1j2_16_set", sites, std::vector<MPO>{toMPO(a1), toMPO(a2)}, neel_mps(sites, N),
+                                  mksweeps({10, 20, 40, 60}, 1e-10), "{\"type\":\"j1j2\",\"J2\":0.3}"));
     }
     {   // transverse-field Ising N=16 with parity QN: H = -sum Sx Sx - h sum Sz, all Up
         int N = 16; double h = 0.5;

@@ -134,3 +134,24 @@ def test_dmrg_excited_state(golden):
         assert abs(a[3] - b[3]) < ENERGY_TOL
         assert abs(a[4] - b[4]) < 1e-12
         assert a[5] == b[5]
+
+
+def test_dmrg_mpo_sum(golden):
+    """dmrg with a sum of MPOs (LocalMPOSet, itensor/mps/localmposet.h): the J1-J2
+    chain as nearest- plus next-nearest-neighbour MPOs, against the reference."""
+    c = [x for x in golden("dmrg")["cases"] if x["name"] == "j1j2_16_set"][0]
+    N = c["N"]
+    H1 = models.heisenberg(N)
+    H2 = models.heisenberg(N, J=0.0, J2=c["model"]["J2"])
+    H2.two = [t for t in H2.two if t[0] != 0.0]
+    sites, W1, _ = models.build_mpo(H1)
+    _, W2, _ = models.build_mpo(H2, sites=sites)
+    psi = models.product_mps(sites, H1.st, ["Up" if i % 2 == 0 else "Dn" for i in range(N)])
+    E, psi2, recs = dmrg([W1, W2], psi, c["sweeps"])
+    assert abs(E - c["energy"]) < ENERGY_TOL
+    assert len(recs) == len(c["bonds"])
+    for a, b in zip(recs, c["bonds"]):
+        assert tuple(a[:3]) == tuple(b[:3])
+        assert abs(a[3] - b[3]) < ENERGY_TOL
+        assert abs(a[4] - b[4]) < 1e-12
+        assert a[5] == b[5]
