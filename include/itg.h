@@ -237,6 +237,13 @@ typedef struct {
 
 int itg_dmrg_run(itg_ctx* ctx, const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps,
                  int precision, itg_dmrg_result** out);
+/* Sums of MPOs: dmrg(psi, {H1, H2, ...}, sweeps) with LocalMPOSet
+ * (itensor/mps/dmrg.h:181-230, itensor/mps/localmposet.h): H is the sum of the
+ * models' Hamiltonians (same site type and length; one MPO each, on shared site
+ * indices), the product state from models[0]. The noise term is refused with
+ * a sum. */
+int itg_dmrg_run_sum(itg_ctx* ctx, const itg_model_desc* models, int32_t nmodels, const itg_sweep_desc* sweeps,
+                     int32_t nsweeps, int precision, itg_dmrg_result** out);
 /* Excited states: dmrg(H, psis, psi0, sweeps, {"Weight", weight}) of
  * itensor/mps/dmrg.h:245-266 with LocalMPO_MPS (itensor/mps/localmpo_mps.h),
  * chained. State 0 is the ground state from the model's default product

@@ -100,6 +100,8 @@ SIGNATURES = {
                                 C.POINTER(C.c_void_p), _f64p, _f64p, _i32p]),
     "itg_truncate": (C.c_int, [_f64p, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int, C.c_int, C.c_int, _f64p,
                                _i32p, _f64p, _f64p, _f64p, _i32p]),
+    "itg_dmrg_run_sum": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.c_int32, C.POINTER(SweepDesc), C.c_int32,
+                                   C.c_int, C.POINTER(C.c_void_p)]),
     "itg_dmrg_run_states": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.c_int32, C.POINTER(C.POINTER(SweepDesc)),
                                       _i32p, C.c_double, C.c_int, C.POINTER(C.c_void_p)]),
     "itg_dmrg_run": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.POINTER(SweepDesc), C.c_int32, C.c_int,
@@ -486,6 +488,14 @@ class Context:
         sw = _sweep_descs(sweeps)
         out = C.c_void_p()
         self._ok(lib().itg_dmrg_run(self.h, C.byref(md), sw, len(sweeps), precision, C.byref(out)), self.h)
+        return _take_dmrg_result(out)
+
+    def dmrg_sum(self, models, sweeps, precision=-1):
+        """DMRG of the sum of the models' Hamiltonians (one MPO each, LocalMPOSet)."""
+        mds = (ModelDesc * len(models))(*[_model_desc(m) for m in models])
+        sw = _sweep_descs(sweeps)
+        out = C.c_void_p()
+        self._ok(lib().itg_dmrg_run_sum(self.h, mds, len(models), sw, len(sweeps), precision, C.byref(out)), self.h)
         return _take_dmrg_result(out)
 
     def dmrg_states(self, model, sweeps_per_state, weight, precision=-1):

@@ -49,6 +49,9 @@ struct LocalOp {
     // apply adds proj_weight * sum_j P_j (P_j . phi), P_j stored in phi's layout.
     std::vector<Tensor> const* proj = nullptr;
     double proj_weight = 0.0;
+    // Sums of MPOs (LocalMPOSet, itensor/mps/localmposet.h:140-152): the local
+    // operators of the other MPOs, whose products are added to this one's.
+    std::vector<LocalOp> const* terms = nullptr;
 };
 // H_eff * phi written in phi's layout (phi must hold every block of its divergence).
 // into_phi_layout=false returns the reference's own output structure instead.
@@ -160,7 +163,8 @@ struct MPO {
     std::vector<Tensor> W;      // W_n: (dag(s_n), s_n', dag(link_{n-1}), link_n), ends projected
     int bond_dim = 0;
 };
-MPO build_mpo(Ctx& ctx, Hamiltonian const& H);
+// sites: the site indices to use (another MPO's, for sums of MPOs); new ones if null.
+MPO build_mpo(Ctx& ctx, Hamiltonian const& H, std::vector<Index> const* sites = nullptr);
 // Product state with the link QNs of MPS(InitState) (itensor/mps/mps.cc:558-585).
 std::vector<Tensor> product_mps(Ctx& ctx, MPO const& H, SiteType const& st, std::vector<int> const& states);
 std::vector<int> default_state(ModelSpec const& m);
@@ -189,7 +193,10 @@ struct DmrgResult {
 // With `prev`, the state that minimises H + weight sum_j |psi_j><psi_j| (the
 // excited-state dmrg of itensor/mps/dmrg.h:245-266, LocalMPO_MPS of
 // itensor/mps/localmpo_mps.h): prev holds earlier results' MPS in the same QN sector.
+// With `more`, H is the sum of H and the MPOs in `more` (on the same sites):
+// dmrg(psi, {H1, H2, ...}, sweeps) with LocalMPOSet (itensor/mps/dmrg.h:181-230).
 DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<SweepSpec> const& sweeps, int prec,
-                std::vector<std::vector<Tensor>> const* prev = nullptr, double weight = 1.0);
+                std::vector<std::vector<Tensor>> const* prev = nullptr, double weight = 1.0,
+                std::vector<MPO> const* more = nullptr);
 
 }  // namespace itg

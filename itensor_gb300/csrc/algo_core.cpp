@@ -432,9 +432,21 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
         pptr[j] = (*op.proj)[j].data();
     }
     std::vector<double> pz(std::max(nproj, 1));
+    // the other MPOs of a sum, each its own prepared program, added to y
+    std::vector<std::shared_ptr<HeffProgram>> more;
+    if (op.terms)
+        for (auto const& t : *op.terms) more.push_back(heff_prepare(ctx, t, phi.lay, prec, true, false));
+    Tensor tmp;
+    if (!more.empty()) tmp = Tensor(phi.lay, ctx.stream);
     auto apply = [&](Tensor const& x) {
         Tensor y(phi.lay, ctx.stream);
         prog->run(ctx, x.data(), y.data());
+        for (auto const& p : more) {
+            p->run(ctx, x.data(), tmp.data());
+            VecList X;
+            X.add(tmp.data(), 1.0);
+            combo(ctx, y.data(), 1.0, X, n, false);
+        }
         if (nproj) {
             // y += w sum_j P_j (P_j . x)
             dots(ctx, pptr.data(), nproj, x.data(), n, pz.data());

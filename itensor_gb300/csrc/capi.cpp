@@ -513,6 +513,36 @@ int itg_dmrg_run(itg_ctx* c, const itg_model_desc* model, const itg_sweep_desc* 
     });
 }
 
+int itg_dmrg_run_sum(itg_ctx* c, const itg_model_desc* models, int32_t nmodels, const itg_sweep_desc* sweeps,
+                     int32_t nsweeps, int precision, itg_dmrg_result** out) {
+    return guard(c, [&] {
+        ITG_REQUIRE(models && nmodels >= 1 && sweeps && nsweeps > 0 && out, "dmrg_run_sum: bad arguments");
+        ModelSpec m0 = model_from(models[0]);
+        Hamiltonian H0 = make_hamiltonian(m0);
+        ITG_REQUIRE(H0.N >= 2, "dmrg_run_sum: need at least two sites");
+        MPO mpo = build_mpo(c->ctx, H0);
+        std::vector<MPO> more;
+        for (int k = 1; k < nmodels; ++k) {
+            ModelSpec mk = model_from(models[k]);
+            ITG_REQUIRE(mk.type == m0.type, "dmrg_run_sum: the models must share their site type");
+            Hamiltonian Hk = make_hamiltonian(mk);
+            ITG_REQUIRE(Hk.N == H0.N, "dmrg_run_sum: the models must have the same number of sites");
+            more.push_back(build_mpo(c->ctx, Hk, &mpo.sites));
+        }
+        auto psi = product_mps(c->ctx, mpo, H0.st, default_state(m0));
+        std::vector<SweepSpec> sw = sweeps_from(sweeps, nsweeps);
+        auto* res = new itg_dmrg_result;
+        try {
+            res->r = dmrg(c->ctx, mpo, psi, sw, precision, nullptr, 1.0, more.empty() ? nullptr : &more);
+            res->r.psi.clear();
+        } catch (...) {
+            delete res;
+            throw;
+        }
+        *out = res;
+    });
+}
+
 int itg_dmrg_run_states(itg_ctx* c, const itg_model_desc* model, int32_t nstates, const itg_sweep_desc* const* sweeps,
                         const int32_t* nsweeps, double weight, int precision, itg_dmrg_result** out) {
     return guard(c, [&] {

@@ -97,10 +97,20 @@ struct MpsEnvironments {
 }  // namespace
 
 DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<SweepSpec> const& sweeps, int prec,
-                std::vector<std::vector<Tensor>> const* prev, double weight) {
+                std::vector<std::vector<Tensor>> const* prev, double weight, std::vector<MPO> const* more) {
     const int N = (int)psi.size();
     ITG_REQUIRE(N >= 2 && (int)H.W.size() == N, "dmrg: MPO and MPS lengths differ");
     Environments env(H.W);
+    std::vector<Environments> menv;
+    if (more)
+        for (auto const& M : *more) {
+            ITG_REQUIRE((int)M.W.size() == N, "dmrg: an MPO of the sum has another length");
+            menv.emplace_back(M.W);
+        }
+    std::vector<LocalOp> mops(menv.size());
+    if (!menv.empty())
+        for (auto const& s : sweeps)
+            ITG_REQUIRE(s.noise == 0.0, "dmrg: the noise term with a sum of MPOs is not supported");
     std::vector<MpsEnvironments> penv;
     if (prev)
         for (auto const& p : *prev) {
@@ -127,6 +137,10 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
             for (int j : mt.b_unc) pinds.push_back(B.inds()[j]);
             auto full = std::make_shared<Layout>(allowed_layout(pinds, tensor_div(A) + tensor_div(B)));
             Tensor phi = contract(ctx, A, B, prec, full);
+            if (!menv.empty()) {
+                for (size_t k = 0; k < menv.size(); ++k) mops[k] = menv[k].position(ctx, b, psi, prec);
+                op.terms = &mops;
+            }
             if (!penv.empty()) {
                 for (size_t j = 0; j < penv.size(); ++j) proj[j] = penv[j].projector(ctx, b, psi, full, PREC_F64);
                 op.proj = &proj;

@@ -134,6 +134,10 @@ Hamiltonian make_hamiltonian(ModelSpec const& m) {
     } else {
         throw Error(ERR_ARG, "unknown model type");
     }
+    // terms with a zero coefficient carry no MPO channel (a model may set J = 0
+    // to hold only the next-nearest terms of a sum of MPOs)
+    H.two.erase(std::remove_if(H.two.begin(), H.two.end(), [](Term2 const& t) { return t.c == 0.0; }), H.two.end());
+    H.one.erase(std::remove_if(H.one.begin(), H.one.end(), [](Term1 const& t) { return t.c == 0.0; }), H.one.end());
     return H;
 }
 
@@ -184,7 +188,7 @@ int mpo_bond_dim(Hamiltonian const& H) {
     return 2 + (int)lefts.size() * rng;
 }
 
-MPO build_mpo(Ctx& ctx, Hamiltonian const& H) {
+MPO build_mpo(Ctx& ctx, Hamiltonian const& H, std::vector<Index> const* sites) {
     SiteType const& st = H.st;
     const int N = H.N, d = st.d();
     std::vector<std::string> lefts;
@@ -215,7 +219,12 @@ MPO build_mpo(Ctx& ctx, Hamiltonian const& H) {
     mpo.bond_dim = D;
     std::vector<Index> links;
     for (int l = 0; l <= N; ++l) links.push_back(Index(secq, secd, 1));
-    for (int n = 0; n < N; ++n) mpo.sites.push_back(Index(st.qn, std::vector<int32_t>(d, 1), 1));
+    if (sites) {
+        ITG_REQUIRE((int)sites->size() == N, "build_mpo: site list of another length");
+        mpo.sites = *sites;
+    } else {
+        for (int n = 0; n < N; ++n) mpo.sites.push_back(Index(st.qn, std::vector<int32_t>(d, 1), 1));
+    }
     for (int n = 1; n <= N; ++n) {
         // dense W[s_in, s_out, row, col]
         std::vector<double> W((size_t)d * d * D * D, 0.0);

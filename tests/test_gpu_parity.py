@@ -375,3 +375,19 @@ def test_dmrg_excited_golden(ctx, golden, prec):
             assert a[5] == b[5]
         for (dr, qn, dims), ref in zip(res[1].links, c["links"]):
             assert [int(x) for x in dims] == [d for _, d in ref["sectors"]]
+
+
+def test_dmrg_mpo_sum_golden(ctx, golden):
+    """DMRG of a sum of two MPOs (the J1-J2 chain as nearest- plus next-nearest-
+    neighbour MPOs) through the C-ABI against the reference's LocalMPOSet run."""
+    c = [x for x in golden("dmrg")["cases"] if x["name"] == "j1j2_16_set"][0]
+    N, J2 = c["N"], c["model"]["J2"]
+    res = ctx.dmrg_sum([dict(type=0, N=N, J=1.0, Jz=1.0), dict(type=0, N=N, J=0.0, Jz=0.0, J2=J2)], c["sweeps"],
+                       precision=0)
+    assert abs(res.energy - c["energy"]) < ENERGY_TOL
+    assert len(res.bonds) == len(c["bonds"])
+    for a, b in zip(res.bonds, c["bonds"]):
+        assert tuple(a[:3]) == tuple(b[:3])
+        assert abs(a[3] - b[3]) < ENERGY_TOL, (a, b)
+        assert abs(a[4] - b[4]) < 1e-12
+        assert a[5] == b[5]
