@@ -240,8 +240,8 @@ int itg_dmrg_run(itg_ctx* ctx, const itg_model_desc* model, const itg_sweep_desc
 /* Sums of MPOs: dmrg(psi, {H1, H2, ...}, sweeps) with LocalMPOSet
  * (itensor/mps/dmrg.h:181-230, itensor/mps/localmposet.h): H is the sum of the
  * models' Hamiltonians (same site type and length; one MPO each, on shared site
- * indices), the product state from models[0]. The noise term is refused with
- * a sum. */
+ * indices), the product state from models[0]. With noise, the density
+ * matrix gets the sum of every MPO's noise term (itensor/mps/localmposet.h:166-176). */
 int itg_dmrg_run_sum(itg_ctx* ctx, const itg_model_desc* models, int32_t nmodels, const itg_sweep_desc* sweeps,
                      int32_t nsweeps, int precision, itg_dmrg_result** out);
 /* Excited states: dmrg(H, psis, psi0, sweeps, {"Weight", weight}) of

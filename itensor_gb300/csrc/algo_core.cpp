@@ -548,27 +548,34 @@ Tensor delta_rho(Ctx& ctx, LocalOp const& op, Tensor const& AA, Combiner const& 
     return contract(ctx, Xc, relabel(Xc, dinds), PREC_F64);
 }
 
-// rho + noise * (D + D^T)/2 on the union of both block structures, divided by
-// its trace (itensor/decomp.h:386-394; ITensor's += keeps every block of both).
-static Tensor noisy_rho(Ctx& ctx, Tensor const& rho, Tensor const& D, double noise) {
+// rho + noise * sum_k (D_k + D_k^T)/2 on the union of the block structures,
+// divided by its trace (itensor/decomp.h:386-394; ITensor's += keeps every
+// block of either operand).
+static Tensor noisy_rho(Ctx& ctx, Tensor const& rho, std::vector<Tensor> const& Ds, double noise) {
     Layout const& RL = *rho.lay;
-    Layout const& DL = *D.lay;
     std::vector<int32_t> coords(RL.coords);
-    coords.insert(coords.end(), DL.coords.begin(), DL.coords.end());
+    for (auto const& D : Ds) coords.insert(coords.end(), D.lay->coords.begin(), D.lay->coords.end());
     auto UL = std::make_shared<Layout>(make_layout(rho.inds(), coords));
     Tensor out(UL, ctx.stream);
-    std::vector<NoiseBlock> blocks(UL->nblocks());
-    for (int b = 0; b < UL->nblocks(); ++b) {
-        int32_t const* c = UL->block(b);
-        ITG_REQUIRE(c[0] == c[1], "noisy_rho: density matrix block off the diagonal");
-        const int rb = RL.find_block(c), db = DL.find_block(c);
-        blocks[b].out_off = UL->offs[b];
-        blocks[b].rho_off = rb >= 0 ? RL.offs[rb] : -1;
-        blocks[b].d_off = db >= 0 ? DL.offs[db] : -1;
-        blocks[b].n = (int32_t)rho.inds()[0].bdim(c[0]);
-        blocks[b].pad = 0;
+    std::vector<std::vector<NoiseBlock>> passes(Ds.size(), std::vector<NoiseBlock>(UL->nblocks()));
+    std::vector<double const*> ds;
+    for (size_t k = 0; k < Ds.size(); ++k) {
+        Layout const& DL = *Ds[k].lay;
+        ds.push_back(Ds[k].data());
+        for (int b = 0; b < UL->nblocks(); ++b) {
+            int32_t const* c = UL->block(b);
+            ITG_REQUIRE(c[0] == c[1], "noisy_rho: density matrix block off the diagonal");
+            const int rb = RL.find_block(c), db = DL.find_block(c);
+            NoiseBlock& nb = passes[k][b];
+            nb.out_off = UL->offs[b];
+            // pass 0 reads rho (or nothing where rho has no block); later passes read out
+            nb.rho_off = k == 0 ? (rb >= 0 ? RL.offs[rb] : -1) : UL->offs[b];
+            nb.d_off = db >= 0 ? DL.offs[db] : -1;
+            nb.n = (int32_t)rho.inds()[0].bdim(c[0]);
+            nb.pad = 0;
+        }
     }
-    launch_noisy_rho(ctx, blocks, rho.data(), D.data(), out.data(), UL->size, noise);
+    launch_noisy_rho(ctx, passes, rho.data(), ds, out.data(), UL->size, noise);
     return out;
 }
 
@@ -585,7 +592,13 @@ SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor co
     std::vector<Index> dinds = dag_all(AAc.inds());
     dinds[0] = dinds[0].prime();
     Tensor rho = contract(ctx, AAc, relabel(AAc, dinds), PREC_F64);
-    if (noise > 0 && op) rho = noisy_rho(ctx, rho, delta_rho(ctx, *op, AA, cmb, fromleft), noise);
+    if (noise > 0 && op) {
+        // LocalMPOSet::deltaRho sums the terms of every MPO (itensor/mps/localmposet.h:166-176)
+        std::vector<Tensor> Ds{delta_rho(ctx, *op, AA, cmb, fromleft)};
+        if (op->terms)
+            for (auto const& t : *op->terms) Ds.push_back(delta_rho(ctx, t, AA, cmb, fromleft));
+        rho = noisy_rho(ctx, rho, Ds, noise);
+    }
     Layout const& RL = *rho.lay;
     // one eigenproblem per diagonal block, in storage order
     const int nb = RL.nblocks();

@@ -108,9 +108,6 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
             menv.emplace_back(M.W);
         }
     std::vector<LocalOp> mops(menv.size());
-    if (!menv.empty())
-        for (auto const& s : sweeps)
-            ITG_REQUIRE(s.noise == 0.0, "dmrg: the noise term with a sum of MPOs is not supported");
     std::vector<MpsEnvironments> penv;
     if (prev)
         for (auto const& p : *prev) {

@@ -299,8 +299,10 @@ void launch_gather(Ctx& ctx, GatherPlan const& g, double const* src, double* dst
 // ------------------------------------------------------------------ noisy density matrix
 // rho + noise * deltaRho with deltaRho's Hermitian part (itensor/mps/localop.h:399-403):
 // one CTA per diagonal block.
-__global__ void noisy_rho_kernel(NoiseBlock const* __restrict__ blocks, double const* __restrict__ rho,
-                                 double const* __restrict__ d, double* __restrict__ out, double half_noise) {
+// rho and out may be the same buffer (a later pass accumulates in place): each
+// element is read and written by the same thread.
+__global__ void noisy_rho_kernel(NoiseBlock const* __restrict__ blocks, double const* rho,
+                                 double const* __restrict__ d, double* out, double half_noise) {
     const NoiseBlock bk = blocks[blockIdx.x];
     const int64_t n = bk.n;
     for (int64_t e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -338,23 +340,31 @@ __global__ void trace_normalise_kernel(double* __restrict__ x, int64_t n, double
         x[i] *= inv;
 }
 
-void launch_noisy_rho(Ctx& ctx, std::vector<NoiseBlock> const& blocks, double const* rho, double const* d,
-                      double* out, int64_t out_size, double noise) {
-    if (blocks.empty()) return;
-    const size_t bytes = sizeof(NoiseBlock) * blocks.size();
+void launch_noisy_rho(Ctx& ctx, std::vector<std::vector<NoiseBlock>> const& passes, double const* rho,
+                      std::vector<double const*> const& ds, double* out, int64_t out_size, double noise) {
+    if (passes.empty() || passes[0].empty()) return;
+    const size_t nb = passes[0].size(), pbytes = sizeof(NoiseBlock) * nb;
+    const size_t bytes = pbytes * passes.size();
     ctx.ensure_stage(bytes);
-    std::memcpy(ctx.stage, blocks.data(), bytes);
+    for (size_t k = 0; k < passes.size(); ++k) {
+        ITG_REQUIRE(passes[k].size() == nb, "noisy_rho: passes over different block lists");
+        std::memcpy(static_cast<char*>(ctx.stage) + k * pbytes, passes[k].data(), pbytes);
+    }
     DevBuf tab(bytes + 16, ctx.stream);
     ITG_CHECK_CUDA(cudaMemcpyAsync(tab.as<char>(), ctx.stage, bytes, cudaMemcpyHostToDevice, ctx.stream));
-    NoiseBlock const* dblocks = reinterpret_cast<NoiseBlock const*>(tab.as<char>());
     double* dtr = reinterpret_cast<double*>(tab.as<char>() + bytes);
-    noisy_rho_kernel<<<(int)blocks.size(), 256, 0, ctx.stream>>>(dblocks, rho, d, out, 0.5 * noise);
-    ITG_CHECK_CUDA(cudaGetLastError());
-    block_trace_kernel<<<1, TRACE_THREADS, 0, ctx.stream>>>(dblocks, (int)blocks.size(), out, dtr);
+    // pass 0: out = rho + noise (D_0 + D_0^T)/2; pass k: out += noise (D_k + D_k^T)/2 (in place)
+    for (size_t k = 0; k < passes.size(); ++k) {
+        NoiseBlock const* dblocks = reinterpret_cast<NoiseBlock const*>(tab.as<char>() + k * pbytes);
+        noisy_rho_kernel<<<(int)nb, 256, 0, ctx.stream>>>(dblocks, k == 0 ? rho : out, ds[k], out, 0.5 * noise);
+        ITG_CHECK_CUDA(cudaGetLastError());
+    }
+    NoiseBlock const* dblocks0 = reinterpret_cast<NoiseBlock const*>(tab.as<char>());
+    block_trace_kernel<<<1, TRACE_THREADS, 0, ctx.stream>>>(dblocks0, (int)nb, out, dtr);
     ITG_CHECK_CUDA(cudaGetLastError());
     trace_normalise_kernel<<<grid_for(ctx, out_size), 256, 0, ctx.stream>>>(out, out_size, dtr);
     ITG_CHECK_CUDA(cudaGetLastError());
-    ctx.kernel_launches += 3;
+    ctx.kernel_launches += passes.size() + 2;
     // the staging buffer is reused by the next upload: wait until the copy has read it
     ctx.sync();
 }

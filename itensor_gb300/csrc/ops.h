@@ -36,8 +36,10 @@ struct NoiseBlock {
 // Writes every block of `out` (blocks listed in storage order), then divides
 // out by its trace when the trace exceeds 1e-16 (itensor/decomp.h:386-394).
 // Device-side throughout: no host wait.
-void launch_noisy_rho(Ctx& ctx, std::vector<NoiseBlock> const& blocks, double const* rho, double const* d,
-                      double* out, int64_t out_size, double noise);
+// Several noise terms (a sum of MPOs): one pass per term over the same block
+// list, the first from rho, the others added in place; one trace at the end.
+void launch_noisy_rho(Ctx& ctx, std::vector<std::vector<NoiseBlock>> const& passes, double const* rho,
+                      std::vector<double const*> const& ds, double* out, int64_t out_size, double noise);
 
 // One symmetric n x n matrix (column-major) to diagonalise.
 struct EigItem {

@@ -391,3 +391,29 @@ def test_dmrg_mpo_sum_golden(ctx, golden):
         assert abs(a[3] - b[3]) < ENERGY_TOL, (a, b)
         assert abs(a[4] - b[4]) < 1e-12
         assert a[5] == b[5]
+
+
+def test_dmrg_mpo_sum_noise_matches_oracle(ctx):
+    """The noise term of a sum of MPOs (every MPO's deltaRho added, LocalMPOSet)
+    against the oracle on the same MPOs: the J1-J2 chain N=10 as two MPOs."""
+    from oracle import models
+    from oracle.dmrg import dmrg as odmrg
+    N, J2 = 10, 0.3
+    sweeps = [dict(maxdim=m, mindim=1, cutoff=1e-10, niter=2, noise=nz)
+              for m, nz in ((8, 1e-5), (16, 1e-6), (24, 0.0))]
+    res = ctx.dmrg_sum([dict(type=0, N=N, J=1.0, Jz=1.0), dict(type=0, N=N, J=0.0, Jz=0.0, J2=J2)], sweeps,
+                       precision=0)
+    H1 = models.heisenberg(N)
+    H2 = models.heisenberg(N, J=0.0, J2=J2)
+    H2.two = [t for t in H2.two if t[0] != 0.0]
+    sites, W1, _ = models.build_mpo(H1)
+    _, W2, _ = models.build_mpo(H2, sites=sites)
+    psi = models.product_mps(sites, H1.st, ["Up" if i % 2 == 0 else "Dn" for i in range(N)])
+    E, _, recs = odmrg([W1, W2], psi, sweeps)
+    assert abs(res.energy - E) < 1e-10
+    assert len(res.bonds) == len(recs)
+    for a, b in zip(res.bonds, recs):
+        assert tuple(a[:3]) == tuple(b[:3])
+        assert abs(a[3] - b[3]) < 1e-7, (a, b)
+        assert abs(a[4] - b[4]) < 1e-11
+        assert a[5] == b[5]
