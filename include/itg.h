@@ -141,9 +141,10 @@ void itg_plan_free(itg_plan* plan);
  * operands are the caller's; the digit-panel scratch lives in one fixed
  * device array of ITG_NOALLOC_SCRATCH_BYTES per device, held until exit.
  * A plan needing more scratch is rejected with ITG_ERR_RANGE. The first call
- * on a device looks up the array's address (cudaGetSymbolAddress) and should
- * come before any stream capture. Calls share the array: calls that overlap on
- * the GPU race. Nothing in the array needs to start at zero. */
+ * from each CUDA context on a device (the primary context, or one the caller
+ * made current) looks up the array's address there (cudaGetSymbolAddress) and
+ * should come before any stream capture. Calls share the array: calls that
+ * overlap on the GPU race. Nothing in the array needs to start at zero. */
 #define ITG_NOALLOC_SCRATCH_BYTES (16u << 20)
 int itg_contract_exec_noalloc(itg_ctx* ctx, const itg_plan* plan, const double* A, const double* B, double* C,
                               int slices);
@@ -252,6 +253,25 @@ int itg_dmrg_run_sum(itg_ctx* ctx, const itg_model_desc* models, int32_t nmodels
  * (each freed with itg_dmrg_free). */
 int itg_dmrg_run_states(itg_ctx* ctx, const itg_model_desc* model, int32_t nstates, const itg_sweep_desc* const* sweeps,
                         const int32_t* nsweeps, double weight, int precision, itg_dmrg_result** out);
+/* dmrg() on the caller's own MPO and initial MPS, device tensors built with
+ * itg_tensor_create (or loaded with itg_mps_file_load): the overloads
+ *   dmrg(H, psi0, sweeps)                  itensor/mps/dmrg.h:67-76      nmpo 1, nprev 0
+ *   dmrg(std::vector<MPO>{H1,...}, psi0, ..) itensor/mps/dmrg.h:181-230  nmpo > 1 (LocalMPOSet)
+ *   dmrg(H, std::vector<MPS>{...}, psi0, .., {"Weight", w})  itensor/mps/dmrg.h:245-266  nprev > 0
+ * W holds nmpo x nsites tensors (MPO k's site j at W[k*nsites + j-1]); an MPO
+ * tensor carries the site index of psi0[j] unprimed and primed and shares one
+ * link with each neighbour (any index order). prev holds nprev x nsites
+ * tensors of earlier states on the same sites. The final MPS stays in the
+ * result (itg_dmrg_mps); after the last right-to-left half-sweep its
+ * orthogonality centre is site 1 (leftLim 0, rightLim 2). New links keep the
+ * tags of the links they replace (MPS::svdBond, itensor/mps/mps_impl.h:81-84).
+ * Also itg_dmrg_run, _sum and _states keep their final MPS. */
+int itg_dmrg_run_mpo(itg_ctx* ctx, int32_t nsites, int32_t nmpo, const itg_tensor* const* W,
+                     const itg_tensor* const* psi0, int32_t nprev, const itg_tensor* const* prev, double weight,
+                     const itg_sweep_desc* sweeps, int32_t nsweeps, int precision, itg_dmrg_result** out);
+/* Site tensor j (1..N) of the final MPS of a result (a new handle on the same
+ * device data; free it with itg_tensor_free). */
+int itg_dmrg_mps(const itg_dmrg_result* r, int32_t j, itg_tensor** out);
 int itg_dmrg_energy(const itg_dmrg_result* r, double* energy);
 int itg_dmrg_nbonds(const itg_dmrg_result* r, int32_t* nbonds);
 int itg_dmrg_bonds(const itg_dmrg_result* r, int32_t* sweep, int32_t* halfsweep, int32_t* bond, double* energy,
@@ -262,6 +282,30 @@ int itg_dmrg_timing(const itg_dmrg_result* r, int32_t* nsweeps, double* sweep_se
 /* Wall seconds spent in [environments + two-site tensor, Davidson, bond split], summed over all bond steps. */
 int itg_dmrg_phases(const itg_dmrg_result* r, double* seconds3);
 void itg_dmrg_free(itg_dmrg_result* r);
+
+/* ---------------------------------------------------------------- checkpoints
+ * MPS and MPO files in the reference's plain binary layout: what
+ * writeToFile(path, psi) and readFromFile(path, psi) read and write
+ * (itensor/util/readwrite.h:337-370; MPS::write/read itensor/mps/mps.cc:353-378,
+ * ITensor::write/read itensor/itensor.cc:769-803, QDense write/read
+ * itensor/itdata/qdense.h:236-248). An MPO file has the same layout. Site
+ * tensors must hold QN block-sparse real storage (QDense<Real>).
+ * A file object is a host copy: read -> write gives the same bytes.
+ * itg_mps_file_load uploads site tensors 1..N (sites receives N handles);
+ * QN slot k of the loaded indices holds the quantum number whose name
+ * itg_mps_file_info returns k-th (qn_names: 4 x 8 chars, zero padded; names
+ * in the reference's order). itg_mps_file_store downloads site tensors and
+ * writes QN slot k under the k-th name of the comma-separated qn_names
+ * ("Sz", "Nf,Sz", ...); index tags are carried as the tensors hold them. */
+typedef struct itg_mps_file itg_mps_file;
+int itg_mps_file_read(const char* path, itg_mps_file** out);
+int itg_mps_file_write(const itg_mps_file* f, const char* path);
+int itg_mps_file_info(const itg_mps_file* f, int32_t* nsites, int32_t* leftlim, int32_t* rightlim, int32_t* nqn,
+                      char* qn_names);
+int itg_mps_file_load(itg_ctx* ctx, const itg_mps_file* f, itg_tensor** sites);
+int itg_mps_file_store(itg_ctx* ctx, int32_t nsites, const itg_tensor* const* sites, int32_t leftlim, int32_t rightlim,
+                       const char* qn_names, itg_mps_file** out);
+void itg_mps_file_free(itg_mps_file* f);
 
 /* ---------------------------------------------------------------- solver pool
  * Many independent ground-state solves (dmrg() as above, one per request) on
@@ -283,6 +327,14 @@ typedef struct itg_pool itg_pool;
 int itg_pool_create(int device, int32_t workers, int32_t slots_per_worker, double budget_bytes, itg_pool** out);
 int itg_pool_submit(itg_pool* p, const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps,
                     int precision, double arrival_s, int64_t* id);
+/* A request on the caller's MPO and initial MPS (as itg_dmrg_run_mpo with one
+ * MPO): the tensors are copied to host memory during the call (ctx is the
+ * context they were made on), so they may be freed afterwards. keep_mps != 0:
+ * the result keeps the final MPS (read with itg_pool_result + itg_dmrg_mps;
+ * device memory held until the result and the pool are freed). */
+int itg_pool_submit_mpo(itg_pool* p, itg_ctx* ctx, int32_t nsites, const itg_tensor* const* W,
+                        const itg_tensor* const* psi0, const itg_sweep_desc* sweeps, int32_t nsweeps, int precision,
+                        double arrival_s, int keep_mps, int64_t* id);
 int itg_pool_start(itg_pool* p);
 int itg_pool_drain(itg_pool* p);   /* waits until every submitted request has finished */
 /* status: -1 queued, -2 running, 0 done, else the request's error code (message in itg_pool_error).
@@ -296,6 +348,10 @@ int itg_pool_stats(itg_pool* p, int64_t* submitted, int64_t* done, int64_t* fail
                    int32_t* peak_running, double* elapsed_s);
 int itg_pool_estimate(const itg_model_desc* model, const itg_sweep_desc* sweeps, int32_t nsweeps, int precision,
                       double* bytes);
+/* The same estimate for an MPO request: nsites sites of local dimension
+ * site_dim, MPO bond dimension mpo_bond_dim. */
+int itg_pool_estimate_mpo(int32_t nsites, int32_t site_dim, int32_t mpo_bond_dim, const itg_sweep_desc* sweeps,
+                          int32_t nsweeps, int precision, double* bytes);
 void itg_pool_destroy(itg_pool* p);
 
 #ifdef __cplusplus

@@ -106,6 +106,17 @@ SIGNATURES = {
                                       _i32p, C.c_double, C.c_int, C.POINTER(C.c_void_p)]),
     "itg_dmrg_run": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.POINTER(SweepDesc), C.c_int32, C.c_int,
                                C.POINTER(C.c_void_p)]),
+    "itg_dmrg_run_mpo": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                   C.c_int32, C.POINTER(C.c_void_p), C.c_double, C.POINTER(SweepDesc), C.c_int32,
+                                   C.c_int, C.POINTER(C.c_void_p)]),
+    "itg_dmrg_mps": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "itg_mps_file_read": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    "itg_mps_file_write": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "itg_mps_file_info": (C.c_int, [C.c_void_p, _i32p, _i32p, _i32p, _i32p, C.c_char_p]),
+    "itg_mps_file_load": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "itg_mps_file_store": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_char_p,
+                                     C.POINTER(C.c_void_p)]),
+    "itg_mps_file_free": (None, [C.c_void_p]),
     "itg_dmrg_energy": (C.c_int, [C.c_void_p, _f64p]),
     "itg_dmrg_nbonds": (C.c_int, [C.c_void_p, _i32p]),
     "itg_dmrg_bonds": (C.c_int, [C.c_void_p, _i32p, _i32p, _i32p, _f64p, _f64p, _i32p]),
@@ -116,6 +127,11 @@ SIGNATURES = {
     "itg_pool_create": (C.c_int, [C.c_int, C.c_int32, C.c_int32, C.c_double, C.POINTER(C.c_void_p)]),
     "itg_pool_submit": (C.c_int, [C.c_void_p, C.POINTER(ModelDesc), C.POINTER(SweepDesc), C.c_int32, C.c_int,
                                   C.c_double, C.POINTER(C.c_int64)]),
+    "itg_pool_submit_mpo": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_void_p),
+                                      C.POINTER(C.c_void_p), C.POINTER(SweepDesc), C.c_int32, C.c_int, C.c_double,
+                                      C.c_int, C.POINTER(C.c_int64)]),
+    "itg_pool_estimate_mpo": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(SweepDesc), C.c_int32, C.c_int,
+                                        _f64p]),
     "itg_pool_start": (C.c_int, [C.c_void_p]),
     "itg_pool_drain": (C.c_int, [C.c_void_p]),
     "itg_pool_record": (C.c_int, [C.c_void_p, C.c_int64, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _i32p]),
@@ -512,6 +528,75 @@ class Context:
                                            outs), self.h)
         return [_take_dmrg_result(C.c_void_p(o)) for o in outs]
 
+    def dmrg_mpo(self, W, psi0, sweeps, precision=-1, more=None, prev=None, weight=1.0):
+        """dmrg() on the caller's MPO tensors W (list of Tensor, one per site) and
+        initial MPS psi0; `more`: further MPOs of a sum (lists like W); `prev`:
+        earlier states (lists of Tensor) for excited states with `weight`.
+        The result carries the final MPS in .mps."""
+        n = len(psi0)
+        mpos = [W] + list(more or [])
+        prevs = list(prev or [])
+        wh = (C.c_void_p * (n * len(mpos)))(*[t.h for M in mpos for t in M])
+        ph = (C.c_void_p * n)(*[t.h for t in psi0])
+        qh = (C.c_void_p * max(1, n * len(prevs)))(*[t.h for P in prevs for t in P])
+        sw = _sweep_descs(sweeps)
+        out = C.c_void_p()
+        self._ok(lib().itg_dmrg_run_mpo(self.h, n, len(mpos), wh, ph, len(prevs), qh, float(weight), sw, len(sweeps),
+                                        precision, C.byref(out)), self.h)
+        return _take_dmrg_result(out, ctx=self, nsites=n)
+
+    def mps_load(self, path):
+        """Reads an MPS or MPO file in the reference's binary layout onto the device:
+        (site tensors, dict(leftlim, rightlim, qn_names))."""
+        f = MpsFile(path)
+        return f.load(self), f.info()
+
+    def mps_store(self, tensors, leftlim, rightlim, qn_names):
+        """An MpsFile (host copy, reference binary layout) of device site tensors."""
+        th = (C.c_void_p * len(tensors))(*[t.h for t in tensors])
+        out = C.c_void_p()
+        self._ok(lib().itg_mps_file_store(self.h, len(tensors), th, leftlim, rightlim, ",".join(qn_names).encode(),
+                                          C.byref(out)), self.h)
+        return MpsFile(handle=out)
+
+
+class MpsFile:
+    """An MPS/MPO file of the reference's binary layout, held in host memory
+    (itg_mps_file_*): read, write, and load onto a context's device."""
+
+    def __init__(self, path=None, handle=None):
+        if handle is None:
+            handle = C.c_void_p()
+            _check(lib().itg_mps_file_read(str(path).encode(), C.byref(handle)))
+        self.h = handle
+
+    def info(self):
+        n, l, r, q = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        buf = C.create_string_buffer(32)
+        _check(lib().itg_mps_file_info(self.h, C.byref(n), C.byref(l), C.byref(r), C.byref(q), buf))
+        names = [buf.raw[8 * k:8 * k + 8].rstrip(b"\0").decode() for k in range(q.value)]
+        return dict(nsites=n.value, leftlim=l.value, rightlim=r.value, qn_names=names)
+
+    def write(self, path):
+        _check(lib().itg_mps_file_write(self.h, str(path).encode()))
+
+    def load(self, ctx):
+        n = self.info()["nsites"]
+        out = (C.c_void_p * n)()
+        ctx._ok(lib().itg_mps_file_load(ctx.h, self.h, out), ctx.h)
+        return [Tensor(ctx, C.c_void_p(o)) for o in out]
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().itg_mps_file_free(self.h)
+            self.h = C.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 def _model_desc(model):
     return ModelDesc(int(model.get("type", 0)), int(model.get("N", 0)), float(model.get("J", 1.0)),
@@ -527,8 +612,9 @@ def _sweep_descs(sweeps):
                                        for s in sweeps])
 
 
-def _take_dmrg_result(out):
-    """Reads an itg_dmrg_result handle into a DmrgResult and frees it."""
+def _take_dmrg_result(out, ctx=None, nsites=0):
+    """Reads an itg_dmrg_result handle into a DmrgResult and frees it; with a
+    context, the final MPS's site tensors come along in .mps."""
     try:
         L = lib()
         e = C.c_double()
@@ -560,6 +646,14 @@ def _take_dmrg_result(out):
         L.itg_dmrg_phases(out, _p(ph, C.c_double))
         r = DmrgResult(e.value, bonds, links, secs[:nsw.value].tolist(), ap.value)
         r.phase_seconds = dict(environments=float(ph[0]), davidson=float(ph[1]), bond_split=float(ph[2]))
+        r.mps = None
+        if ctx is not None:
+            n = nsites or N
+            r.mps = []
+            for j in range(1, n + 1):
+                t = C.c_void_p()
+                _check(L.itg_dmrg_mps(out, j, C.byref(t)))
+                r.mps.append(Tensor(ctx, t))
         return r
     finally:
         lib().itg_dmrg_free(out)
@@ -595,6 +689,18 @@ class Pool:
         _check(lib().itg_pool_submit(self.h, C.byref(md), sw, len(sweeps), precision, float(arrival), C.byref(i)))
         return i.value
 
+    def submit_mpo(self, ctx, W, psi0, sweeps, precision=0, arrival=0.0, keep_mps=False):
+        """A request on the caller's MPO and initial MPS (device tensors of ctx;
+        copied during the call)."""
+        n = len(psi0)
+        wh = (C.c_void_p * n)(*[t.h for t in W])
+        ph = (C.c_void_p * n)(*[t.h for t in psi0])
+        sw = _sweep_descs(sweeps)
+        i = C.c_int64()
+        _check(lib().itg_pool_submit_mpo(self.h, ctx.h, n, wh, ph, sw, len(sweeps), precision, float(arrival),
+                                         int(keep_mps), C.byref(i)))
+        return i.value
+
     def start(self):
         _check(lib().itg_pool_start(self.h))
 
@@ -613,10 +719,12 @@ class Pool:
             err = buf.value.decode()
         return PoolRecord(i, st.value, e.value, ta.value, tad.value, td.value, eb.value, pb.value, wk.value, err)
 
-    def result(self, i):
+    def result(self, i, ctx=None):
+        """Full result of request i; with ctx (any context on this device) and a
+        request submitted with keep_mps, the final MPS comes along in .mps."""
         out = C.c_void_p()
         _check(lib().itg_pool_result(self.h, i, C.byref(out)))
-        return _take_dmrg_result(out)
+        return _take_dmrg_result(out, ctx=ctx)
 
     def stats(self):
         s, d, f = C.c_int64(), C.c_int64(), C.c_int64()
@@ -645,6 +753,14 @@ def pool_estimate(model, sweeps, precision=0):
     md = _model_desc(model)
     sw = _sweep_descs(sweeps)
     _check(lib().itg_pool_estimate(C.byref(md), sw, len(sweeps), precision, C.byref(b)))
+    return b.value
+
+
+def pool_estimate_mpo(nsites, site_dim, mpo_bond_dim, sweeps, precision=0):
+    """Device-memory estimate (bytes) of an MPO request."""
+    b = C.c_double()
+    sw = _sweep_descs(sweeps)
+    _check(lib().itg_pool_estimate_mpo(nsites, site_dim, mpo_bond_dim, sw, len(sweeps), precision, C.byref(b)))
     return b.value
 
 

@@ -19,8 +19,9 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["contract.cu", "ozaki.cu", "ops.cu", "eigh.cu", "eigh_tri.cu", "svd.cu", "peaks.cu", "noalloc.cu"]
-CPP_SOURCES = ["tridiag_ql.cpp", "tensor.cpp", "algo_core.cpp", "heff_program.cpp", "svd_split.cpp", "models.cpp", "dmrg.cpp", "fiber.cpp", "pool.cpp", "capi.cpp"]
-HEADERS = ["common.h", "tensor.h", "engine.h", "ops.h", "algo.h", "fiber.h", "pool.h", "eigh_tri.h", "tridiag_ql.h"]
+CPP_SOURCES = ["tridiag_ql.cpp", "tensor.cpp", "algo_core.cpp", "heff_program.cpp", "svd_split.cpp", "models.cpp", "dmrg.cpp", "fiber.cpp", "pool.cpp", "mps_io.cpp", "capi.cpp"]
+HEADERS = ["common.h", "tensor.h", "engine.h", "ops.h", "algo.h", "fiber.h", "pool.h", "eigh_tri.h", "tridiag_ql.h",
+           "mps_io.h"]
 
 
 def _newest(paths):

@@ -165,6 +165,13 @@ struct MPO {
 };
 // sites: the site indices to use (another MPO's, for sums of MPOs); new ones if null.
 MPO build_mpo(Ctx& ctx, Hamiltonian const& H, std::vector<Index> const* sites = nullptr);
+// A caller's MPO tensors with an initial MPS on the same sites (site j: the
+// index psi0[j] shares with W[j] at prime level 0, which W[j] also holds
+// primed; neighbouring tensors share one link each), as dmrg(H, psi0, sweeps)
+// receives them (itensor/mps/dmrg.h:67-76). `sites`: the site indices another
+// MPO of a sum already uses (they must agree).
+MPO mpo_from_tensors(std::vector<Tensor> const& W, std::vector<Tensor> const& psi0,
+                     std::vector<Index> const* sites = nullptr);
 // Product state with the link QNs of MPS(InitState) (itensor/mps/mps.cc:558-585).
 std::vector<Tensor> product_mps(Ctx& ctx, MPO const& H, SiteType const& st, std::vector<int> const& states);
 std::vector<int> default_state(ModelSpec const& m);

@@ -2,6 +2,7 @@
 // descriptions and the host data model, and turns exceptions into status codes.
 #include "../../include/itg.h"
 #include "pool.h"
+#include "mps_io.h"
 #include <cstring>
 
 using namespace itg;
@@ -65,6 +66,16 @@ ModelSpec model_from(itg_model_desc const& d) {
     m.J = d.J; m.Jz = d.Jz; m.J2 = d.J2; m.h = d.h; m.t = d.t; m.U = d.U;
     m.Lx = d.Lx; m.Ly = d.Ly; m.yperiodic = d.yperiodic;
     return m;
+}
+
+std::vector<Tensor> tensors_from(itg_tensor const* const* t, int n, char const* what) {
+    ITG_REQUIRE(t, std::string("dmrg: null ") + what + " array");
+    std::vector<Tensor> v;
+    for (int j = 0; j < n; ++j) {
+        ITG_REQUIRE(t[j], std::string("dmrg: null ") + what + " tensor");
+        v.push_back(t[j]->t);
+    }
+    return v;
 }
 
 std::vector<SweepSpec> sweeps_from(itg_sweep_desc const* sweeps, int n) {
@@ -193,7 +204,13 @@ int itg_tensor_create(itg_ctx* c, int32_t rank, const itg_index_desc* inds, int3
                     ITG_REQUIRE(L->coords[(size_t)b * rank + k] >= 0 && L->coords[(size_t)b * rank + k] < is[k].nblock(),
                                 "tensor_create: block coordinate out of range");
             for (int b = 1; b < nblocks; ++b)
-                ITG_REQUIRE(coords_less(L->block(b - 1), L->block(b), rank), "tensor_create: blocks not in storage order");
+                ITG_REQUIRE(coords_less(L->block(b - 1), L->block(b), rank),
+                            "tensor_create: blocks not in storage order (or a block listed twice)");
+            // one divergence per tensor: every stored block has the same flux (QDense,
+            // itensor/itdata/qdense.cc:134-171)
+            for (int b = 1; b < nblocks; ++b)
+                ITG_REQUIRE(L->flux(L->block(b)) == L->flux(L->block(0)),
+                            "tensor_create: blocks of different flux (no single divergence)");
         }
         L->finish();
         Tensor t(L, c->ctx.stream);
@@ -340,7 +357,7 @@ void itg_plan_free(itg_plan* p) { delete p; }
 
 int itg_contract_exec_noalloc(itg_ctx* c, const itg_plan* p, const double* A, const double* B, double* C, int slices) {
     return guard(c, [&] {
-        ITG_REQUIRE(p && A && B && C, "contract_exec_noalloc: null argument");
+        ITG_REQUIRE(c && p && A && B && C, "contract_exec_noalloc: null argument");
         exec_plan_noalloc(c->ctx, *p->p, A, B, C, slices);
     });
 }
@@ -504,7 +521,6 @@ int itg_dmrg_run(itg_ctx* c, const itg_model_desc* model, const itg_sweep_desc* 
         auto* res = new itg_dmrg_result;
         try {
             res->r = dmrg(c->ctx, mpo, psi, sw, precision);
-            res->r.psi.clear();
         } catch (...) {
             delete res;
             throw;
@@ -534,7 +550,6 @@ int itg_dmrg_run_sum(itg_ctx* c, const itg_model_desc* models, int32_t nmodels, 
         auto* res = new itg_dmrg_result;
         try {
             res->r = dmrg(c->ctx, mpo, psi, sw, precision, nullptr, 1.0, more.empty() ? nullptr : &more);
-            res->r.psi.clear();
         } catch (...) {
             delete res;
             throw;
@@ -562,7 +577,6 @@ int itg_dmrg_run_states(itg_ctx* c, const itg_model_desc* model, int32_t nstates
                 made.push_back(res);
                 res->r = dmrg(c->ctx, mpo, psi, sw, precision, k ? &prev : nullptr, weight);
                 prev.push_back(res->r.psi);
-                res->r.psi.clear();
             }
         } catch (...) {
             for (auto* r : made) delete r;
@@ -571,6 +585,110 @@ int itg_dmrg_run_states(itg_ctx* c, const itg_model_desc* model, int32_t nstates
         for (int k = 0; k < nstates; ++k) out[k] = made[k];
     });
 }
+
+int itg_dmrg_run_mpo(itg_ctx* c, int32_t nsites, int32_t nmpo, const itg_tensor* const* W, const itg_tensor* const* psi0,
+                     int32_t nprev, const itg_tensor* const* prev, double weight, const itg_sweep_desc* sweeps,
+                     int32_t nsweeps, int precision, itg_dmrg_result** out) {
+    return guard(c, [&] {
+        ITG_REQUIRE(c && out && nsites >= 2 && nmpo >= 1 && nprev >= 0, "dmrg_run_mpo: bad arguments");
+        ITG_REQUIRE(nprev == 0 || weight > 0, "dmrg_run_mpo: the weight must be positive");
+        std::vector<Tensor> start = tensors_from(psi0, nsites, "MPS");
+        MPO H = mpo_from_tensors(tensors_from(W, nsites, "MPO"), start);
+        std::vector<MPO> more;
+        for (int k = 1; k < nmpo; ++k)
+            more.push_back(mpo_from_tensors(tensors_from(W + (size_t)k * nsites, nsites, "MPO"), start, &H.sites));
+        std::vector<std::vector<Tensor>> prevs;
+        for (int k = 0; k < nprev; ++k) {
+            ITG_REQUIRE(prev, "dmrg_run_mpo: null array of earlier states");
+            prevs.push_back(tensors_from(prev + (size_t)k * nsites, nsites, "earlier-state"));
+        }
+        std::vector<SweepSpec> sw = sweeps_from(sweeps, nsweeps);
+        auto* res = new itg_dmrg_result;
+        try {
+            res->r = dmrg(c->ctx, H, start, sw, precision, prevs.empty() ? nullptr : &prevs, weight,
+                          more.empty() ? nullptr : &more);
+        } catch (...) {
+            delete res;
+            throw;
+        }
+        *out = res;
+    });
+}
+
+int itg_dmrg_mps(const itg_dmrg_result* r, int32_t j, itg_tensor** out) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(r && out, "dmrg_mps: null argument");
+        ITG_REQUIRE(!r->r.psi.empty(), "dmrg_mps: this result holds no MPS");
+        ITG_REQUIRE(j >= 1 && j <= (int)r->r.psi.size(), "dmrg_mps: site out of range");
+        *out = new itg_tensor{r->r.psi[j - 1]};
+    });
+}
+
+struct itg_mps_file {
+    MpsFile f;
+};
+
+int itg_mps_file_read(const char* path, itg_mps_file** out) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(path && out, "mps_file_read: null argument");
+        auto* f = new itg_mps_file{read_mps_file(path)};
+        *out = f;
+    });
+}
+
+int itg_mps_file_write(const itg_mps_file* f, const char* path) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(f && path, "mps_file_write: null argument");
+        write_mps_file(f->f, path);
+    });
+}
+
+int itg_mps_file_info(const itg_mps_file* f, int32_t* nsites, int32_t* leftlim, int32_t* rightlim, int32_t* nqn,
+                      char* qn_names) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(f, "mps_file_info: null file");
+        if (nsites) *nsites = f->f.N;
+        if (leftlim) *leftlim = f->f.leftlim;
+        if (rightlim) *rightlim = f->f.rightlim;
+        if (nqn) *nqn = (int32_t)f->f.qn_names.size();
+        if (qn_names) {
+            std::memset(qn_names, 0, 4 * 8);
+            for (size_t k = 0; k < f->f.qn_names.size(); ++k) std::memcpy(qn_names + 8 * k, f->f.qn_names[k].data(), 7);
+        }
+    });
+}
+
+int itg_mps_file_load(itg_ctx* c, const itg_mps_file* f, itg_tensor** sites) {
+    return guard(c, [&] {
+        ITG_REQUIRE(c && f && sites, "mps_file_load: null argument");
+        std::vector<Tensor> ts = load_mps(c->ctx, f->f);
+        for (size_t j = 0; j < ts.size(); ++j) sites[j] = new itg_tensor{ts[j]};
+    });
+}
+
+int itg_mps_file_store(itg_ctx* c, int32_t nsites, const itg_tensor* const* sites, int32_t leftlim, int32_t rightlim,
+                       const char* qn_names, itg_mps_file** out) {
+    return guard(c, [&] {
+        ITG_REQUIRE(c && out && nsites >= 1, "mps_file_store: bad arguments");
+        std::vector<std::array<char, 7>> names;
+        std::string s = qn_names ? qn_names : "";
+        size_t p = 0;
+        while (p < s.size()) {
+            size_t q = s.find(',', p);
+            if (q == std::string::npos) q = s.size();
+            std::string n = s.substr(p, q - p);
+            ITG_REQUIRE(!n.empty() && n.size() <= 7, "mps_file_store: QN names hold 1 to 7 characters");
+            std::array<char, 7> a{};
+            std::memcpy(a.data(), n.data(), n.size());
+            names.push_back(a);
+            p = q + 1;
+        }
+        auto* f = new itg_mps_file{store_mps(c->ctx, tensors_from(sites, nsites, "MPS"), leftlim, rightlim, names)};
+        *out = f;
+    });
+}
+
+void itg_mps_file_free(itg_mps_file* f) { delete f; }
 
 int itg_dmrg_energy(const itg_dmrg_result* r, double* e) {
     return guard(nullptr, [&] { ITG_REQUIRE(r && e, "null"); *e = r->r.energy; });
@@ -645,6 +763,27 @@ int itg_pool_submit(itg_pool* p, const itg_model_desc* model, const itg_sweep_de
     });
 }
 
+int itg_pool_submit_mpo(itg_pool* p, itg_ctx* c, int32_t nsites, const itg_tensor* const* W,
+                        const itg_tensor* const* psi0, const itg_sweep_desc* sweeps, int32_t nsweeps, int precision,
+                        double arrival_s, int keep_mps, int64_t* id) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p && c && id && nsites >= 2, "pool_submit_mpo: bad arguments");
+        ITG_REQUIRE(precision == PREC_F64 || precision == PREC_OZAKI_BF16, "pool_submit_mpo: unsupported precision");
+        std::vector<Tensor> w = tensors_from(W, nsites, "MPO"), s = tensors_from(psi0, nsites, "MPS");
+        mpo_from_tensors(w, s);  // checks the structure now, so a bad request fails here
+        auto in = std::make_shared<MpoInput>();
+        for (auto const& t : w) in->W.push_back(HostTensor{t.lay, download(c->ctx, t)});
+        for (auto const& t : s) in->psi0.push_back(HostTensor{t.lay, download(c->ctx, t)});
+        SolveRequest r;
+        r.mpo = in;
+        r.keep_mps = keep_mps != 0;
+        r.sweeps = sweeps_from(sweeps, nsweeps);
+        r.prec = precision;
+        r.arrival = arrival_s;
+        *id = p->pool.submit(std::move(r));
+    });
+}
+
 int itg_pool_start(itg_pool* p) {
     return guard(nullptr, [&] { ITG_REQUIRE(p, "null pool"); p->pool.start(); });
 }
@@ -707,6 +846,15 @@ int itg_pool_estimate(const itg_model_desc* model, const itg_sweep_desc* sweeps,
     return guard(nullptr, [&] {
         ITG_REQUIRE(model && bytes, "pool_estimate: bad arguments");
         *bytes = (double)solve_footprint_estimate(model_from(*model), sweeps_from(sweeps, nsweeps), precision);
+    });
+}
+
+int itg_pool_estimate_mpo(int32_t nsites, int32_t site_dim, int32_t mpo_bond_dim, const itg_sweep_desc* sweeps,
+                          int32_t nsweeps, int precision, double* bytes) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(bytes && nsites >= 2 && site_dim >= 1 && mpo_bond_dim >= 1, "pool_estimate_mpo: bad arguments");
+        *bytes = (double)solve_footprint_estimate(nsites, site_dim, mpo_bond_dim, sweeps_from(sweeps, nsweeps),
+                                                  precision);
     });
 }
 

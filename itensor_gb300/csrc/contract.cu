@@ -685,6 +685,11 @@ Match match_indices(std::vector<Index> const& A, std::vector<Index> const& B) {
     for (size_t i = 0; i < A.size(); ++i)
         for (size_t j = 0; j < B.size(); ++j)
             if (!bused[j] && A[i].same(B[j])) {
+                // one index seen twice must have one sector structure (the reference's
+                // Index carries its sectors, so equal indices cannot disagree)
+                if (A[i].sec != B[j].sec)
+                    ITG_REQUIRE(A[i].sec->dim == B[j].sec->dim,
+                                "contract: a contracted index has different sector sizes on the two operands");
                 m.a_con.push_back((int)i);
                 m.b_con.push_back((int)j);
                 bused[j] = 1;

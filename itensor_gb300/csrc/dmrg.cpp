@@ -94,7 +94,48 @@ struct MpsEnvironments {
         return contract(ctx, o, r, prec, phi_layout);
     }
 };
+
+// T with the tags of index `link` replaced (same data, same block structure)
+Tensor with_link_tags(Tensor const& T, Index const& link, std::array<char, TAG_BYTES> const& tags) {
+    std::vector<Index> inds = T.inds();
+    for (auto& I : inds)
+        if (I.id == link.id) I.tags = tags;
+    return relabel(T, inds);
+}
 }  // namespace
+
+MPO mpo_from_tensors(std::vector<Tensor> const& W, std::vector<Tensor> const& psi0, std::vector<Index> const* sites) {
+    const int N = (int)W.size();
+    ITG_REQUIRE(N >= 2 && (int)psi0.size() == N, "dmrg: the MPO and the MPS need the same length, at least 2");
+    MPO H;
+    H.W = W;
+    for (int j = 0; j < N; ++j) {
+        ITG_REQUIRE(W[j].valid() && psi0[j].valid(), "dmrg: null MPO or MPS tensor");
+        Index site;
+        bool found = false;
+        for (auto const& I : psi0[j].inds()) {
+            if (I.plev != 0) continue;
+            bool in_w = false, primed = false;
+            for (auto const& J : W[j].inds()) {
+                if (J.id == I.id && J.plev == 0) in_w = true;
+                if (J.id == I.id && J.plev == 1) primed = true;
+            }
+            if (in_w && primed) { site = I; found = true; break; }
+        }
+        ITG_REQUIRE(found, "dmrg: MPO tensor " + std::to_string(j + 1) +
+                               " does not act on a site index of MPS tensor " + std::to_string(j + 1));
+        if (sites) ITG_REQUIRE(site.same((*sites)[j]), "dmrg: the MPOs of a sum act on different site indices");
+        H.sites.push_back(site);
+        if (j + 1 < N) {
+            Match mt = match_indices(W[j].inds(), W[j + 1].inds());
+            ITG_REQUIRE(mt.a_con.size() == 1, "dmrg: neighbouring MPO tensors must share exactly one link");
+            H.bond_dim = std::max<int>(H.bond_dim, (int)W[j].inds()[mt.a_con[0]].dim());
+            Match pm = match_indices(psi0[j].inds(), psi0[j + 1].inds());
+            ITG_REQUIRE(pm.a_con.size() == 1, "dmrg: neighbouring MPS tensors must share exactly one link");
+        }
+    }
+    return H;
+}
 
 DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<SweepSpec> const& sweeps, int prec,
                 std::vector<std::vector<Tensor>> const* prev, double weight, std::vector<MPO> const* more) {
@@ -157,6 +198,15 @@ DmrgResult dmrg(Ctx& ctx, MPO const& H, std::vector<Tensor> psi, std::vector<Swe
             const bool svd_route = s.use_svd || (s.noise == 0 && s.cutoff < 1e-12);
             SplitResult sr = svd_route ? svd_split(ctx, phi, A, B, ha == 1, sa, prec)
                                        : denmat_decomp(ctx, phi, A, B, ha == 1, sa, prec, &op, s.noise);
+            // the new link keeps the old link's tags (MPS::svdBond, itensor/mps/mps_impl.h:81-84)
+            if (!mt.a_con.empty()) {
+                auto const& tags = A.inds()[mt.a_con[0]].tags;
+                if (tags != std::array<char, TAG_BYTES>{}) {
+                    sr.A = with_link_tags(sr.A, sr.link, tags);
+                    sr.B = with_link_tags(sr.B, sr.link, tags);
+                    sr.link.tags = tags;
+                }
+            }
             psi[b - 1] = sr.A;
             psi[b] = sr.B;
             auto tp3 = clk::now();

@@ -9,9 +9,12 @@
 // (ITG_NOALLOC_SCRATCH_BYTES) instead of pool memory. The array exists once
 // per device that loads the library, until the process exits.
 //
-// Set-up: the first call on a device, with that device current, looks up the
-// array's device address with cudaGetSymbolAddress (the host-side name is only
-// a stand-in, never a device address) and keeps it. That first call should
+// Set-up: the first call from a CUDA context (the device's primary context,
+// or a context the caller created and made current), with that device
+// current, looks up the array's device address with cudaGetSymbolAddress (the
+// host-side name is only a stand-in, never a device address) and keeps it for
+// that context. A later call from another context, or from a new primary
+// context after cudaDeviceReset, looks it up again. That first call should
 // come before any stream capture.
 //
 // Every call shares the array and the array keeps the last call's contents.
@@ -21,6 +24,7 @@
 #include "../../include/itg.h"
 #include "engine.h"
 #include <mutex>
+#include <vector>
 
 namespace itg {
 
@@ -28,22 +32,44 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[ITG_NOALLOC_SCR
 
 namespace {
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[64] = {};
+// The array's address is a property of the CUDA context it was looked up in:
+// one entry per (device, context) seen so far.
+struct NoallocEntry { int device; void* context; void* ptr; };
+std::vector<NoallocEntry> g_noalloc_seen;
+
+typedef int (*CtxGetCurrentFn)(void**);
+CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<CtxGetCurrentFn>(f);
+    }();
+    return fn;
+}
 
 void* noalloc_scratch(int device) {
-    ITG_REQUIRE(device >= 0 && device < 64, "noalloc: device ordinal out of range");
+    int cur = -1;
+    ITG_CHECK_CUDA(cudaGetDevice(&cur));
+    if (cur != device) ITG_CHECK_CUDA(cudaSetDevice(device));
+    struct Restore {
+        int cur, dev;
+        ~Restore() { if (cur != dev) cudaSetDevice(cur); }
+    } restore{cur, device};
+    CtxGetCurrentFn get = ctx_get_current();
+    if (!get) throw Error(ERR_CUDA, "noalloc: cuCtxGetCurrent is not available from the driver");
+    void* context = nullptr;
+    if (get(&context) != 0 || !context) throw Error(ERR_CUDA, "noalloc: no current CUDA context");
     std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
-        int cur = -1;
-        ITG_CHECK_CUDA(cudaGetDevice(&cur));
-        if (cur != device) ITG_CHECK_CUDA(cudaSetDevice(device));
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (cur != device) cudaSetDevice(cur);
-        if (e != cudaSuccess) throw Error(ERR_CUDA, std::string("noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_noalloc_ptr[device] = p;
-    }
-    return g_noalloc_ptr[device];
+    for (auto const& e : g_noalloc_seen)
+        if (e.device == device && e.context == context) return e.ptr;
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) throw Error(ERR_CUDA, std::string("noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_seen.push_back(NoallocEntry{device, context, p});
+    return p;
 }
 }  // namespace
 

@@ -7,7 +7,26 @@ namespace itg {
 
 int64_t solve_footprint_estimate(ModelSpec const& m, std::vector<SweepSpec> const& sweeps, int prec) {
     Hamiltonian H = make_hamiltonian(m);
-    const int N = H.N, d = H.st.d(), D = mpo_bond_dim(H);
+    return solve_footprint_estimate(H.N, H.st.d(), mpo_bond_dim(H), sweeps, prec);
+}
+
+int64_t solve_footprint_estimate(SolveRequest const& r) {
+    if (!r.mpo) return solve_footprint_estimate(r.model, r.sweeps, r.prec);
+    const int N = (int)r.mpo->W.size();
+    int d = 1, D = 1;
+    for (int j = 0; j < N; ++j) {
+        auto const& W = *r.mpo->W[j].lay;
+        for (auto const& I : W.inds) {
+            bool site = false;
+            for (auto const& J : r.mpo->psi0[j].lay->inds) site = site || J.id == I.id;
+            if (site) d = std::max<int>(d, (int)I.dim());
+            else D = std::max<int>(D, (int)I.dim());
+        }
+    }
+    return solve_footprint_estimate(N, d, D, r.sweeps, r.prec);
+}
+
+int64_t solve_footprint_estimate(int N, int d, int D, std::vector<SweepSpec> const& sweeps, int prec) {
     long maxdim = 1;
     int niter = 2;
     for (auto const& s : sweeps) {
@@ -60,7 +79,7 @@ double SolverPool::now() const {
 
 int64_t SolverPool::submit(SolveRequest req) {
     auto rec = std::make_shared<SolveRecord>();
-    rec->est_bytes = solve_footprint_estimate(req.model, req.sweeps, req.prec);
+    rec->est_bytes = solve_footprint_estimate(req);
     ITG_REQUIRE(!req.sweeps.empty(), "pool: empty sweep schedule");
     {
         std::lock_guard<std::mutex> g(mu_);
@@ -158,12 +177,22 @@ void SolverPool::finish(std::shared_ptr<SolveRecord> const& rec) {
 namespace {
 void run_solve(Ctx& ctx, SolveRecord& rec, SolverPool const& pool) {
     try {
-        Hamiltonian H = make_hamiltonian(rec.req.model);
-        ITG_REQUIRE(H.N >= 2, "pool: need at least two sites");
-        MPO mpo = build_mpo(ctx, H);
-        auto psi = product_mps(ctx, mpo, H.st, default_state(rec.req.model));
-        rec.result = dmrg(ctx, mpo, std::move(psi), rec.req.sweeps, rec.req.prec);
-        rec.result.psi.clear();   // the record keeps energies and links, not the state
+        if (rec.req.mpo) {
+            // the caller's MPO and initial MPS, uploaded on this solve's stream
+            std::vector<Tensor> W, psi;
+            for (auto const& h : rec.req.mpo->W) W.push_back(upload_tensor(ctx, h.lay, h.data.data()));
+            for (auto const& h : rec.req.mpo->psi0) psi.push_back(upload_tensor(ctx, h.lay, h.data.data()));
+            MPO mpo = mpo_from_tensors(W, psi);
+            rec.result = dmrg(ctx, mpo, std::move(psi), rec.req.sweeps, rec.req.prec);
+        } else {
+            Hamiltonian H = make_hamiltonian(rec.req.model);
+            ITG_REQUIRE(H.N >= 2, "pool: need at least two sites");
+            MPO mpo = build_mpo(ctx, H);
+            auto psi = product_mps(ctx, mpo, H.st, default_state(rec.req.model));
+            rec.result = dmrg(ctx, mpo, std::move(psi), rec.req.sweeps, rec.req.prec);
+        }
+        // the record keeps energies and links; the state only when asked for
+        if (!rec.req.keep_mps) rec.result.psi.clear();
         rec.status = 0;
     } catch (Error const& e) {
         rec.status = e.code;

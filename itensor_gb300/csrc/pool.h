@@ -21,8 +21,21 @@
 
 namespace itg {
 
+// A caller's MPO and initial MPS, copied to host memory when submitted (the
+// solve uploads them on its own stream, so the caller's tensors may be freed
+// or changed after submission).
+struct HostTensor {
+    std::shared_ptr<Layout> lay;
+    std::vector<double> data;
+};
+struct MpoInput {
+    std::vector<HostTensor> W, psi0;
+};
+
 struct SolveRequest {
-    ModelSpec model;
+    ModelSpec model;                      // used when mpo is empty
+    std::shared_ptr<const MpoInput> mpo;  // else the caller's MPO and initial MPS
+    bool keep_mps = false;                // the record keeps the final MPS (device memory until freed)
     std::vector<SweepSpec> sweeps;
     int prec = PREC_F64;
     double arrival = 0;          // seconds after the pool started (<= 0: at once)
@@ -45,6 +58,9 @@ struct SolveRecord {
 // (Davidson vectors, H_eff intermediates, density matrix, split-precision
 // digit panels).
 int64_t solve_footprint_estimate(ModelSpec const& m, std::vector<SweepSpec> const& sweeps, int prec);
+// The same bound for N sites of local dimension d and an MPO of bond dimension D.
+int64_t solve_footprint_estimate(int N, int d, int D, std::vector<SweepSpec> const& sweeps, int prec);
+int64_t solve_footprint_estimate(SolveRequest const& r);
 
 struct PoolStats {
     int64_t submitted = 0, done = 0, failed = 0;

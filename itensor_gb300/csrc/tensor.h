@@ -71,11 +71,16 @@ struct Sectors {
 
 uint64_t new_index_id();
 
+constexpr int TAG_BYTES = 28;  // four tags of seven characters (TagSet, itensor/tagset.h:35)
+
 struct Index {
     uint64_t id = 0;
     int32_t plev = 0;
     int32_t dir = 1;  // +1 Out, -1 In
     std::shared_ptr<const Sectors> sec;
+    // Tags as the reference stores them (carried through unchanged; only
+    // the checkpoint files read or write them). All zero: no tags.
+    std::array<char, TAG_BYTES> tags{};
 
     Index() = default;
     Index(std::vector<QN> qn, std::vector<int32_t> dims, int dir_, uint64_t id_ = 0, int plev_ = 0) {

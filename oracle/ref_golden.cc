@@ -19,6 +19,8 @@
 #include <string>
 #include <cmath>
 #include <cstdint>
+#include <chrono>
+#include <cstdlib>
 
 using namespace itensor;
 
@@ -717,9 +719,202 @@ static void gen_dmrg(std::string const& dir) {
     write_file(dir + "/dmrg.json", o.str());
 }
 
+// ---------------------------------------------------------------- benchmark configurations
+// The isolated H_eff apply in the benchmark's layout (Gaussian Sz link over
+// 2K+1 = 31 sectors, sigma = 6, N(0,1) blocks, Heisenberg bulk MPO tensors),
+// at bond dimension m (the benchmark runs m = 1024; the fixture is smaller).
+static void gen_heff_config(std::string const& dir, long m) {
+    Rng r(20241204);
+    int N = 12, b = 5;
+    auto sites = SpinHalf(N);
+    auto H = MPO(Heisenberg(sites));
+    auto W1 = H(b), W2 = H(b + 1);
+    auto s1 = sites(b), s2 = sites(b + 1);
+    auto wl = commonIndex(H(b - 1), H(b));
+    auto wr = commonIndex(H(b + 1), H(b + 2));
+    auto l = gauss_link(m, 15, 6.0, Out, "l");
+    auto rr = gauss_link(m, 15, 6.0, Out, "r");
+    auto psi = randqn(QN(), IndexSet(dag(l), s1, s2, rr), r);
+    auto L = randqn(QN(), IndexSet(l, wl, dag(prime(l))), r);
+    auto R = randqn(QN(), IndexSet(dag(rr), dag(wr), prime(rr)), r);
+    LocalOp op(W1, W2, L, R);
+    ITensor phip;
+    op.product(psi, phip);
+    std::ostringstream o;
+    o << "{\"kind\":\"heff\",\"cases\":[{\"name\":\"gauss31_m" << m << "\",\"m\":" << m << ",\"L\":" << jtensor(L)
+      << ",\"W1\":" << jtensor(W1) << ",\"W2\":" << jtensor(W2) << ",\"R\":" << jtensor(R) << ",\"phi\":"
+      << jtensor(psi) << ",\"Hphi\":" << jtensor(phip) << "}]}";
+    write_file(dir + "/heff_config.json", o.str());
+}
+
+// Hubbard model on the 4 x 16 cylinder (squareLattice Nx=16, Ny=4, periodic in
+// y, as sample/hubbard_2d.cc:17-46), t=1, U=4, half filling, Neel start; the
+// sweep table's maxdims up to `maxdim`, cutoff 1e-9, niter 2, noise 0 (so that
+// every bond step is reproducible; the sample's noise splits multiplets).
+static void gen_cylinder(std::string const& dir, int maxdim) {
+    int Nx = 16, Ny = 4, N = Nx * Ny;
+    double t = 1.0, U = 4.0;
+    auto sites = Electron(N);
+    auto ampo = AutoMPO(sites);
+    auto lattice = squareLattice(Nx, Ny, {"YPeriodic", true});
+    for (auto j : lattice) {
+        ampo += -t, "Cdagup", j.s1, "Cup", j.s2;
+        ampo += -t, "Cdagup", j.s2, "Cup", j.s1;
+        ampo += -t, "Cdagdn", j.s1, "Cdn", j.s2;
+        ampo += -t, "Cdagdn", j.s2, "Cdn", j.s1;
+    }
+    for (int j = 1; j <= N; ++j) ampo += U, "Nupdn", j;
+    auto H = toMPO(ampo);
+    auto st = InitState(sites);
+    for (int j = 1; j <= N; ++j) st.set(j, j % 2 == 1 ? "Up" : "Dn");
+    std::vector<int> mds;
+    for (int d : {20, 60, 100, 100, 200, 400, 800, 2000, 3000}) if (d < maxdim) mds.push_back(d);
+    mds.push_back(maxdim);
+    auto sw = mksweeps(mds, 1e-9);
+    auto t0 = std::chrono::steady_clock::now();
+    auto rec = run_dmrg("hubbard_cylinder_4x16", sites, H, MPS(st), sw,
+                        "{\"type\":\"hubbard\",\"t\":1.0,\"U\":4.0,\"Lx\":16,\"Ly\":4,\"yperiodic\":true}");
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::printf("  cylinder up to maxdim %d: %.1f s\n", maxdim, secs);
+    write_file(dir + "/cylinder.json", "{\"kind\":\"dmrg\",\"seconds\":" + num(secs) + ",\"cases\":[" + rec + "]}");
+}
+
+// dmrg() on the caller's own MPO and initial MPS: the reference's MPO tensors
+// (sample/Heisenberg.h for the chain, toMPO for the Hubbard ladder) and
+// MPS(InitState) tensors, with the run they give.
+template <typename SitesT>
+static std::string mpo_case(std::string const& name, SitesT const& sites, MPO const& H, MPS const& psi0,
+                            Sweeps const& sw, std::string const& model) {
+    int N = length(psi0);
+    std::ostringstream o;
+    o << "{\"W\":[";
+    for (int j = 1; j <= N; ++j) { if (j > 1) o << ","; o << jtensor(H(j)); }
+    o << "],\"psi0\":[";
+    for (int j = 1; j <= N; ++j) { if (j > 1) o << ","; o << jtensor(psi0(j)); }
+    o << "],\"run\":" << run_dmrg(name, sites, H, psi0, sw, model) << "}";
+    return o.str();
+}
+
+static void gen_mpo_io(std::string const& dir) {
+    std::vector<std::string> cs;
+    {
+        int N = 20;
+        auto sites = SpinHalf(N);
+        MPO H = Heisenberg(sites);
+        cs.push_back(mpo_case("heis20", sites, H, neel_mps(sites, N), mksweeps({10, 20, 100, 100, 200}, 1e-10),
+                              "{\"type\":\"heisenberg\",\"J\":1.0,\"Jz\":1.0}"));
+    }
+    {
+        int Nx = 4, Ny = 2, N = Nx * Ny;
+        auto sites = Electron(N);
+        auto ampo = AutoMPO(sites);
+        for (auto j : squareLattice(Nx, Ny, {"YPeriodic", false})) {
+            ampo += -1.0, "Cdagup", j.s1, "Cup", j.s2;
+            ampo += -1.0, "Cdagup", j.s2, "Cup", j.s1;
+            ampo += -1.0, "Cdagdn", j.s1, "Cdn", j.s2;
+            ampo += -1.0, "Cdagdn", j.s2, "Cdn", j.s1;
+        }
+        for (int j = 1; j <= N; ++j) ampo += 4.0, "Nupdn", j;
+        auto H = toMPO(ampo);
+        auto st = InitState(sites);
+        for (int j = 1; j <= N; ++j) st.set(j, j % 2 == 1 ? "Up" : "Dn");
+        cs.push_back(mpo_case("hubbard4x2", sites, H, MPS(st), mksweeps({20, 40, 80, 80}, 1e-10),
+                              "{\"type\":\"hubbard\",\"t\":1.0,\"U\":4.0,\"Lx\":4,\"Ly\":2,\"yperiodic\":false}"));
+    }
+    std::ostringstream o;
+    o << "{\"kind\":\"mpo_io\",\"cases\":[";
+    for (size_t n = 0; n < cs.size(); ++n) { if (n) o << ",\n"; o << cs[n]; }
+    o << "]}";
+    write_file(dir + "/mpo_io.json", o.str());
+}
+
+// Checkpoints in the reference's binary layout (MPS::write, itensor/mps/mps.cc:365-378,
+// ITensor::write itensor/itensor.cc:769-784, QDense write itensor/itdata/qdense.h:236-241,
+// writeToFile itensor/util/readwrite.h:363-370): the MPO and the MPS after the
+// first sweeps, the record of the run continued from that MPS, and the final MPS.
+template <typename SitesT>
+static std::string checkpoint_case(std::string const& dir, std::string const& name, SitesT const& sites, MPO const& H,
+                                   MPS const& psi0, Sweeps const& sw_first, Sweeps const& sw_rest,
+                                   std::string const& model) {
+    auto [E1, psi1] = dmrg(H, psi0, sw_first, {"Quiet", true, "Silent", true});
+    writeToFile(dir + "/" + name + ".mpo", H);
+    writeToFile(dir + "/" + name + "_start.mps", psi1);
+    Recorder obs(psi1);
+    auto [E2, psi2] = dmrg(H, psi1, sw_rest, obs, {"Quiet", true, "Silent", true});
+    writeToFile(dir + "/" + name + "_final.mps", psi2);
+    std::ostringstream o;
+    o << "{\"name\":\"" << name << "\",\"model\":" << model << ",\"N\":" << length(psi2) << ",\"mpo\":\"" << name
+      << ".mpo\",\"start\":\"" << name << "_start.mps\",\"final\":\"" << name << "_final.mps\",\"start_energy\":"
+      << num(E1) << ",\"start_lims\":[" << psi1.leftLim() << "," << psi1.rightLim() << "],\"final_lims\":["
+      << psi2.leftLim() << "," << psi2.rightLim() << "],\"sweeps\":[";
+    for (int s = 1; s <= sw_rest.nsweep(); ++s) {
+        if (s > 1) o << ",";
+        o << "{\"maxdim\":" << sw_rest.maxdim(s) << ",\"mindim\":" << sw_rest.mindim(s) << ",\"cutoff\":"
+          << num(sw_rest.cutoff(s)) << ",\"niter\":" << sw_rest.niter(s) << ",\"noise\":" << num(sw_rest.noise(s))
+          << "}";
+    }
+    o << "],\"energy\":" << num(E2) << ",\"bonds\":[" << obs.rec.str() << "],\"start_links\":[";
+    for (int b = 1; b < length(psi1); ++b) { if (b > 1) o << ","; o << jindex(linkIndex(psi1, b)); }
+    o << "],\"links\":[";
+    for (int b = 1; b < length(psi2); ++b) { if (b > 1) o << ","; o << jindex(linkIndex(psi2, b)); }
+    o << "],\"sites\":[";
+    for (int j = 1; j <= length(psi2); ++j) { if (j > 1) o << ","; o << jindex(sites(j)); }
+    o << "]}";
+    std::printf("  %s: E(start)=%.15f E(final)=%.15f\n", name.c_str(), E1, E2);
+    return o.str();
+}
+
+static void gen_checkpoint(std::string const& dir) {
+    std::vector<std::string> cs;
+    {
+        int N = 12;
+        auto sites = SpinHalf(N);
+        MPO H = Heisenberg(sites);
+        cs.push_back(checkpoint_case(dir, "heis12", sites, H, neel_mps(sites, N), mksweeps({8, 16}, 1e-10),
+                                     mksweeps({32, 32}, 1e-10), "{\"type\":\"heisenberg\",\"J\":1.0,\"Jz\":1.0}"));
+    }
+    {
+        int Nx = 4, Ny = 2, N = Nx * Ny;
+        auto sites = Electron(N);
+        auto ampo = AutoMPO(sites);
+        for (auto j : squareLattice(Nx, Ny, {"YPeriodic", false})) {
+            ampo += -1.0, "Cdagup", j.s1, "Cup", j.s2;
+            ampo += -1.0, "Cdagup", j.s2, "Cup", j.s1;
+            ampo += -1.0, "Cdagdn", j.s1, "Cdn", j.s2;
+            ampo += -1.0, "Cdagdn", j.s2, "Cdn", j.s1;
+        }
+        for (int j = 1; j <= N; ++j) ampo += 4.0, "Nupdn", j;
+        auto H = toMPO(ampo);
+        auto st = InitState(sites);
+        for (int j = 1; j <= N; ++j) st.set(j, j % 2 == 1 ? "Up" : "Dn");
+        cs.push_back(checkpoint_case(dir, "hubbard4x2", sites, H, MPS(st), mksweeps({10, 20}, 1e-10),
+                                     mksweeps({40, 40}, 1e-10),
+                                     "{\"type\":\"hubbard\",\"t\":1.0,\"U\":4.0,\"Lx\":4,\"Ly\":2,\"yperiodic\":false}"));
+    }
+    std::ostringstream o;
+    o << "{\"kind\":\"checkpoint\",\"cases\":[";
+    for (size_t n = 0; n < cs.size(); ++n) { if (n) o << ",\n"; o << cs[n]; }
+    o << "]}";
+    write_file(dir + "/checkpoint.json", o.str());
+}
+
+// Reads an MPS (or MPO) file with the reference's readFromFile and writes it
+// back with writeToFile: a file the reference can read gives the same bytes.
+static int rewrite_mps(std::string const& in, std::string const& out) {
+    MPS psi;
+    readFromFile(in, psi);
+    writeToFile(out, psi);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     std::string dir = argc > 1 ? argv[1] : "tests/golden";
     std::string what = argc > 2 ? argv[2] : "all";
+    if (dir == "--rewrite" && argc > 3) return rewrite_mps(argv[2], argv[3]);
+    if (what == "cylinder") { gen_cylinder(dir, argc > 3 ? std::atoi(argv[3]) : 200); return 0; }
+    if (what == "all" || what == "configs") gen_heff_config(dir, 256);
+    if (what == "all" || what == "mpo_io") gen_mpo_io(dir);
+    if (what == "all" || what == "checkpoint") gen_checkpoint(dir);
     if (what == "all" || what == "contract") gen_contract(dir);
     if (what == "all" || what == "heff") gen_heff(dir);
     if (what == "all" || what == "truncate") gen_truncate(dir);

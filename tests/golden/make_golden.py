@@ -19,7 +19,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ITENSOR_REFERENCE", "/root/reference")
     subprocess.check_call(["make", "-f", "oracle/Makefile.ref", "-j8", "REF=" + ref], cwd=ROOT)
     env = dict(os.environ, OMP_NUM_THREADS="1")
     subprocess.check_call([os.path.join(ROOT, "oracle/_ref/ref_golden"), os.path.join(ROOT, "tests/golden"), "all"],

@@ -114,3 +114,76 @@ def bst_json(X):
 
 def to_gpu(ctx, X, names):
     return gpu_tensor(ctx, bst_json(X), names)
+
+
+def device_to_oracle(t, names):
+    """A device tensor (itensor_gb300.Tensor) as an oracle BSTensor; QN slot k is `names[k]`."""
+    from oracle.blocksparse import BSTensor, Index as OIndex
+    inds = []
+    for I in t.inds:
+        secs = []
+        for q, d in zip(I.qns, I.dims):
+            items = [(names[k], int(q[k]), int(I.mods[k])) for k in range(len(names)) if I.mods[k] != 0]
+            secs.append((QN(*items), int(d)))
+        inds.append(OIndex(secs, dir=I.dir, id=str(I.id), plev=I.plev))  # fixture ids are strings
+    X = BSTensor(inds)
+    coords, offs = t.blocks()
+    data = t.numpy()
+    for c, o in zip(coords.reshape(len(offs), -1) if len(offs) else [], offs):
+        c = tuple(int(x) for x in c)
+        shp = X.block_shape(c)
+        n = int(np.prod(shp))
+        X.blocks[c] = np.reshape(data[o:o + n], shp, order="F").copy(order="F")
+    return X
+
+
+def workload_to_oracle(t):
+    """A synthetic workload tensor (itensor_gb300.workloads form: Sz in QN slot 0)
+    as an oracle BSTensor holding the same bytes."""
+    from oracle.blocksparse import BSTensor, Index as OIndex
+    inds = [OIndex([(QN(("Sz", q, 1)), d) for q, d in zip(I["qn"], I["dims"])], dir=I["dir"], id=str(I["id"]),
+                   plev=I["plev"]) for I in t["inds"]]
+    X = BSTensor(inds)
+    off = 0
+    for c in t["coords"]:
+        c = tuple(int(x) for x in c)
+        shp = X.block_shape(c)
+        n = int(np.prod(shp))
+        X.blocks[c] = np.reshape(t["data"][off:off + n], shp, order="F").copy(order="F")
+        off += n
+    return X
+
+
+def check_dmrg_record(res, ref, names, energy_tol=1e-10, trunc_tol=1e-12):
+    """A device DMRG result against a recorded reference run: final energy and
+    every bond step's energy within energy_tol, truncation errors within
+    trunc_tol, kept dimensions exact; final link layouts (arrow, QN sectors and
+    sizes) exact. QN slot k of the device indices is `names[k]`."""
+    assert abs(res.energy - ref["energy"]) < energy_tol, (res.energy, ref["energy"])
+    assert len(res.bonds) == len(ref["bonds"])
+    for a, b in zip(res.bonds, ref["bonds"]):
+        assert tuple(a[:3]) == tuple(b[:3])
+        assert abs(a[3] - b[3]) < energy_tol, (a, b)
+        assert abs(a[4] - b[4]) < trunc_tol, (a, b)
+        assert a[5] == b[5], (a, b)
+    assert len(res.links) == len(ref["links"])
+    for (dr, qn, dims), r in zip(res.links, ref["links"]):
+        assert dr == r["dir"]
+        got = [(tuple(sorted((names[k], int(q[k])) for k in range(len(names)) if q[k] != 0)), int(d))
+               for q, d in zip(qn, dims)]
+        assert got == json_sectors(r)
+
+
+def mps_energy(psi, W):
+    """<psi|H|psi> / <psi|psi> of an MPS (oracle BSTensors) under an MPO (oracle
+    BSTensors): the site of tensor j is the index it shares with W[j]."""
+    from oracle.blocksparse import contract
+    E = nrm = None
+    for A, Wj in zip(psi, W):
+        site_ids = {I.id for I in Wj.inds}
+        links = {I.id for I in A.inds if I.id not in site_ids}
+        Ad_all = A.dag().prime()
+        Ad_links = A.dag().prime(which=links)
+        E = contract(contract(contract(E, A) if E is not None else A, Wj), Ad_all)
+        nrm = contract(contract(nrm, A) if nrm is not None else A, Ad_links)
+    return float(E.scalar) / float(nrm.scalar)

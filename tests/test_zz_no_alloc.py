@@ -7,8 +7,9 @@ sandbox that forbids cudaMalloc after start-up. It runs a plan built earlier,
 with the split-precision digit panels in one fixed device array.
 
 Checked here through the C-ABI: two calls in a row match the pooled entry point
-(itg_contract_exec, same arithmetic) within the split-form tolerance, and a
-plan too large for the fixed array is refused with ITG_ERR_RANGE. Kept in its
+(itg_contract_exec, same arithmetic) within the split-form tolerance, calls
+leave the device's free memory unchanged, and a plan too large for the fixed
+array is refused with ITG_ERR_RANGE. Kept in its
 own file, collected last; it also passes alone in a fresh process.
 """
 import numpy as np
@@ -65,6 +66,24 @@ def test_noalloc_matches_pooled_exec_twice(ctx):
         o = out.cpu().numpy()
         assert np.all(np.isfinite(o)), call
         assert np.max(np.abs(o - r)) <= SPLIT_RTOL * scale, call
+
+
+def test_noalloc_calls_allocate_no_device_memory(ctx):
+    """The defining property: once the plan exists, calls take no device memory.
+    The driver's free-memory count stays put across several calls (a call that
+    grew any allocator pool, the library's or torch's, would lower it)."""
+    import torch
+    plan, psi, L = _psi_L_plan(ctx, 512)
+    _, _, size = plan.output()
+    out = torch.empty(size, dtype=torch.float64, device="cuda")
+    ctx.contract_exec_noalloc(plan, psi.device_ptr(), L.device_ptr(), out.data_ptr(), slices=6)  # set-up call
+    ctx.sync()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        ctx.contract_exec_noalloc(plan, psi.device_ptr(), L.device_ptr(), out.data_ptr(), slices=6)
+    ctx.sync()
+    assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_noalloc_rejects_plans_beyond_the_fixed_array(ctx):
