@@ -106,7 +106,62 @@ def _single_thread_env():
     return env
 
 
+REF_BENCH = os.path.join(ROOT, "oracle", "_ref", "ref_bench")
+
+
+def reference_runnable():
+    """('', True) when the reference library's timing program (oracle/ref_bench.cc,
+    built from the reference's own sources by oracle/Makefile.ref) runs on this
+    host, else (why not, False)."""
+    if not os.path.exists(REF_BENCH):
+        return ("the ITensor C++ reference is built only where its sources lie (the x86 build container); "
+                "this host has no build of it (oracle/_ref/ref_bench absent)"), False
+    try:
+        r = subprocess.run([REF_BENCH], capture_output=True, timeout=60)
+    except OSError as e:
+        return "oracle/_ref/ref_bench does not run on this host: %s" % e, False
+    return ("", True) if r.returncode == 2 else ("oracle/_ref/ref_bench failed: rc %d" % r.returncode, False)
+
+
+def _reference_heff(threads, budget_s):
+    """LocalOp::product of the reference library on the benchmark's bytes
+    (written in the reference's ITensor file layout): (applies, seconds)."""
+    import tempfile
+    from itensor_gb300 import workloads
+    from oracle import itensor_file
+    wl = workloads.heff_workload(M_BOND, K_SECT, SIGMA, SEED)
+    with tempfile.TemporaryDirectory() as d:
+        for k in ("psi", "L", "W1", "W2", "R"):
+            itensor_file.write(os.path.join(d, k + ".itensor"), wl[k])
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
+        out = subprocess.run([REF_BENCH, "heff", d, str(budget_s)], capture_output=True, text=True, env=env,
+                             timeout=600)
+    if out.returncode != 0:
+        raise RuntimeError("ref_bench heff: " + out.stderr[-300:])
+    r = json.loads(out.stdout.strip().splitlines()[-1])
+    return r["n"], r["sec"]
+
+
 def cpu_baseline(flops_per_apply, budget_s=15.0):
+    """The reference's own apply (LocalOp::product of the C++ library) timed on
+    one host core where it is built, else the oracle's restatement; a bounded
+    sample of the same input."""
+    why, ok = reference_runnable()
+    if ok:
+        try:
+            n, sec = _reference_heff(1, budget_s)
+            per = sec / n
+            return {"value": flops_per_apply / per / 1e12, "unit": UNIT, "cores": 1, "kind": "reference",
+                    "sample": "%d applies of the reference library's LocalOp::product (oracle/_ref, LAPACK/BLAS "
+                              "build, OMP 1, BLAS 1) on the same input, %.1f ms/apply" % (n, per * 1e3)}
+        except (RuntimeError, subprocess.TimeoutExpired, ValueError) as e:
+            why = str(e)[:300]
+    line = _port_baseline(flops_per_apply, budget_s)
+    line["reference_unavailable"] = why
+    return line
+
+
+def _port_baseline(flops_per_apply, budget_s):
     """Oracle apply timed on one host core in a subprocess (bounded sample)."""
     code = ("import sys,json;sys.path.insert(0,%r);import bench;"
             "t1=bench._oracle_apply_loop(1);n=max(1,int(%f/max(t1,1e-3)));"
@@ -126,11 +181,30 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
+    cores = os.cpu_count() or 1
+    flops = _oracle_flops()
+    why, ok = reference_runnable()
+    if ok:
+        # the reference library itself, all host threads (its OpenMP loop over output blocks), BLAS 1
+        try:
+            _reference_heff(cores, 0.2 * max(1, args.warmup))
+            n, sec = _reference_heff(cores, 0.5 * max(1, args.steps))
+            value = flops * n / sec / 1e12
+            line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                    "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / n * 1e3,
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                    "data": "synthetic", "config": CONFIG,
+                    "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "reference",
+                                     "sample": "%d applies of the reference library's LocalOp::product "
+                                               "(oracle/_ref, OMP_NUM_THREADS=%d, BLAS 1 thread)" % (n, cores)},
+                    "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            print(json.dumps(line))
+            return 0
+        except (RuntimeError, subprocess.TimeoutExpired, ValueError) as e:
+            why = str(e)[:300]
     import multiprocessing as mp
     for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
         os.environ[k] = "1"
-    cores = os.cpu_count() or 1
-    flops = _oracle_flops()
     ctxm = mp.get_context("spawn")
     with ctxm.Pool(cores, initializer=_oracle_worker_init) as pool:
         for _ in range(args.warmup):
@@ -147,8 +221,8 @@ def run_reference(args):
             "config": CONFIG,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": "each step: %d parallel single-thread applies of the numpy oracle "
-                                       "(restatement of LocalOp::product; the reference C++ library does not "
-                                       "build on the GPU host)" % cores},
+                                       "(restatement of LocalOp::product)" % cores,
+                             "reference_unavailable": why},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -307,34 +381,52 @@ def bench_batched(ctx, n_chains, n_seq, budget_bytes):
     t_seq = time.perf_counter() - t0
     seq_bonds = sum(len(r.bonds) for r in seq.values())
     workers, slots = pool_shape()
-    pool = itg.Pool(0, workers=workers, slots_per_worker=slots, budget_bytes=budget_bytes)
-    try:
-        ids = [pool.submit(m, sw, itg.PREC_OZAKI_BF16) for m, sw in chains]
-        t0 = time.perf_counter()
-        pool.start()
-        pool.drain()
-        t_pool = time.perf_counter() - t0
-        st = pool.stats()
-        res = {i: pool.result(ids[i]) for i in range(n_chains) if pool.record(ids[i]).status == 0}
-    finally:
-        pool.close()
+
+    def pool_run(prec):
+        pool = itg.Pool(0, workers=workers, slots_per_worker=slots, budget_bytes=budget_bytes)
+        try:
+            ids = [pool.submit(m, sw, prec) for m, sw in chains]
+            t0 = time.perf_counter()
+            pool.start()
+            pool.drain()
+            el = time.perf_counter() - t0
+            st = pool.stats()
+            res = {i: pool.result(ids[i]) for i in range(n_chains) if pool.record(ids[i]).status == 0}
+        finally:
+            pool.close()
+        return el, st, res
+
+    # the same pool (workers, slots, chains) in plain FP64: separates the
+    # precision form's gain from the concurrency's
+    t_pool64, st64, res64 = pool_run(itg.PREC_F64)
+    t_pool, st, res = pool_run(itg.PREC_OZAKI_BF16)
     pool_bonds = sum(len(r.bonds) for r in res.values())
-    dE = [abs(res[i].energy - seq[i].energy) for i in sample if i in res]
+    # split-precision energies against plain FP64, every chain
+    dE = [abs(res[i].energy - res64[i].energy) for i in range(n_chains) if i in res and i in res64]
+    dE_seq = [abs(res64[i].energy - seq[i].energy) for i in sample if i in res64]
     seq_rate = len(sample) / t_seq
     pool_rate = len(res) / t_pool
+    pool64_rate = len(res64) / t_pool64
     return {"workload": "%d independent J1-J2 chains (J2~U[0,0.5], N~U{16..64}, maxdim~U{64..256}, Sz QN, "
                         "Neel start, 5 sweeps ramping to maxdim, cutoff 1e-10, niter 2; seed %d)" % (n_chains, BATCH_SEED),
             "batched": {"precision": "split (6 BF16 slices, FP32-exact accumulation); FP64 Davidson, eigensolver, SVD",
                         "seconds": t_pool, "solves_per_s": pool_rate, "sweeps_per_s": pool_rate * 5,
                         "bond_steps_per_s": pool_bonds / t_pool, "failed": st["failed"],
                         "workers": workers, "slots_per_worker": slots, "peak_running": st["peak_running"]},
+            "pool_f64": {"precision": "plain FP64, the same pool shape and chains", "seconds": t_pool64,
+                         "solves_per_s": pool64_rate, "bond_steps_per_s": sum(len(r.bonds) for r in res64.values())
+                         / t_pool64, "failed": st64["failed"], "peak_running": st64["peak_running"]},
             "plain_f64_sequential": {"chains": len(sample), "seconds": t_seq, "solves_per_s": seq_rate,
                                      "sweeps_per_s": seq_rate * 5, "bond_steps_per_s": seq_bonds / t_seq,
                                      "sample": "every %dth chain of the same set, one context, one after the other"
                                                % stride},
             "speedup_solves_per_s": pool_rate / seq_rate,
+            "speedup_split_over_pool_f64": pool_rate / pool64_rate,
+            "speedup_pool_f64_over_sequential_f64": pool64_rate / seq_rate,
             "energy_vs_f64": {"max_abs_dE": max(dE) if dE else None,
-                              "within_1e-9": sum(1 for x in dE if x <= 1e-9), "compared": len(dE)}}
+                              "within_1e-9": sum(1 for x in dE if x <= 1e-9), "compared": len(dE),
+                              "against": "the same chains in the FP64 pool"},
+            "pool_f64_vs_sequential_max_abs_dE": max(dE_seq) if dE_seq else None}
 
 
 def bench_serving(n_req, budget_bytes, load=0.8):
@@ -628,6 +720,14 @@ def main():
         roofline["mma_sync_bf16_tflops_measured"] = None
         roofline["peaks_error"] = str(e)[:200]
     d64_ms, d64_flops, _ = dom_stats(prof_64)
+    # the plain FP64 path's dominant kernel (gemm_f64_kernel, psi*L) against the FP64 FFMA
+    # issue rate this library measures (register-only loop; no FP64 figure in MEASURED_PEAKS.json)
+    f64_ach = d64_flops / (d64_ms / 1e3) / 1e12
+    f64_peak = roofline.get("fp64_ffma_tflops_measured")
+    f64_roofline = {"bound": "fp64", "achieved": f64_ach, "peak": f64_peak, "unit": "TFLOP/s",
+                    "frac": f64_ach / f64_peak if f64_peak else None, "traffic": None,
+                    "kernel": "gemm_f64_kernel (psi*L block GEMM)",
+                    "note": "peak = FP64 FFMA rate measured by itg_measure_peaks on this GPU (of measured)"}
 
     # end-to-end through the C-ABI with host buffers: psi host -> device, apply, result -> host
     psi_host = np.ascontiguousarray(wl["psi"]["data"])
@@ -703,7 +803,8 @@ def main():
                 "split_vs_f64_max_rel_err": rel,
                 "f64_path": {"value": f64_value, "unit": UNIT, "ms_per_step": t_64 / n64,
                              "dominant_kernel_ms": d64_ms,
-                             "dominant_kernel_tflops": d64_flops / (d64_ms / 1e3) / 1e12},
+                             "dominant_kernel_tflops": d64_flops / (d64_ms / 1e3) / 1e12,
+                             "roofline": f64_roofline},
                 "speedup_split_over_f64": value / f64_value,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk, "dmrg_heis20": dmrg, "batched_chains": batched, "serving": serving}
