@@ -126,7 +126,7 @@ int itg_set_precision(itg_ctx* c, int mode, int slices) {
 
 int itg_set_gemm_variant(itg_ctx* c, int variant) {
     return guard(c, [&] {
-        ITG_REQUIRE(variant >= -1 && variant <= 3, "gemm variant must be -1..3");
+        ITG_REQUIRE(variant >= -1 && variant <= 4, "gemm variant must be -1..4");
         c->ctx.gemm_variant = variant;
     });
 }

@@ -569,6 +569,9 @@ Ctx::Ctx(int dev) : device(dev) {
     uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
     ITG_CHECK_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
     ITG_CHECK_CUDA(cudaEventCreateWithFlags(&sync_event, cudaEventDisableTiming));
+    ITG_CHECK_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&err_host), 64, cudaHostAllocMapped));
+    ITG_CHECK_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&err_dev), err_host, 0));
+    err_host[0] = 0;
 }
 
 cudaStream_t Ctx::side_stream(int i) {
@@ -603,6 +606,7 @@ Ctx::~Ctx() {
     plans.reset();
     split_scratch.reset();
     if (sync_event) cudaEventDestroy(sync_event);
+    if (err_host) cudaFreeHost(err_host);
     if (pin) cudaFreeHost(pin);
     if (stage) cudaFreeHost(stage);
     if (stream) {
@@ -630,6 +634,12 @@ void Ctx::sync() {
         fiber_wait_event(sync_event);
     } else {
         ITG_CHECK_CUDA(cudaStreamSynchronize(stream));
+    }
+    if (err_host && *reinterpret_cast<volatile int*>(err_host)) {
+        const int code = err_host[0];
+        err_host[0] = 0;
+        throw Error(ERR_TIMEOUT, "a kernel's bounded wait gave up (tensor-core MMA completion, code " +
+                                     std::to_string(code) + "); its output is not valid");
     }
 }
 
@@ -1066,18 +1076,39 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             std::stable_sort(o64.begin(), o64.end(), [&](int x, int y) { return cost64[x] > cost64[y]; });
             for (int i : o64) items64.push_back(raw[i]);
         }
+        // tensor-core tiles: 128 rows along each block's longer side, TC_TILE_N columns along the other
+        std::vector<TcItem> items_tc;
+        if (!plan->skinny) {
+            std::vector<TcItem> raw;
+            std::vector<double> ctc;
+            for (int c = 0; c < ncb; ++c) {
+                const int swap = cblk[c].N > cblk[c].M ? 1 : 0;
+                const int R = swap ? cblk[c].N : cblk[c].M, W = swap ? cblk[c].M : cblk[c].N;
+                for (int r0 = 0; r0 < R; r0 += TC_TILE_M)
+                    for (int c0 = 0; c0 < W; c0 += TC_TILE_N) {
+                        raw.push_back(TcItem{c, r0, c0, cp0[c], cp1[c], swap});
+                        ctc.push_back(cK[c] + 1.0);
+                    }
+            }
+            std::vector<int> otc(raw.size());
+            std::iota(otc.begin(), otc.end(), 0);
+            std::stable_sort(otc.begin(), otc.end(), [&](int x, int y) { return ctc[x] > ctc[y]; });
+            for (int i : otc) items_tc.push_back(raw[i]);
+        }
         // upload
         size_t t_items = 0, t_pairs = align16(sizeof(ItemRec) * sitems.size());
         size_t t_cblk = align16(t_pairs + sizeof(PairRec) * pairs.size());
         size_t t_ops = align16(t_cblk + sizeof(CBlockRec) * cblk.size());
         size_t t_prep = align16(t_ops + sizeof(OpBlockRec) * ops.size());
         size_t t_i64 = align16(t_prep + sizeof(PrepItem) * prep.size());
-        size_t t_tab = align16(t_i64 + sizeof(ItemRec) * items64.size());
+        size_t t_itc = align16(t_i64 + sizeof(ItemRec) * items64.size());
+        size_t t_tab = align16(t_itc + sizeof(TcItem) * items_tc.size());
         size_t tbytes = align16(t_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size()));
         ctx.ensure_stage(tbytes);
         st = static_cast<char*>(ctx.stage);
         if (!sitems.empty()) std::memcpy(st + t_items, sitems.data(), sizeof(ItemRec) * sitems.size());
         if (!items64.empty()) std::memcpy(st + t_i64, items64.data(), sizeof(ItemRec) * items64.size());
+        if (!items_tc.empty()) std::memcpy(st + t_itc, items_tc.data(), sizeof(TcItem) * items_tc.size());
         if (!pairs.empty()) std::memcpy(st + t_pairs, pairs.data(), sizeof(PairRec) * pairs.size());
         if (!cblk.empty()) std::memcpy(st + t_cblk, cblk.data(), sizeof(CBlockRec) * cblk.size());
         if (!ops.empty()) std::memcpy(st + t_ops, ops.data(), sizeof(OpBlockRec) * ops.size());
@@ -1103,6 +1134,8 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->d_tab = reinterpret_cast<int32_t*>(db + t_tab);
         plan->d_items64 = reinterpret_cast<ItemRec*>(db + t_i64);
         plan->nitems64 = (int)items64.size();
+        plan->d_items_tc = reinterpret_cast<TcItem*>(db + t_itc);
+        plan->nitems_tc = (int)items_tc.size();
         plan->nitems = (int)sitems.size();
         plan->npairs = np;
         plan->ncblk = ncb;

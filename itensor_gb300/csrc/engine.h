@@ -48,6 +48,14 @@ struct CBlockRec {        // output block
 struct ItemRec {          // one output tile (TILE x TILE) of one output block
     int32_t c, m0, n0, p0, p1;
 };
+// One output tile of the tensor-core (tcgen05) split-precision kernel: 128
+// rows along the block's longer side (swap = 0: C's m, A's rows; swap = 1: C's
+// n, B's rows) times TC_TILE_N columns along the other side.
+struct TcItem {
+    int32_t c, r0, c0, p0, p1, swap;
+};
+constexpr int TC_TILE_M = 128;
+constexpr int TC_TILE_N = 32;
 
 // Offset tables ("table positions" above): the element offsets of a block's
 // rows (or columns, or contracted positions) in enumeration order, stored as
@@ -96,6 +104,9 @@ struct Plan {
     // 64-row tiles of the same output blocks (the 64 x 32 split-precision variant)
     ItemRec* d_items64 = nullptr;
     int nitems64 = 0;
+    // 128 x TC_TILE_N tiles of the tensor-core (tcgen05) variant
+    TcItem* d_items_tc = nullptr;
+    int nitems_tc = 0;
     // split-precision GEMM variant picked by the autotuner (-1: not tuned, run variant 0)
     mutable std::atomic<int> oz_variant{-1};
     // split-precision executions so far (a plan is tuned only once it is reused)
@@ -156,6 +167,10 @@ struct Ctx {
     DevBufPtr split_scratch;
     // event used by sync() when the calling thread multiplexes solves
     cudaEvent_t sync_event = nullptr;
+    // status word in host-mapped memory: a kernel whose bounded wait gave up
+    // sets it (and returns); sync() turns it into ERR_TIMEOUT
+    int* err_host = nullptr;
+    int* err_dev = nullptr;
     // freed buffers of this stream, reused by its next allocations
     std::shared_ptr<BlockCache> cache;
     // partial sums + completion counter of the fused reductions (ops.cu)
@@ -222,6 +237,11 @@ void exec_plan_noalloc(Ctx& ctx, Plan const& p, double const* A, double const* B
 // the plan's scratch (S digit planes of the padded panel size, row exponents).
 void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S, __nv_bfloat16* panels,
                   int32_t* exps, bool prep_b = true);
+// The tensor-core variant of the split-precision GEMM (ozaki_tc.cu): digit
+// panels staged into shared memory, tcgen05.mma with the diagonal sums in
+// tensor memory. Panels and exponents must be in place (the prep has run).
+void launch_ozaki_tc(Ctx& ctx, Plan const& p, double* C, int S, __nv_bfloat16 const* panels, int64_t plane,
+                     int32_t const* exps);
 // Times every split-precision GEMM variant of the plan on these operands and
 // stores the fastest in p.oz_variant (ozaki.cu); C is overwritten.
 int autotune_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S,
