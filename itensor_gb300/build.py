@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["contract.cu", "ozaki.cu", "ops.cu", "eigh.cu", "eigh_tri.cu", "svd.cu", "peaks.cu", "noalloc.cu"]
 CPP_SOURCES = ["tridiag_ql.cpp", "tensor.cpp", "algo_core.cpp", "heff_program.cpp", "svd_split.cpp", "models.cpp", "dmrg.cpp", "fiber.cpp", "pool.cpp", "mps_io.cpp", "capi.cpp"]
 HEADERS = ["common.h", "tensor.h", "engine.h", "ops.h", "algo.h", "fiber.h", "pool.h", "eigh_tri.h", "tridiag_ql.h",
-           "mps_io.h"]
+           "mps_io.h", "ozaki_tc.cuh"]
 
 
 def _newest(paths):

@@ -991,7 +991,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             o.src = src; o.rows = rows; o.K = K; o.Kp = (K + 15) / 16 * 16;
             o.trow = trow; o.tcol = tcol;
             o.panel = panel; o.exp = (int32_t)expo;
-            panel += ((int64_t)rows * o.Kp + 15) / 16 * 16;
+            panel += (int64_t)panel_row_groups(rows) * 8 * o.Kp;  // tiled: whole row groups, 128-element units
             expo += rows;
             max_rows = std::max(max_rows, rows);
             ops.push_back(o);

@@ -28,8 +28,13 @@ struct PairRec {          // one (A block, B block) product feeding an output bl
     int32_t pad;
 };
 // One operand block seen as a rows x K matrix (rows = A's m or B's n), for the
-// split-precision path: its digit planes are stored k-contiguous, K padded to
-// Kp (multiple of 16), one power-of-two exponent per row.
+// split-precision path: K padded to Kp (multiple of 16), one power-of-two
+// exponent per row, and per digit plane a tiled panel: k-steps of 16
+// outermost, then groups of 8 rows, then the two 8-k halves of the step, each
+// an 8 rows x 8 k core matrix (16 bytes per row). One k-step of 8g rows is
+// then one contiguous run of g x 256 bytes laid out exactly as the tensor
+// cores read a K-major operand without swizzle (core matrices 128 B apart
+// along k, 256 B apart along the rows), so it moves with one bulk copy.
 struct OpBlockRec {
     int64_t src;          // element offset of the block in the operand
     int64_t panel;        // bf16 element offset of digit plane 0 in the panel buffer
@@ -37,6 +42,16 @@ struct OpBlockRec {
     int32_t trow, tcol;   // table positions: offsets along rows and along k
     int32_t exp;          // position of the row exponents in the exponent buffer
 };
+#ifdef __CUDACC__
+#define ITG_HD __host__ __device__ __forceinline__
+#else
+#define ITG_HD inline
+#endif
+ITG_HD int panel_row_groups(int rows) { return (rows + 7) >> 3; }
+// element offset of digit (row r, k) in a block's tiled panel of nrg row groups
+ITG_HD int64_t panel_off(int r, int k, int nrg) {
+    return ((int64_t)(k >> 4) * nrg + (r >> 3)) * 128 + ((k >> 3) & 1) * 64 + (r & 7) * 8 + (k & 7);
+}
 struct PrepItem {         // rows [r0, r1) of operand block `op`; which = 0 (A) or 1 (B)
     int32_t op, r0, r1, which;
 };
@@ -259,9 +274,15 @@ inline bool plan_uses_split(Plan const& p, int prec) {
     return !p.skinny && prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0 && p.max_pair_K <= SPLIT_MAX_PAIR_K;
 }
 // Bytes of split-precision scratch (digit planes + row exponents) a plan needs.
+// The tensor-core kernel copies whole 128-row (or TC_TILE_N-row) k-steps: the
+// rows past a block's end come from whatever follows it (they only feed
+// output rows that are never stored), and at the very end of the scratch
+// they come from this padding.
+constexpr size_t SPLIT_SCRATCH_PAD = 2 * TC_TILE_M * 16 * sizeof(__nv_bfloat16);
 inline size_t split_scratch_bytes(Plan const& p, int S) {
     const int64_t plane = (p.panel_elems + 15) / 16 * 16;
-    return sizeof(__nv_bfloat16) * (size_t)plane * S + sizeof(int32_t) * (size_t)(p.exp_elems + 4);
+    return sizeof(__nv_bfloat16) * (size_t)plane * S + sizeof(int32_t) * (size_t)(p.exp_elems + 4) +
+           SPLIT_SCRATCH_PAD;
 }
 
 // TFLOP/s of [FP64 FFMA, FP32 FFMA, FP64 mma.sync, TF32 mma.sync, BF16 mma.sync] (peaks.cu)

@@ -36,14 +36,53 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
     }
     P->in_size = phi_layout->size;
     P->in = dev_alloc(sizeof(double) * std::max<int64_t>(1, P->in_size), ctx.stream);
+
+    // The layouts the reference's chain produces, step by step (plans only,
+    // nothing runs): ((phi L) W1) W2 R. Their flops are the algorithmic work.
+    std::vector<std::shared_ptr<Layout>> ref_out;
+    {
+        std::shared_ptr<Layout> cur = phi_layout;
+        for (size_t s = 0; s < chain.size(); ++s) {
+            const bool last = (s + 1 == chain.size());
+            Match mt = match_indices(cur->inds, chain[s]->inds());
+            auto plan = get_plan(ctx, *cur, *chain[s]->lay, mt, last ? target : nullptr);
+            auto outL = std::make_shared<Layout>(*plan->C);
+            if (!(last && target)) {
+                outL->inds.clear();
+                for (int i : mt.a_unc) outL->inds.push_back(cur->inds[i]);
+                for (int j : mt.b_unc) outL->inds.push_back(chain[s]->inds()[j]);
+            }
+            P->flops += plan->flops;
+            ref_out.push_back(outL);
+            cur = outL;
+        }
+    }
+    // The two MPO tensors are contracted with each other once (W1 W2, or W2 W1
+    // from the right end), so an apply runs one MPO-tensor step instead of two
+    // and one intermediate less goes through memory. That step writes the
+    // layout the reference's second MPO step produces (same index order, same
+    // blocks), so everything after it is unchanged.
+    Tensor Wf;
+    size_t wpos = 0;
+    for (size_t s = 0; s + 1 < chain.size(); ++s)
+        if ((chain[s] == op.W1 && chain[s + 1] == op.W2) || (chain[s] == op.W2 && chain[s + 1] == op.W1)) wpos = s + 1;
+    if (wpos > 0) {
+        Wf = contract(ctx, *chain[wpos - 1], *chain[wpos], PREC_F64);
+        chain.erase(chain.begin() + (long)wpos);
+        chain[wpos - 1] = &Wf;
+        ref_out.erase(ref_out.begin() + (long)(wpos - 1));  // the fused step writes the second step's layout
+    }
     std::shared_ptr<Layout> cur = phi_layout;
     for (size_t s = 0; s < chain.size(); ++s) {
         const bool last = (s + 1 == chain.size());
         Match mt = match_indices(cur->inds, chain[s]->inds());
-        auto plan = get_plan(ctx, *cur, *chain[s]->lay, mt, last ? target : nullptr);
+        const bool fused = wpos > 0 && s == wpos - 1;
+        auto plan = get_plan(ctx, *cur, *chain[s]->lay, mt, (last && target) ? target : (fused ? ref_out[s] : nullptr));
         std::shared_ptr<Layout> outL;
         if (last && target) {
             outL = target;
+        } else if (fused) {
+            outL = ref_out[s];
         } else {
             outL = std::make_shared<Layout>(*plan->C);
             outL->inds.clear();
@@ -65,7 +104,6 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
             P->inter.push_back(dev_alloc(sizeof(double) * std::max<int64_t>(1, outL->size), ctx.stream));
             st.out_buf = (int)P->inter.size() - 1;
         }
-        P->flops += plan->flops;
         P->steps.push_back(st);
         cur = outL;
     }

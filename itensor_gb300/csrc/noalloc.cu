@@ -83,7 +83,7 @@ void exec_plan_noalloc(Ctx& ctx, Plan const& p, double const* A, double const* B
     }
     const int64_t plane = (p.panel_elems + 15) / 16 * 16;
     const size_t panel_bytes = sizeof(__nv_bfloat16) * (size_t)plane * S;
-    const size_t need = panel_bytes + sizeof(int32_t) * (size_t)(p.exp_elems + 4);
+    const size_t need = split_scratch_bytes(p, S);
     if (need > (size_t)ITG_NOALLOC_SCRATCH_BYTES)
         throw Error(ERR_RANGE, "contract_exec_noalloc: the plan needs " + std::to_string(need) +
                                    " bytes of scratch, the fixed array holds " +

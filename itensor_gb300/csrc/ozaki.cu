@@ -100,11 +100,12 @@ __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restr
         }
         __syncthreads();
         for (int r = threadIdx.x; r < rows; r += blockDim.x) exps[ob.exp + pi.r0 + r] = rexp[r] - 1022;
-        const int np = rows * ob.Kp;
-        __nv_bfloat16* pan = panels + ob.panel + (int64_t)pi.r0 * ob.Kp;
+        const int np = rows * ob.Kp, nrg = panel_row_groups(ob.rows);
+        __nv_bfloat16* pan = panels + ob.panel;
         for (int e = threadIdx.x; e < np; e += blockDim.x) {
             const int k = e % ob.Kp, r = e / ob.Kp;
-            oz_digits<S>(k < ob.K ? base[trow[r] + tab_at(tab, ob.tcol, k)] : 0.0, rexp[r], pan + e, plane);
+            oz_digits<S>(k < ob.K ? base[trow[r] + tab_at(tab, ob.tcol, k)] : 0.0, rexp[r],
+                         pan + panel_off(pi.r0 + r, k, nrg), plane);
         }
         return;
     }
@@ -122,14 +123,15 @@ __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restr
             emax = max(emax, exp_field(base[ro + tab_at(tab, ob.tcol, k)]));
         emax = __reduce_max_sync(0xffffffffu, emax);
         if (lane == 0) exps[ob.exp + r] = emax - 1022;  // |x| < 2^(E-1022)
-        __nv_bfloat16* pan = panels + ob.panel + (int64_t)r * ob.Kp;
+        __nv_bfloat16* pan = panels + ob.panel;
+        const int nrg = panel_row_groups(ob.rows);
 #pragma unroll
         for (int j = 0; j < OZ_PREP_REGS; ++j) {
             const int k = lane + 32 * j;
-            if (k < ob.Kp) oz_digits<S>(xr[j], emax, pan + k, plane);
+            if (k < ob.Kp) oz_digits<S>(xr[j], emax, pan + panel_off(r, k, nrg), plane);
         }
         for (int k = lane + 32 * OZ_PREP_REGS; k < ob.Kp; k += 32)
-            oz_digits<S>(k < ob.K ? base[ro + tab_at(tab, ob.tcol, k)] : 0.0, emax, pan + k, plane);
+            oz_digits<S>(k < ob.K ? base[ro + tab_at(tab, ob.tcol, k)] : 0.0, emax, pan + panel_off(r, k, nrg), plane);
     }
 }
 
@@ -217,12 +219,14 @@ __device__ __forceinline__ void oz_tile(ItemRec const& it, const PairRec* __rest
                 if (r2 < S * TM) {
                     const int row = r2 % TM, s = r2 / TM;
                     const bool ok = it.m0 + row < cb.M;
-                    const __nv_bfloat16* src = ok ? pa + s * plane + (int64_t)(it.m0 + row) * oa.Kp + k0 + half * 8 : pa;
+                    const __nv_bfloat16* src =
+                        ok ? pa + s * plane + panel_off(it.m0 + row, k0 + half * 8, panel_row_groups(oa.rows)) : pa;
                     cp_async16(&As[buf][s][row][half * 8], src, ok);
                 } else {
                     const int row = (r2 - S * TM) % TN, s = (r2 - S * TM) / TN;
                     const bool ok = it.n0 + row < cb.N;
-                    const __nv_bfloat16* src = ok ? pb + s * plane + (int64_t)(it.n0 + row) * ob.Kp + k0 + half * 8 : pb;
+                    const __nv_bfloat16* src =
+                        ok ? pb + s * plane + panel_off(it.n0 + row, k0 + half * 8, panel_row_groups(ob.rows)) : pb;
                     cp_async16(&Bs[buf][s][row][half * 8], src, ok);
                 }
             }
@@ -340,259 +344,7 @@ gemm_ozaki_kernel(const ItemRec* __restrict__ items, int nitems, const PairRec* 
 }
 
 // ---------------------------------------------------------------- tensor-core (tcgen05) variant
-//
-// The same digit products on the 5th-generation tensor cores: one CTA (one
-// warpgroup) per output tile of 128 rows (TMEM lanes) x TN columns. Per k-step
-// of 16 the S digit planes of both operands' tiles are staged with cp.async
-// into shared memory in the no-swizzle K-major core-matrix layout (8 rows x
-// 16 bytes per core matrix; neighbours along k 128 B apart, along the rows
-// 256 B apart), two stages in a ring. One thread issues the S(S+1)/2
-// tcgen05.mma (kind::f16, BF16 in, FP32 accumulate) of the step, each into the
-// TMEM columns of its diagonal D = s + t, and commits them to the stage's
-// mbarrier; the stage is refilled once that barrier has flipped. Every KCHUNK k
-// (and at each pair's end) the warps read the S diagonals back with
-// tcgen05.ld (thread t holds row t), fold them exactly into int64 and, per
-// pair, scale into the FP64 result as the mma.sync variants do: the results
-// are bit-identical to theirs. Every wait on an mbarrier is bounded (clock64);
-// a wait that gives up sets the context's status word, waits (bounded) for the
-// MMAs in flight, frees TMEM and returns without writing the tile.
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Waits for the completion of the barrier phase with this parity, at most
-// `limit` SM clocks; false when it gave up.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long long limit) {
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > limit) return false;
-    return true;
-}
-
-// Shared-memory matrix descriptor of tcgen05.mma: start address, leading
-// (k-direction) and stride (row-direction) byte offsets of the core matrices,
-// descriptor version 1, no swizzle.
-__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
-
-// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, M x N.
-__host__ __device__ constexpr uint32_t tc_idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void tc_commit(uint32_t bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-// 32 consecutive TMEM columns of this warp's 32 lanes (thread = lane = row)
-__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-template <int S, int TN>
-struct TcShape {
-    static constexpr int TM = TC_TILE_M, KS = 16;
-    static constexpr int A_PLANE = TM * KS * 2;   // bytes of one digit plane of the row tile
-    static constexpr int B_PLANE = TN * KS * 2;   // of the column tile
-    static constexpr int STAGE = S * (A_PLANE + B_PLANE);
-    static constexpr int KCHUNK = (S <= 4) ? 256 : 128;
-    static constexpr int CHUNK_STEPS = KCHUNK / KS;
-    static constexpr uint32_t TMEM_COLS = (S * TN <= 128) ? 128 : (S * TN <= 256 ? 256 : 512);
-    static constexpr int OUT = 8 * TN * TM;          // FP64 partial results, [column][row]
-    static constexpr int TAIL = 64 + 4 * TN;        // barriers, TMEM address, column exponents
-    // at least 80 KB, so that at most two CTAs share an SM (their TMEM then always fits)
-    static constexpr size_t SMEM =
-        (2 * STAGE + OUT + TAIL) > 80 * 1024 ? (size_t)(2 * STAGE + OUT + TAIL) : (size_t)80 * 1024;
-};
-
-template <int S, int TN>
-__global__ void __launch_bounds__(128, 1)
-gemm_ozaki_tc_kernel(const TcItem* __restrict__ items, const PairRec* __restrict__ pairs,
-                     const CBlockRec* __restrict__ cblk, const OpBlockRec* __restrict__ ops,
-                     const int32_t* __restrict__ tab, const __nv_bfloat16* __restrict__ panels, int64_t plane,
-                     const int32_t* __restrict__ exps, double* __restrict__ C, int* __restrict__ status,
-                     long long wait_limit, int stuck_test) {
-    using SH = TcShape<S, TN>;
-    static_assert(S * TN <= 512, "diagonal accumulators must fit in TMEM");
-    static_assert((long long)SH::KCHUNK * S * 128 * 128 <= (1LL << 24), "digit sums must stay exact in FP32");
-    extern __shared__ __align__(128) unsigned char tc_smem[];
-    unsigned char* stage0 = tc_smem;
-    double* outs = reinterpret_cast<double*>(tc_smem + 2 * SH::STAGE);  // outs[j * TM + row]
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(tc_smem + 2 * SH::STAGE + SH::OUT);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tc_smem + 2 * SH::STAGE + SH::OUT + 16);
-    int* ecol = reinterpret_cast<int*>(tc_smem + 2 * SH::STAGE + SH::OUT + 64);
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const TcItem it = items[blockIdx.x];
-    const CBlockRec cb = cblk[it.c];
-    const uint32_t bar0 = smem_u32(&mbar[0]), bar1 = smem_u32(&mbar[1]);
-    // a barrier nothing arrives at: with stuck_test the first fold waits on it
-    // until the wait limit runs out (the test of the timeout path)
-    const uint32_t bar_stuck = smem_u32(tmem_slot + 2);
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar1));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_stuck));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(SH::TMEM_COLS));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
-    const uint32_t tmem_warp = tmem + ((uint32_t)(warp * 32) << 16);
-    const int Mrows = it.swap ? cb.N : cb.M, Ncols = it.swap ? cb.M : cb.N;
-    constexpr uint32_t IDESC = tc_idesc_bf16(SH::TM, TN);
-    uint32_t ncommit[2] = {0u, 0u};
-    long long tot[TN];
-    bool fail = false;
-    const int row = it.r0 + tid;
-    for (int p = it.p0; p < it.p1 && !fail; ++p) {
-        const PairRec pr = pairs[p];
-        const OpBlockRec orow = ops[it.swap ? pr.ib : pr.ia];
-        const OpBlockRec ocol = ops[it.swap ? pr.ia : pr.ib];
-        const __nv_bfloat16* prow = panels + orow.panel;
-        const __nv_bfloat16* pcol = panels + ocol.panel;
-        const int Kp = orow.Kp;
-        const int nk = Kp / SH::KS;
-        const int erow = row < Mrows ? exps[orow.exp + row] : 0;
-        __syncthreads();  // the previous pair's readers of ecol are done
-        for (int j = tid; j < TN; j += 128) ecol[j] = (it.c0 + j < Ncols) ? exps[ocol.exp + it.c0 + j] : 0;
-#pragma unroll
-        for (int j = 0; j < TN; ++j) tot[j] = 0;
-        // stage k-step kk into ring slot buf: 16-byte chunks (8 k of one row) into core matrices
-        auto load = [&](int kk, int buf) {
-            unsigned char* sb = stage0 + buf * SH::STAGE;
-            const int k0 = kk * SH::KS;
-#pragma unroll 1
-            for (int e = tid; e < S * (SH::TM + TN) * 2; e += 128) {
-                const int kg = e & 1, r2 = e >> 1;
-                if (r2 < S * SH::TM) {
-                    const int s = r2 / SH::TM, r = r2 % SH::TM;
-                    const bool ok = it.r0 + r < Mrows;
-                    const __nv_bfloat16* src = ok ? prow + s * plane + (int64_t)(it.r0 + r) * Kp + k0 + kg * 8 : prow;
-                    cp_async16(sb + s * SH::A_PLANE + ((r >> 3) * 2 + kg) * 128 + (r & 7) * 16, src, ok);
-                } else {
-                    const int r3 = r2 - S * SH::TM;
-                    const int s = r3 / TN, r = r3 % TN;
-                    const bool ok = it.c0 + r < Ncols;
-                    const __nv_bfloat16* src = ok ? pcol + s * plane + (int64_t)(it.c0 + r) * Kp + k0 + kg * 8 : pcol;
-                    cp_async16(sb + S * SH::A_PLANE + s * SH::B_PLANE + ((r >> 3) * 2 + kg) * 128 + (r & 7) * 16, src,
-                               ok);
-                }
-            }
-            cp_async_commit();
-        };
-        load(0, 0);
-        for (int kk = 0; kk < nk; ++kk) {
-            const int buf = kk & 1;
-            if (kk + 1 < nk) {
-                // ring slot buf^1 was last read by the MMAs of step kk-1 (or an earlier pair's)
-                if (ncommit[buf ^ 1] > 0) {
-                    const bool ok = mbar_wait_bounded(buf ? bar0 : bar1, (ncommit[buf ^ 1] - 1) & 1, wait_limit);
-                    if (__syncthreads_or(!ok)) { fail = true; break; }
-                }
-                load(kk + 1, buf ^ 1);
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // cp.async data -> the MMA's reads
-            __syncthreads();
-            tc_fence_after();
-            if (tid == 0) {
-                const bool first = (kk % SH::CHUNK_STEPS) == 0;
-                const uint32_t sa = smem_u32(stage0 + buf * SH::STAGE), sbb = sa + S * SH::A_PLANE;
-#pragma unroll 1
-                for (int s = 0; s < S; ++s)
-#pragma unroll 1
-                    for (int t = 0; s + t < S; ++t)
-                        tc_mma(tmem + (uint32_t)((s + t) * TN), tc_sdesc(sa + s * SH::A_PLANE, 128, 256),
-                               tc_sdesc(sbb + t * SH::B_PLANE, 128, 256), IDESC, (first && s == 0) ? 0u : 1u);
-                tc_commit(buf ? bar1 : bar0);
-            }
-            ncommit[buf]++;
-            if ((kk + 1) % SH::CHUNK_STEPS == 0 || kk + 1 == nk) {
-                const bool ok = stuck_test ? mbar_wait_bounded(bar_stuck, 0, wait_limit)
-                                           : mbar_wait_bounded(buf ? bar1 : bar0, (ncommit[buf] - 1) & 1, wait_limit);
-                if (__syncthreads_or(!ok)) { fail = true; break; }
-                tc_fence_after();
-#pragma unroll
-                for (int d = 0; d < S; ++d)
-#pragma unroll
-                    for (int c0 = 0; c0 < TN; c0 += 32) {
-                        uint32_t r[32];
-                        tc_ld32(tmem_warp + (uint32_t)(d * TN + c0), r);
-#pragma unroll
-                        for (int j = 0; j < 32; ++j)
-                            // |acc| < 2^24: the 32-bit conversion is exact
-                            tot[c0 + j] += (long long)__float2int_rn(__uint_as_float(r[j])) << (7 * (S - 1 - d));
-                    }
-                tc_fence_before();
-                __syncthreads();  // every warp has read TMEM before the next MMAs overwrite it
-            }
-        }
-        if (fail) break;
-#pragma unroll
-        for (int j = 0; j < TN; ++j) {
-            const double v = scaled_i64(tot[j], erow + ecol[j] - 7 * S - 7);
-            outs[j * SH::TM + tid] = (p == it.p0) ? v : outs[j * SH::TM + tid] + v;
-        }
-    }
-    if (fail) {
-        if (tid == 0) atomicExch(status, 1);
-        cp_async_wait<0>();
-        // the MMAs in flight finish before TMEM is released (bounded again)
-        if (ncommit[0] > 0) mbar_wait_bounded(bar0, (ncommit[0] - 1) & 1, wait_limit);
-        if (ncommit[1] > 0) mbar_wait_bounded(bar1, (ncommit[1] - 1) & 1, wait_limit);
-    } else if (row < Mrows) {
-#pragma unroll
-        for (int j = 0; j < TN; ++j) {
-            const int col = it.c0 + j;
-            if (col < Ncols) {
-                const int m = it.swap ? col : row, n = it.swap ? row : col;
-                C[cb.coff + tab_at(tab, cb.tcm, m) + tab_at(tab, cb.tcn, n)] = outs[j * SH::TM + tid];
-            }
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(SH::TMEM_COLS));
-}
+#include "ozaki_tc.cuh"
 
 namespace {
 // Resident CTAs per SM of a variant (queried once per process).
@@ -641,12 +393,13 @@ void launch_tc(Ctx& ctx, Plan const& p, double* C, __nv_bfloat16 const* panels, 
         return true;
     }();
     (void)attr;
-    // ITG_TC_TEST_STUCK_WAIT: every tile's first fold waits on a barrier nothing
+    // ITG_TC_TEST_STUCK_WAIT: the epilogue's first wait is on a barrier nothing
     // arrives at, so the bounded wait runs out (tests of the ERR_TIMEOUT path)
     static const int stuck = std::getenv("ITG_TC_TEST_STUCK_WAIT") ? 1 : 0;
-    gemm_ozaki_tc_kernel<S, TC_TILE_N><<<p.nitems_tc, 128, SH::SMEM, ctx.stream>>>(
-        p.d_items_tc, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C, ctx.err_dev, tc_wait_limit(),
-        stuck);
+    const int grid = std::min(p.nitems_tc, ctx.sm_count);  // persistent: one CTA per SM
+    gemm_ozaki_tc_kernel<S, TC_TILE_N><<<grid, SH::THREADS, SH::SMEM, ctx.stream>>>(
+        p.d_items_tc, p.nitems_tc, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C, ctx.err_dev,
+        tc_wait_limit(), stuck);
 }
 
 template <int S>

@@ -53,6 +53,28 @@ def test_heff_benchmark_size_matches_the_oracle(ctx):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
+def test_prepared_apply_matches_the_plain_call(ctx, prec):
+    """The prepared, graph-replayed apply the benchmark times (itg_heff_create /
+    itg_heff_run: the two MPO tensors contracted with each other once, one MPO
+    step per apply) against itg_heff_apply (the reference's four-step chain),
+    on the benchmark's bytes: same structure, values within the tolerance."""
+    import torch
+    from itensor_gb300 import workloads
+    wl = workloads.heff_workload(1024, 15, 6.0, 20241204)
+    dev = {k: workloads.to_device(ctx, wl[k]) for k in ("psi", "L", "W1", "W2", "R")}
+    args = (dev["L"], dev["W1"], dev["W2"], dev["R"], dev["psi"])
+    ref = ctx.heff_apply(*args, precision=0).numpy()
+    for graph in (False, True):
+        h = ctx.heff_prepare(*args, precision=prec, use_graph=graph)
+        assert h.out_size == ref.size
+        out = torch.empty(h.out_size, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            h.run(dev["psi"].device_ptr(), out.data_ptr())
+        ctx.sync()
+        assert _relerr(out.cpu().numpy(), ref) <= (1e-12 if prec == 0 else 1e-11), graph
+
+
+@pytest.mark.parametrize("prec", [0, 1])
 def test_heff_benchmark_layout_matches_the_reference(ctx, golden, prec):
     d = golden("heff_config")
     names = qn_names(d)
