@@ -69,8 +69,9 @@ int itg_synchronize(itg_ctx* ctx);
 int itg_set_precision(itg_ctx* ctx, int mode, int ozaki_slices);
 /* Tile shape of the split-precision block GEMM: -1 (default) lets the
  * autotuner time every variant on a plan's first large use and keep the
- * fastest; 0..3 forces 32x32 tiles, 64x32 tiles, persistent 32x32, persistent
- * 64x32. All variants give bit-identical results. */
+ * fastest; 0..3 forces the mma.sync kernel with 32x32 tiles, 64x32 tiles,
+ * persistent 32x32, persistent 64x32; 4 the tcgen05 kernel (128 x 32 tiles,
+ * TMEM accumulators). All variants give bit-identical results. */
 int itg_set_gemm_variant(itg_ctx* ctx, int variant);
 int itg_stats(itg_ctx* ctx, uint64_t* kernel_launches, double* gemm_flops, uint64_t* plans_built,
               uint64_t* plan_hits);

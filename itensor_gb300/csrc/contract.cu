@@ -1076,17 +1076,27 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             std::stable_sort(o64.begin(), o64.end(), [&](int x, int y) { return cost64[x] > cost64[y]; });
             for (int i : o64) items64.push_back(raw[i]);
         }
-        // tensor-core tiles: 128 rows along each block's longer side, TC_TILE_N columns along the other
-        std::vector<TcItem> items_tc;
+        // tensor-core tiles: 128 rows along each block's longer side, TC_TILE_N columns along the
+        // other; the pairs seen from each block's rows and columns
+        std::vector<TcTile> items_tc;
+        std::vector<TcPair> pairs_tc;
         if (!plan->skinny) {
-            std::vector<TcItem> raw;
+            std::vector<TcTile> raw;
             std::vector<double> ctc;
+            pairs_tc.resize(pairs.size());
             for (int c = 0; c < ncb; ++c) {
                 const int swap = cblk[c].N > cblk[c].M ? 1 : 0;
                 const int R = swap ? cblk[c].N : cblk[c].M, W = swap ? cblk[c].M : cblk[c].N;
+                for (int q = cp0[c]; q < cp1[c]; ++q) {
+                    OpBlockRec const& orow = ops[swap ? pairs[q].ib : pairs[q].ia];
+                    OpBlockRec const& ocol = ops[swap ? pairs[q].ia : pairs[q].ib];
+                    pairs_tc[q] = TcPair{orow.panel, ocol.panel, orow.exp, ocol.exp, panel_row_groups(orow.rows),
+                                         panel_row_groups(ocol.rows), orow.Kp / 16, 0};
+                }
                 for (int r0 = 0; r0 < R; r0 += TC_TILE_M)
                     for (int c0 = 0; c0 < W; c0 += TC_TILE_N) {
-                        raw.push_back(TcItem{c, r0, c0, cp0[c], cp1[c], swap});
+                        raw.push_back(TcTile{cblk[c].coff, swap ? cblk[c].tcn : cblk[c].tcm,
+                                             swap ? cblk[c].tcm : cblk[c].tcn, R, W, r0, c0, cp0[c], cp1[c], swap, 0});
                         ctc.push_back(cK[c] + 1.0);
                     }
             }
@@ -1102,13 +1112,15 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         size_t t_prep = align16(t_ops + sizeof(OpBlockRec) * ops.size());
         size_t t_i64 = align16(t_prep + sizeof(PrepItem) * prep.size());
         size_t t_itc = align16(t_i64 + sizeof(ItemRec) * items64.size());
-        size_t t_tab = align16(t_itc + sizeof(TcItem) * items_tc.size());
+        size_t t_ptc = align16(t_itc + sizeof(TcTile) * items_tc.size());
+        size_t t_tab = align16(t_ptc + sizeof(TcPair) * pairs_tc.size());
         size_t tbytes = align16(t_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size()));
         ctx.ensure_stage(tbytes);
         st = static_cast<char*>(ctx.stage);
         if (!sitems.empty()) std::memcpy(st + t_items, sitems.data(), sizeof(ItemRec) * sitems.size());
         if (!items64.empty()) std::memcpy(st + t_i64, items64.data(), sizeof(ItemRec) * items64.size());
-        if (!items_tc.empty()) std::memcpy(st + t_itc, items_tc.data(), sizeof(TcItem) * items_tc.size());
+        if (!items_tc.empty()) std::memcpy(st + t_itc, items_tc.data(), sizeof(TcTile) * items_tc.size());
+        if (!pairs_tc.empty()) std::memcpy(st + t_ptc, pairs_tc.data(), sizeof(TcPair) * pairs_tc.size());
         if (!pairs.empty()) std::memcpy(st + t_pairs, pairs.data(), sizeof(PairRec) * pairs.size());
         if (!cblk.empty()) std::memcpy(st + t_cblk, cblk.data(), sizeof(CBlockRec) * cblk.size());
         if (!ops.empty()) std::memcpy(st + t_ops, ops.data(), sizeof(OpBlockRec) * ops.size());
@@ -1134,7 +1146,8 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->d_tab = reinterpret_cast<int32_t*>(db + t_tab);
         plan->d_items64 = reinterpret_cast<ItemRec*>(db + t_i64);
         plan->nitems64 = (int)items64.size();
-        plan->d_items_tc = reinterpret_cast<TcItem*>(db + t_itc);
+        plan->d_items_tc = reinterpret_cast<TcTile*>(db + t_itc);
+        plan->d_pairs_tc = reinterpret_cast<TcPair*>(db + t_ptc);
         plan->nitems_tc = (int)items_tc.size();
         plan->nitems = (int)sitems.size();
         plan->npairs = np;

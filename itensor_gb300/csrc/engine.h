@@ -65,9 +65,23 @@ struct ItemRec {          // one output tile (TILE x TILE) of one output block
 };
 // One output tile of the tensor-core (tcgen05) split-precision kernel: 128
 // rows along the block's longer side (swap = 0: C's m, A's rows; swap = 1: C's
-// n, B's rows) times TC_TILE_N columns along the other side.
-struct TcItem {
-    int32_t c, r0, c0, p0, p1, swap;
+// n, B's rows) times TC_TILE_N columns along the other side. Everything a tile
+// needs is in the record (no chain of dependent loads per tile).
+struct TcTile {
+    int64_t coff;          // C block offset
+    int32_t rtab, ctab;    // table positions of C's offsets along the tile's rows and columns
+    int32_t rows, cols;    // the block's extent along the tile's rows and columns
+    int32_t r0, c0;        // first row and column of the tile
+    int32_t p0, p1;        // the block's pairs in the tensor-core pair list
+    int32_t swap, pad;
+};
+// A block pair seen from the tile's rows and columns: the digit panels and
+// row exponents of the row-side and column-side operand blocks.
+struct TcPair {
+    int64_t rpanel, cpanel;  // panel offsets (elements) of both blocks
+    int32_t rexp, cexp;      // their row exponents' offsets
+    int32_t nrg_r, nrg_c;    // their row groups of 8
+    int32_t nk, pad;         // k-steps of 16
 };
 constexpr int TC_TILE_M = 128;
 constexpr int TC_TILE_N = 32;
@@ -119,8 +133,9 @@ struct Plan {
     // 64-row tiles of the same output blocks (the 64 x 32 split-precision variant)
     ItemRec* d_items64 = nullptr;
     int nitems64 = 0;
-    // 128 x TC_TILE_N tiles of the tensor-core (tcgen05) variant
-    TcItem* d_items_tc = nullptr;
+    // 128 x TC_TILE_N tiles of the tensor-core (tcgen05) variant and its view of the pairs
+    TcTile* d_items_tc = nullptr;
+    TcPair* d_pairs_tc = nullptr;
     int nitems_tc = 0;
     // split-precision GEMM variant picked by the autotuner (-1: not tuned, run variant 0)
     mutable std::atomic<int> oz_variant{-1};

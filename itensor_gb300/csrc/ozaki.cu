@@ -21,12 +21,13 @@
 // folding are integer work: FP64 issue slots on this part are ~1/60 of FP32.
 //
 // prep: one CTA per item of whole rows (~2048 elements), one warp per row,
-//       writes the row exponents and the S digit planes, k-contiguous, K
-//       padded to 16.
-// gemm: output tiles of 32 x 32 (4 warps of 16 x 16) or 64 x 32 (8 warps),
-//       one CTA per tile or persistent CTAs over the tile list; the variant
-//       is chosen per plan by autotune_ozaki. Digit panels are staged with
-//       cp.async into a two-stage shared-memory ring and read with ldmatrix.
+//       writes the row exponents and the S digit planes, tiled (see
+//       OpBlockRec in engine.h), K padded to 16.
+// gemm: mma.sync variants: output tiles of 32 x 32 (4 warps of 16 x 16) or
+//       64 x 32 (8 warps), one CTA per tile or persistent CTAs over the tile
+//       list; digit panels staged with cp.async into a two-stage shared-memory
+//       ring and read with ldmatrix. tcgen05 variant: ozaki_tc.cuh. The
+//       variant is chosen per plan by autotune_ozaki.
 #include "engine.h"
 #include <cuda_bf16.h>
 #include <algorithm>
@@ -398,8 +399,8 @@ void launch_tc(Ctx& ctx, Plan const& p, double* C, __nv_bfloat16 const* panels, 
     static const int stuck = std::getenv("ITG_TC_TEST_STUCK_WAIT") ? 1 : 0;
     const int grid = std::min(p.nitems_tc, ctx.sm_count);  // persistent: one CTA per SM
     gemm_ozaki_tc_kernel<S, TC_TILE_N><<<grid, SH::THREADS, SH::SMEM, ctx.stream>>>(
-        p.d_items_tc, p.nitems_tc, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C, ctx.err_dev,
-        tc_wait_limit(), stuck);
+        p.d_items_tc, p.nitems_tc, p.d_pairs_tc, p.d_tab, panels, plane, exps, C, ctx.err_dev, tc_wait_limit(),
+        stuck);
 }
 
 template <int S>
@@ -463,7 +464,7 @@ int autotune_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, do
         }
     };
     prep();
-    constexpr int NV = 4, REPS = 3;
+    constexpr int NV = 5, REPS = 3;  // 4: the tensor-core (tcgen05) kernel
     cudaEvent_t ev[NV][2];
     for (int v = 0; v < NV; ++v)
         for (int k = 0; k < 2; ++k) ITG_CHECK_CUDA(cudaEventCreate(&ev[v][k]));

@@ -124,13 +124,14 @@ struct TcShape {
     static constexpr uint32_t TMEM_COLS = (2 * ACC <= 128) ? 128 : (2 * ACC <= 256 ? 256 : 512);
     static constexpr int LDO = TN + 1;            // row stride of the FP64 partial results (doubles)
     static constexpr int OUT = 8 * TM * LDO;      // FP64 partial results, [row][column]
-    // full[NST], empty[NST], tfull[2], tempty[2], drain, stuck; TMEM address; abort flag
+    // full[NST], empty[NST], tfull[2], tempty[2], drain, stuck; TMEM address, abort, flags
     static constexpr int BAR_OFF = NST * STAGE + OUT;
     static constexpr int NBAR = 2 * NST + 6;
     static constexpr int MISC_OFF = BAR_OFF + 8 * NBAR;
-    static constexpr int ECOL_OFF = MISC_OFF + 16;
-    static constexpr int CCOL_OFF = ECOL_OFF + 4 * TN;
-    static constexpr size_t SMEM = (size_t)CCOL_OFF + 4 * TN;
+    static constexpr int ECOL_OFF = MISC_OFF + 16;          // column exponents of the pair
+    static constexpr int COFF_OFF = ECOL_OFF + 4 * TN;      // C offsets along the tile's columns
+    static constexpr int ROFF_OFF = COFF_OFF + 4 * TN;      // C offsets along the tile's rows
+    static constexpr size_t SMEM = (size_t)ROFF_OFF + 4 * TM;
     static constexpr int EPI_WARPS = 8;           // two warpgroups, each half of the columns
     static constexpr int PRODUCER = 8, ISSUER = 9;   // warp numbers
     static constexpr int THREADS = 320;
@@ -138,13 +139,13 @@ struct TcShape {
 
 template <int S, int TN>
 __global__ void __launch_bounds__(320, 1)
-gemm_ozaki_tc_kernel(const TcItem* __restrict__ items, int nitems, const PairRec* __restrict__ pairs,
-                     const CBlockRec* __restrict__ cblk, const OpBlockRec* __restrict__ ops,
+gemm_ozaki_tc_kernel(const TcTile* __restrict__ tiles, int ntiles, const TcPair* __restrict__ tpairs,
                      const int32_t* __restrict__ tab, const __nv_bfloat16* __restrict__ panels, int64_t plane,
                      const int32_t* __restrict__ exps, double* __restrict__ C, int* __restrict__ status,
                      long long wait_limit, int stuck_test) {
     using SH = TcShape<S, TN>;
     static_assert(2 * S * TN <= 512, "two accumulator sets must fit in TMEM");
+    static_assert(TN % 32 == 0, "the column-wise store gives each lane one column per 32");
     static_assert((long long)SH::KCHUNK * S * 128 * 128 <= (1LL << 24), "digit sums must stay exact in FP32");
     extern __shared__ __align__(128) unsigned char tc_smem[];
     const uint32_t sbase = smem_u32(tc_smem);
@@ -160,7 +161,8 @@ gemm_ozaki_tc_kernel(const TcItem* __restrict__ items, int nitems, const PairRec
     volatile int* abort = reinterpret_cast<volatile int*>(tc_smem + SH::MISC_OFF + 4);
     volatile int* epi_ok = reinterpret_cast<volatile int*>(tc_smem + SH::MISC_OFF + 8);
     int* ecol = reinterpret_cast<int*>(tc_smem + SH::ECOL_OFF);
-    int* ccol = reinterpret_cast<int*>(tc_smem + SH::CCOL_OFF);
+    int* coff = reinterpret_cast<int*>(tc_smem + SH::COFF_OFF);
+    int* roff = reinterpret_cast<int*>(tc_smem + SH::ROFF_OFF);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         for (int i = 0; i < SH::NST; ++i) {
@@ -195,21 +197,17 @@ gemm_ozaki_tc_kernel(const TcItem* __restrict__ items, int nitems, const PairRec
             int stage = 0;
             uint32_t phase = 0;
             uint32_t filled[SH::NST] = {};
-            for (int ti = blockIdx.x; ti < nitems && !*abort; ti += gridDim.x) {
-                const TcItem it = items[ti];
-                const int rg0 = it.r0 >> 3, cg0 = it.c0 >> 3;
-                for (int p = it.p0; p < it.p1 && !*abort; ++p) {
-                    const PairRec pr = pairs[p];
-                    const OpBlockRec orow = ops[it.swap ? pr.ib : pr.ia];
-                    const OpBlockRec ocol = ops[it.swap ? pr.ia : pr.ib];
-                    const int nrg_r = panel_row_groups(orow.rows), nrg_c = panel_row_groups(ocol.rows);
-                    const int nk = orow.Kp / SH::KS;
-                    for (int ks = 0; ks < nk; ++ks) {
+            for (int ti = blockIdx.x; ti < ntiles && !*abort; ti += gridDim.x) {
+                const TcTile T = tiles[ti];
+                const int rg0 = T.r0 >> 3, cg0 = T.c0 >> 3;
+                for (int p = T.p0; p < T.p1 && !*abort; ++p) {
+                    const TcPair P = tpairs[p];
+                    for (int ks = 0; ks < P.nk; ++ks) {
                         if (!mbar_wait_bounded(empty(stage), phase ^ 1u, wait_limit, abort)) { fail(); break; }
                         mbar_expect_tx(full(stage), SH::STAGE);
                         const uint32_t dst = sbase + stage * SH::STAGE;
-                        const __nv_bfloat16* a0 = panels + orow.panel + ((int64_t)ks * nrg_r + rg0) * 128;
-                        const __nv_bfloat16* b0 = panels + ocol.panel + ((int64_t)ks * nrg_c + cg0) * 128;
+                        const __nv_bfloat16* a0 = panels + P.rpanel + ((int64_t)ks * P.nrg_r + rg0) * 128;
+                        const __nv_bfloat16* b0 = panels + P.cpanel + ((int64_t)ks * P.nrg_c + cg0) * 128;
 #pragma unroll 1
                         for (int s = 0; s < S; ++s) {
                             bulk_g2s(dst + s * SH::A_PLANE, a0 + s * plane, SH::A_PLANE, full(stage));
@@ -235,10 +233,10 @@ gemm_ozaki_tc_kernel(const TcItem* __restrict__ items, int nitems, const PairRec
             int stage = 0;
             uint32_t phase = 0, unit = 0;
             bool issued = false;
-            for (int ti = blockIdx.x; ti < nitems && !*abort; ti += gridDim.x) {
-                const TcItem it = items[ti];
-                for (int p = it.p0; p < it.p1 && !*abort; ++p) {
-                    const int nk = ops[it.swap ? pairs[p].ib : pairs[p].ia].Kp / SH::KS;
+            for (int ti = blockIdx.x; ti < ntiles && !*abort; ti += gridDim.x) {
+                const TcTile T = tiles[ti];
+                for (int p = T.p0; p < T.p1 && !*abort; ++p) {
+                    const int nk = tpairs[p].nk;
                     bool ok = true;
                     for (int ks = 0; ks < nk && ok; ++ks) {
                         const uint32_t b = unit & 1u;
@@ -284,26 +282,22 @@ gemm_ozaki_tc_kernel(const TcItem* __restrict__ items, int nitems, const PairRec
         const uint32_t tmem_warp = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(g * HALF);
         uint32_t unit = 0;
         bool live = true;
-        for (int ti = blockIdx.x; ti < nitems && live; ti += gridDim.x) {
-            const TcItem it = items[ti];
-            const CBlockRec cb = cblk[it.c];
-            const int Mrows = it.swap ? cb.N : cb.M, Ncols = it.swap ? cb.M : cb.N;
-            const int row = it.r0 + trow;
-            const bool row_ok = row < Mrows;
-            epi_sync();  // the previous tile's readers of ccol / ecol / outs are done
-            if (tid < TN) {
-                const int col = it.c0 + tid;
-                ccol[tid] = col < Ncols ? tab_at(tab, it.swap ? cb.tcm : cb.tcn, col) : 0;
-            }
-            for (int p = it.p0; p < it.p1 && live; ++p) {
-                const PairRec pr = pairs[p];
-                const OpBlockRec orow = ops[it.swap ? pr.ib : pr.ia];
-                const OpBlockRec ocol = ops[it.swap ? pr.ia : pr.ib];
-                const int nk = orow.Kp / SH::KS;
-                const int nchunks = (nk + SH::CHUNK_STEPS - 1) / SH::CHUNK_STEPS;
-                const int erow = row_ok ? exps[orow.exp + row] : 0;
-                if (p > it.p0) epi_sync();  // the previous pair's readers of ecol are done
-                if (tid < TN) ecol[tid] = (it.c0 + tid < Ncols) ? exps[ocol.exp + it.c0 + tid] : 0;
+        TcTile T = blockIdx.x < ntiles ? tiles[blockIdx.x] : TcTile{};
+        for (int ti = blockIdx.x; ti < ntiles && live; ti += gridDim.x) {
+            const TcTile cur = T;
+            if (ti + (int)gridDim.x < ntiles) T = tiles[ti + gridDim.x];  // the next tile's record, early
+            const int row = cur.r0 + trow;
+            const bool row_ok = row < cur.rows;
+            epi_sync();  // the previous tile's readers of coff / roff / ecol / outs are done
+            // C offsets along the tile's rows and columns, while the MMAs run
+            if (g == 0) roff[trow] = row_ok ? tab_at(tab, cur.rtab, row) : 0;
+            else if (trow < TN) coff[trow] = (cur.c0 + trow < cur.cols) ? tab_at(tab, cur.ctab, cur.c0 + trow) : 0;
+            for (int p = cur.p0; p < cur.p1 && live; ++p) {
+                const TcPair P = tpairs[p];
+                const int nchunks = (P.nk + SH::CHUNK_STEPS - 1) / SH::CHUNK_STEPS;
+                const int erow = row_ok ? exps[P.rexp + row] : 0;
+                if (p > cur.p0) epi_sync();  // the previous pair's readers of ecol are done
+                if (tid < TN) ecol[tid] = (cur.c0 + tid < cur.cols) ? exps[P.cexp + cur.c0 + tid] : 0;
                 long long tot[HALF];
 #pragma unroll
                 for (int j = 0; j < HALF; ++j) tot[j] = 0;
@@ -344,27 +338,28 @@ gemm_ozaki_tc_kernel(const TcItem* __restrict__ items, int nitems, const PairRec
                     const int jj = g * HALF + j;
                     const double v = scaled_i64(tot[j], erow + ecol[jj] - 7 * S - 7);
                     double* o = outs + trow * SH::LDO + jj;
-                    *o = (p == it.p0) ? v : *o + v;
+                    *o = (p == cur.p0) ? v : *o + v;
                 }
             }
             if (!live) break;
-            epi_sync();  // every row's results are in outs
-            if (!it.swap) {
+            epi_sync();  // every row's results and the offsets are in shared memory
+            if (!cur.swap) {
                 // tile rows run along C's first (fastest) output index: thread = row
                 if (row_ok) {
-                    const int64_t base = cb.coff + tab_at(tab, cb.tcm, row);
+                    double* base = C + cur.coff + roff[trow];
 #pragma unroll 4
                     for (int j = 0; j < HALF; ++j) {
                         const int jj = g * HALF + j;
-                        if (it.c0 + jj < Ncols) C[base + ccol[jj]] = outs[trow * SH::LDO + jj];
+                        if (cur.c0 + jj < cur.cols) base[coff[jj]] = outs[trow * SH::LDO + jj];
                     }
                 }
             } else {
                 // tile columns run along C's fastest index: lane = column, one warp per row
-                for (int rr = warp; rr < SH::TM && it.r0 + rr < Mrows; rr += SH::EPI_WARPS) {
-                    const int64_t base = cb.coff + tab_at(tab, cb.tcn, it.r0 + rr);
+                for (int rr = warp; rr < SH::TM && cur.r0 + rr < cur.rows; rr += SH::EPI_WARPS) {
+                    double* base = C + cur.coff + roff[rr];
+#pragma unroll
                     for (int c = lane; c < TN; c += 32)
-                        if (it.c0 + c < Ncols) C[base + ccol[c]] = outs[rr * SH::LDO + c];
+                        if (cur.c0 + c < cur.cols) base[coff[c]] = outs[rr * SH::LDO + c];
                 }
             }
         }
