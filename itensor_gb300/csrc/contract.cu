@@ -356,6 +356,11 @@ __device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& 
     int mrow[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) mrow[j] = it.m0 + threadIdx.x + j * SKINNY_THREADS;
+    // row sets whose whole warp lies past the block's end skip their FMAs (a
+    // warp-uniform branch: FP64 issue slots bound this kernel)
+    bool wlive[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) wlive[j] = it.m0 + (int)(threadIdx.x & ~31u) + j * SKINNY_THREADS < cb.M;
     for (int p = it.p0; p < it.p1; ++p) {
         const PairRec pr = pairs[p];
         int arow[R];
@@ -379,7 +384,8 @@ __device__ __forceinline__ void skinny_item(ItemRec const& it, CBlockRec const& 
                     const double b = Bs[k][n];
                     if (nonzero_bits(b)) {
 #pragma unroll
-                        for (int j = 0; j < R; ++j) acc[j][n] = fma(a[j], b, acc[j][n]);
+                        for (int j = 0; j < R; ++j)
+                            if (wlive[j]) acc[j][n] = fma(a[j], b, acc[j][n]);
                     }
                 }
             }
@@ -412,6 +418,11 @@ __device__ __forceinline__ void skinny_item_direct(ItemRec const& it, CBlockRec 
     int mrow[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) mrow[j] = it.m0 + threadIdx.x + j * SKINNY_THREADS;
+    // row sets whose whole warp lies past the block's end skip their FMAs (a
+    // warp-uniform branch: FP64 issue slots bound this kernel)
+    bool wlive[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) wlive[j] = it.m0 + (int)(threadIdx.x & ~31u) + j * SKINNY_THREADS < cb.M;
     int bcol[NN];
     for (int p = it.p0; p < it.p1; ++p) {
         const PairRec pr = pairs[p];
@@ -431,7 +442,8 @@ __device__ __forceinline__ void skinny_item_direct(ItemRec const& it, CBlockRec 
                 const double b = __ldg(B + bk + bcol[n]);
                 if (nonzero_bits(b)) {
 #pragma unroll
-                    for (int j = 0; j < R; ++j) acc[j][n] = fma(a[j], b, acc[j][n]);
+                    for (int j = 0; j < R; ++j)
+                            if (wlive[j]) acc[j][n] = fma(a[j], b, acc[j][n]);
                 }
             }
         }
@@ -1008,24 +1020,13 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         for (int bb = 0; bb < nB; ++bb)
             if (tbkB[bb] >= 0) ib_of[bb] = add_op(B.offs[bb], rows_of(B, bb, mt.b_unc), rows_of(B, bb, mt.b_con), tbnB[bb], tbkB[bb]);
         const int nopsB = (int)ops.size() - nopsA;
-        // prep items of whole rows (exponents complete per row). Short rows: one
-        // warp each, the item size chosen so that the items fill the GPU about 16
-        // times over (8 to 128 rows: small operands keep every row in flight,
-        // large ones do not pay for hundreds of thousands of tiny CTAs); long
-        // rows: ~2048 entries per item.
+        // prep items: one row group of the tiled panel (8 rows, whole rows so the
+        // row exponents are complete) each, one warp per item; A's items first
         std::vector<PrepItem> prep;
-        int64_t short_rows = 0;
-        for (auto const& o : ops)
-            if (o.Kp <= 32 * OZ_PREP_REGS) short_rows += o.rows;
-        int short_chunk = (int)std::min<int64_t>(128, std::max<int64_t>(OZ_PREP_ITEM_ROWS,
-                                                                       short_rows / (16 * (int64_t)ctx.sm_count)));
-        short_chunk = (short_chunk + 7) / 8 * 8;
         for (int o = 0; o < (int)ops.size(); ++o) {
-            const int rows = ops[o].rows, Kp = std::max(ops[o].Kp, 1);
-            const int chunk = Kp <= 32 * OZ_PREP_REGS ? short_chunk
-                                                      : std::max(1, std::min(OZ_PREP_LONG_ROWS, 2048 / Kp));
-            for (int r0 = 0; r0 < rows; r0 += chunk)
-                prep.push_back(PrepItem{o, r0, std::min(rows, r0 + chunk), o < nopsA ? 0 : 1});
+            const int rows = ops[o].rows;
+            for (int r0 = 0; r0 < rows; r0 += 8)
+                prep.push_back(PrepItem{o, r0, std::min(rows, r0 + 8), o < nopsA ? 0 : 1});
         }
         {
             int q = 0;

@@ -102,9 +102,6 @@ __device__ __forceinline__ int32_t tab_at(const int32_t* __restrict__ tab, int32
 #endif
 
 constexpr int GEMM_TILE = 32;
-constexpr int OZ_PREP_REGS = 8;        // split-precision prep: entries per lane of a short row
-constexpr int OZ_PREP_ITEM_ROWS = 8;   // rows per prep item of short rows, at least (one warp each)
-constexpr int OZ_PREP_LONG_ROWS = 256; // rows per prep item of long rows (at most)
 
 struct Plan {
     std::shared_ptr<Layout> C;       // output layout

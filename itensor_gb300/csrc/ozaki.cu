@@ -40,10 +40,10 @@ __device__ __forceinline__ int exp_field(double x) {
     return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
 }
 
-// The S balanced digits of x against the row exponent field emax, written to
-// dst[s * plane] (BF16-exact integers).
+// The S balanced digits of x against the row exponent field emax (BF16-exact
+// integers): d_1..d_{S-1} in [-64, 63], d_0 in [-128, 128].
 template <int S>
-__device__ __forceinline__ void oz_digits(double x, int emax, __nv_bfloat16* dst, int64_t plane) {
+__device__ __forceinline__ void oz_digit_vals(double x, int emax, int (&dig)[S]) {
     long long bits = __double_as_longlong(x);
     int ef = (int)((bits >> 52) & 0x7FF);
     unsigned long long Xf = 0;
@@ -55,11 +55,10 @@ __device__ __forceinline__ void oz_digits(double x, int emax, __nv_bfloat16* dst
         if (sh >= 0) Xf = mant << sh;
         else if (sh > -64) Xf = (mant >> (-sh)) + ((mant >> (-sh - 1)) & 1ull);
     }
-    // balanced digits: d_1..d_{S-1} in [-64, 63], d_0 in [-128, 128] (BF16-exact).
-    // Their signs are independent of the entry's sign, so the digit products
-    // left out (s + t >= S) average to zero instead of always shrinking |x y|.
+    // balanced digits: their signs are independent of the entry's sign, so the
+    // digit products left out (s + t >= S) average to zero instead of always
+    // shrinking |x y|
     long long X = bits < 0 ? -(long long)Xf : (long long)Xf;
-    int dig[S];
 #pragma unroll
     for (int s = S - 1; s >= 1; --s) {
         const long long d = ((X + 64) & 127) - 64;
@@ -67,72 +66,68 @@ __device__ __forceinline__ void oz_digits(double x, int emax, __nv_bfloat16* dst
         X = (X - d) >> 7;
     }
     dig[0] = (int)X;
-#pragma unroll
-    for (int s = 0; s < S; ++s) dst[s * plane] = __float2bfloat16_rn((float)dig[s]);
 }
 
-// Rows of up to 32 * OZ_PREP_REGS entries: one warp per row, the row read once
-// into registers, the exponent a warp max, the digits written k-contiguous
-// (items of OZ_PREP_ITEM_ROWS rows, all rows in flight at once). Longer rows:
-// items of a few rows whose rows x K entries are spread over the whole CTA.
+// One CTA (8 warps) per item of up to 8 rows: one row group of the tiled
+// panel, whole rows so that the row exponents are complete. First warp w
+// finds row w's exponent (lanes stride over k, then a shuffle max). Then the
+// warps share out the k-steps: per k-step of 16 the row group's 128 entries
+// of the tiled panel (two 8 x 8 core matrices) are one contiguous run per
+// digit plane; lane l computes entries 4l..4l+3 (row (l/2) mod 8, k = 8 (l/16)
+// + 4 (l mod 2) ..+3) and writes their digits as one 8-byte store per plane,
+// so a warp writes 256 contiguous bytes per plane. Rows past the block's end
+// get zero digits.
 template <int S>
-__global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restrict__ items, const OpBlockRec* __restrict__ ops,
+__global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restrict__ items, int nitems,
+                                                         const OpBlockRec* __restrict__ ops,
                                                          const int32_t* __restrict__ tab, const double* __restrict__ A,
                                                          const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
                                                          int64_t plane, int32_t* __restrict__ exps) {
+    __shared__ int rexp[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const PrepItem pi = items[blockIdx.x];
     const OpBlockRec ob = ops[pi.op];
     const double* __restrict__ base = (pi.which ? B : A) + ob.src;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (ob.Kp > 32 * OZ_PREP_REGS) {
-        // long rows: the item's rows x K entries spread over the CTA (a few rows per item)
-        __shared__ int rexp[OZ_PREP_LONG_ROWS];
-        __shared__ int32_t trow[OZ_PREP_LONG_ROWS];
-        const int rows = pi.r1 - pi.r0;
-        const int n = rows * ob.K;
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            rexp[r] = 0;
-            trow[r] = tab_at(tab, ob.trow, pi.r0 + r);
-        }
-        __syncthreads();
-        for (int e = threadIdx.x; e < n; e += blockDim.x) {
-            const int r = e % rows, k = e / rows;
-            atomicMax(&rexp[r], exp_field(base[trow[r] + tab_at(tab, ob.tcol, k)]));
-        }
-        __syncthreads();
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) exps[ob.exp + pi.r0 + r] = rexp[r] - 1022;
-        const int np = rows * ob.Kp, nrg = panel_row_groups(ob.rows);
-        __nv_bfloat16* pan = panels + ob.panel;
-        for (int e = threadIdx.x; e < np; e += blockDim.x) {
-            const int k = e % ob.Kp, r = e / ob.Kp;
-            oz_digits<S>(k < ob.K ? base[trow[r] + tab_at(tab, ob.tcol, k)] : 0.0, rexp[r],
-                         pan + panel_off(pi.r0 + r, k, nrg), plane);
-        }
-        return;
-    }
-    for (int r = pi.r0 + warp; r < pi.r1; r += nw) {
-        const int32_t ro = tab_at(tab, ob.trow, r);
-        double xr[OZ_PREP_REGS];
+    // row exponents: warp w takes row r0 + w
+    {
+        const int r = pi.r0 + warp;
         int emax = 0;
-#pragma unroll
-        for (int j = 0; j < OZ_PREP_REGS; ++j) {
-            const int k = lane + 32 * j;
-            xr[j] = k < ob.K ? base[ro + tab_at(tab, ob.tcol, k)] : 0.0;
-            emax = max(emax, exp_field(xr[j]));
+        if (r < pi.r1) {
+            const int32_t ro = tab_at(tab, ob.trow, r);
+            for (int k = lane; k < ob.K; k += 32) emax = max(emax, exp_field(base[ro + tab_at(tab, ob.tcol, k)]));
         }
-        for (int k = lane + 32 * OZ_PREP_REGS; k < ob.K; k += 32)
-            emax = max(emax, exp_field(base[ro + tab_at(tab, ob.tcol, k)]));
         emax = __reduce_max_sync(0xffffffffu, emax);
-        if (lane == 0) exps[ob.exp + r] = emax - 1022;  // |x| < 2^(E-1022)
-        __nv_bfloat16* pan = panels + ob.panel;
-        const int nrg = panel_row_groups(ob.rows);
-#pragma unroll
-        for (int j = 0; j < OZ_PREP_REGS; ++j) {
-            const int k = lane + 32 * j;
-            if (k < ob.Kp) oz_digits<S>(xr[j], emax, pan + panel_off(r, k, nrg), plane);
+        if (lane == 0) {
+            rexp[warp] = emax;
+            if (r < pi.r1) exps[ob.exp + r] = emax - 1022;  // |x| < 2^(E-1022)
         }
-        for (int k = lane + 32 * OZ_PREP_REGS; k < ob.Kp; k += 32)
-            oz_digits<S>(k < ob.K ? base[ro + tab_at(tab, ob.tcol, k)] : 0.0, emax, pan + panel_off(r, k, nrg), plane);
+    }
+    __syncthreads();
+    // digits, one 128-entry run per k-step and plane
+    const int row = (lane >> 1) & 7, kq = (lane >> 4) * 8 + (lane & 1) * 4;
+    const int er = rexp[row];
+    const int rr = pi.r0 + row;
+    const bool rrv = rr < pi.r1;
+    const int32_t ro = rrv ? tab_at(tab, ob.trow, rr) : 0;
+    const int nrg = panel_row_groups(ob.rows);
+    __nv_bfloat16* dst0 = panels + ob.panel + (int64_t)(pi.r0 >> 3) * 128 + lane * 4;
+    for (int ks = warp; ks < ob.Kp / 16; ks += 8) {
+        int dig[4][S];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int k = ks * 16 + kq + i;
+            oz_digit_vals<S>((rrv && k < ob.K) ? base[ro + tab_at(tab, ob.tcol, k)] : 0.0, er, dig[i]);
+        }
+        __nv_bfloat16* dst = dst0 + (int64_t)ks * nrg * 128;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            __nv_bfloat162 lo = __floats2bfloat162_rn((float)dig[0][s], (float)dig[1][s]);
+            __nv_bfloat162 hi = __floats2bfloat162_rn((float)dig[2][s], (float)dig[3][s]);
+            uint2 v;
+            v.x = *reinterpret_cast<uint32_t*>(&lo);
+            v.y = *reinterpret_cast<uint32_t*>(&hi);
+            *reinterpret_cast<uint2*>(dst + s * plane) = v;
+        }
     }
 }
 
@@ -421,7 +416,7 @@ void launch_s(Ctx& ctx, Plan const& p, double const* A, double const* B, double*
     // A items come first: without prep_b only A is sliced (B's panels are already in place)
     const int nprep = prep_b ? p.nprep : p.nprepA;
     if (nprep > 0)
-        ozaki_prep_kernel<S><<<nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
+        ozaki_prep_kernel<S><<<nprep, 256, 0, ctx.stream>>>(p.d_prep, nprep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
     launch_variant<S>(ctx, p, variant, C, panels, plane, exps);
 }
 }  // namespace
@@ -449,10 +444,10 @@ int autotune_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, do
     auto prep = [&] {
         if (p.nprep == 0) return;
         switch (S) {
-            case 3: ozaki_prep_kernel<3><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
-            case 4: ozaki_prep_kernel<4><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
-            case 5: ozaki_prep_kernel<5><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
-            default: ozaki_prep_kernel<6><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
+            case 3: ozaki_prep_kernel<3><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.nprep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
+            case 4: ozaki_prep_kernel<4><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.nprep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
+            case 5: ozaki_prep_kernel<5><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.nprep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
+            default: ozaki_prep_kernel<6><<<p.nprep, 256, 0, ctx.stream>>>(p.d_prep, p.nprep, p.d_ops, p.d_tab, A, B, panels, plane, exps); break;
         }
     };
     auto run = [&](int v) {
