@@ -568,6 +568,14 @@ bool& cache_bypass() {
     return bypass;
 }
 
+double split_min_flops() {
+    static const double v = [] {
+        const char* e = std::getenv("ITG_SPLIT_MIN_FLOPS");
+        return e ? std::max(0.0, std::atof(e)) : 1e7;
+    }();
+    return v;
+}
+
 Ctx::Ctx(int dev) : device(dev) {
     ITG_CHECK_CUDA(cudaSetDevice(dev));
     ITG_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));

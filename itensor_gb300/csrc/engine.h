@@ -282,8 +282,14 @@ constexpr int AUTOTUNE_MIN_USES = 32;
 // Whether exec_plan runs this plan with the split-precision kernels.
 // (The int64 digit sums of one block pair are exact up to K = 8192.)
 constexpr int SPLIT_MAX_PAIR_K = 8192;
+// Below this many algorithmic flops a contraction runs the FP64 kernel even in
+// the split precision: slicing both operands costs more than the FP64 GEMM it
+// would replace (measured crossover ~1e7 flops on GB300). ITG_SPLIT_MIN_FLOPS
+// overrides it (0: every eligible contraction takes the split kernels).
+double split_min_flops();
 inline bool plan_uses_split(Plan const& p, int prec) {
-    return !p.skinny && prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0 && p.max_pair_K <= SPLIT_MAX_PAIR_K;
+    return !p.skinny && prec == PREC_OZAKI_BF16 && p.avgK >= 8.0 && p.npairs > 0 && p.max_pair_K <= SPLIT_MAX_PAIR_K &&
+           p.flops >= split_min_flops();
 }
 // Bytes of split-precision scratch (digit planes + row exponents) a plan needs.
 // The tensor-core kernel copies whole 128-row (or TC_TILE_N-row) k-steps: the

@@ -4,6 +4,11 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# The split-precision kernels run every eligible contraction in the tests, the
+# small fixtures' too (the library's default sends contractions below 1e7
+# flops to the FP64 kernel, where slicing would not pay).
+os.environ.setdefault("ITG_SPLIT_MIN_FLOPS", "0")
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
