@@ -336,6 +336,16 @@ int itg_pool_submit(itg_pool* p, const itg_model_desc* model, const itg_sweep_de
 int itg_pool_submit_mpo(itg_pool* p, itg_ctx* ctx, int32_t nsites, const itg_tensor* const* W,
                         const itg_tensor* const* psi0, const itg_sweep_desc* sweeps, int32_t nsweeps, int precision,
                         double arrival_s, int keep_mps, int64_t* id);
+/* No counterpart in the reference (it has no batched mode; the nearest is the
+ * per-output-block loop of itensor/itdata/qutil.h:330-348). Cross-solve
+ * grouping, on by default, set before itg_pool_start: the split-precision
+ * contractions that a worker's solves reach while all of them wait run as one
+ * grouped prep launch and one grouped GEMM launch covering every solve's
+ * blocks, instead of one launch each. Results are identical either way.
+ * itg_pool_grouping_stats counts the grouped launches and the contractions
+ * they carried. */
+int itg_pool_set_grouping(itg_pool* p, int on);
+int itg_pool_grouping_stats(itg_pool* p, int64_t* grouped_launches, int64_t* grouped_contractions);
 int itg_pool_start(itg_pool* p);
 int itg_pool_drain(itg_pool* p);   /* waits until every submitted request has finished */
 /* status: -1 queued, -2 running, 0 done, else the request's error code (message in itg_pool_error).

@@ -132,6 +132,8 @@ SIGNATURES = {
                                       C.c_int, C.POINTER(C.c_int64)]),
     "itg_pool_estimate_mpo": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(SweepDesc), C.c_int32, C.c_int,
                                         _f64p]),
+    "itg_pool_set_grouping": (C.c_int, [C.c_void_p, C.c_int]),
+    "itg_pool_grouping_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "itg_pool_start": (C.c_int, [C.c_void_p]),
     "itg_pool_drain": (C.c_int, [C.c_void_p]),
     "itg_pool_record": (C.c_int, [C.c_void_p, C.c_int64, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _i32p]),
@@ -675,12 +677,19 @@ class Pool:
     """Solver pool (itg_pool_*): many ground-state solves on one GPU with
     continuous batching and admission by device-memory estimate."""
 
-    def __init__(self, device=0, workers=4, slots_per_worker=4, budget_bytes=None):
+    def __init__(self, device=0, workers=4, slots_per_worker=4, budget_bytes=None, grouping=True):
         if budget_bytes is None:
             budget_bytes = 64 << 30
         h = C.c_void_p()
         _check(lib().itg_pool_create(device, workers, slots_per_worker, float(budget_bytes), C.byref(h)))
         self.h = h
+        _check(lib().itg_pool_set_grouping(self.h, int(grouping)))
+
+    def grouping_stats(self):
+        """(grouped launches, contractions they carried)."""
+        a, b = C.c_int64(), C.c_int64()
+        _check(lib().itg_pool_grouping_stats(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def submit(self, model, sweeps, precision=0, arrival=0.0):
         md = _model_desc(model)

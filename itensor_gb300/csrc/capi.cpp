@@ -784,6 +784,22 @@ int itg_pool_submit_mpo(itg_pool* p, itg_ctx* c, int32_t nsites, const itg_tenso
     });
 }
 
+int itg_pool_set_grouping(itg_pool* p, int on) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p, "null pool");
+        p->pool.set_grouping(on != 0);
+    });
+}
+
+int itg_pool_grouping_stats(itg_pool* p, int64_t* grouped_launches, int64_t* grouped_contractions) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p, "null pool");
+        PoolStats s = p->pool.stats();
+        if (grouped_launches) *grouped_launches = s.grouped_launches;
+        if (grouped_contractions) *grouped_contractions = s.grouped_contractions;
+    });
+}
+
 int itg_pool_start(itg_pool* p) {
     return guard(nullptr, [&] { ITG_REQUIRE(p, "null pool"); p->pool.start(); });
 }

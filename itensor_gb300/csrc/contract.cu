@@ -261,18 +261,14 @@ __global__ void __launch_bounds__(1024) plan_kernel(PlanArgs a) {
 // One CTA per 32x32 output tile; 256 threads, 2x2 outputs each. Warps own
 // output columns, so warps whose columns lie outside a narrow block skip the
 // FMA loop entirely (FP64 issue slots are the bound on this part).
-__global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict__ items,
-                                                       const PairRec* __restrict__ pairs,
-                                                       const CBlockRec* __restrict__ cblk,
-                                                       const int32_t* __restrict__ tab,
-                                                       const double* __restrict__ A,
-                                                       const double* __restrict__ B,
-                                                       double* __restrict__ C) {
+__device__ __forceinline__ void f64_tile(ItemRec const& it, const PairRec* __restrict__ pairs,
+                                         const CBlockRec* __restrict__ cblk, const int32_t* __restrict__ tab,
+                                         const double* __restrict__ A, const double* __restrict__ B,
+                                         double* __restrict__ C) {
     constexpr int T = GEMM_TILE, TK = 16;
     __shared__ double As[TK][T + 1];
     __shared__ double Bs[TK][T + 1];
     __shared__ int32_t rowA[T], colB[T], kA[TK], kB[TK];   // this tile's offsets
-    const ItemRec it = items[blockIdx.x];
     const CBlockRec cb = cblk[it.c];
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;     // rows tx*2+{0,1}, cols ty*2+{0,1}
@@ -322,6 +318,35 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
 #pragma unroll
         for (int s = 0; s < 2; ++s)
             if (m + r < cb.M && n + s < cb.N) C[cb.coff + tab_at(tab, cb.tcm, m + r) + tab_at(tab, cb.tcn, n + s)] = accs[r][s];
+}
+
+__global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict__ items,
+                                                       const PairRec* __restrict__ pairs,
+                                                       const CBlockRec* __restrict__ cblk,
+                                                       const int32_t* __restrict__ tab,
+                                                       const double* __restrict__ A,
+                                                       const double* __restrict__ B,
+                                                       double* __restrict__ C) {
+    f64_tile(items[blockIdx.x], pairs, cblk, tab, A, B, C);
+}
+
+// FP64 contractions of several independent solves in one launch (the solver
+// pool's cross-solve grouping): a CTA finds its contraction by binary search
+// over the tile prefix positions and runs the lone launch's tile code.
+__global__ void __launch_bounds__(256) gemm_f64_group_kernel(const GroupRef* __restrict__ refs, int nrefs) {
+    int lo = 0, hi = nrefs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (refs[mid].tile_start <= (int)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const GroupRef& g = refs[lo];
+    f64_tile(g.items[blockIdx.x - g.tile_start], g.pairs, g.cblk, g.tab, g.A, g.B, g.C);
+}
+
+void launch_f64_group(cudaStream_t stream, GroupRef const* refs, int nrefs, int total_tiles) {
+    if (total_tiles > 0) gemm_f64_group_kernel<<<total_tiles, 256, 0, stream>>>(refs, nrefs);
+    ITG_CHECK_CUDA(cudaGetLastError());
 }
 
 // ------------------------------------------------------------------ skinny FP64 block GEMM
@@ -1238,10 +1263,19 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
         if (ctx.gemm_variant < 0 && p.oz_variant.load(std::memory_order_relaxed) < 0 && p.flops >= AUTOTUNE_MIN_FLOPS &&
             p.split_uses.fetch_add(1, std::memory_order_relaxed) + 1 >= AUTOTUNE_MIN_USES)
             autotune_ozaki(ctx, p, A, B, C, S, panels, exps);
-        launch_ozaki(ctx, p, A, B, C, S, panels, exps);
-        ctx.kernel_launches += 1;
+        // in a solver-pool fiber that groups launches: one launch with the other solves' contractions
+        if (ctx.profiling || !fiber_group_contract(ctx, p, A, B, C, S, panels, exps, true)) {
+            launch_ozaki(ctx, p, A, B, C, S, panels, exps);
+            ctx.kernel_launches += 1;
+        } else {
+            ctx.kernel_launches -= 1;  // flush() counted the group's two launches
+        }
     } else if (prec == PREC_F64 || prec == PREC_OZAKI_BF16) {
-        gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+        // in a solver-pool fiber that groups launches: one launch with the other solves' contractions
+        if (ctx.profiling || !fiber_group_contract(ctx, p, A, B, C, 0, nullptr, nullptr, false))
+            gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+        else
+            ctx.kernel_launches -= 1;  // flush() counted the group's launch
     } else {
         throw Error(ERR_ARG, "contract: unsupported precision mode");
     }

@@ -264,6 +264,36 @@ void exec_plan_noalloc(Ctx& ctx, Plan const& p, double const* A, double const* B
 // the plan's scratch (S digit planes of the padded panel size, row exponents).
 void launch_ozaki(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S, __nv_bfloat16* panels,
                   int32_t* exps, bool prep_b = true);
+// One split-precision contraction of a grouped launch (launch_ozaki_group):
+// its plan tables, operands, digit-panel scratch and output, and where its
+// prep items and output tiles start in the group's grids.
+struct GroupRef {
+    const PrepItem* prep;
+    const OpBlockRec* ops;
+    const int32_t* tab;
+    const ItemRec* items;
+    const PairRec* pairs;
+    const CBlockRec* cblk;
+    const double* A;
+    const double* B;
+    double* C;
+    __nv_bfloat16* panels;
+    int32_t* exps;
+    int64_t plane;
+    int32_t prep_start, tile_start;
+};
+// The same for FP64 contractions (gemm_f64_kernel tiles; contract.cu).
+void launch_f64_group(cudaStream_t stream, GroupRef const* refs, int nrefs, int total_tiles);
+// Prep and GEMM of every contraction in refs (device memory, prefix
+// positions filled in) as one launch each, on `stream` (ozaki.cu).
+void launch_ozaki_group(cudaStream_t stream, GroupRef const* refs, int nrefs, int total_prep, int total_tiles, int S);
+// Inside a solver-pool fiber whose scheduler groups launches: hands the
+// contraction (split precision with S slices, or FP64 tiles when S == 0) to
+// the thread's next grouped launch and yields until it is enqueued (the
+// context's stream then waits for it); returns false when grouping is off,
+// and the caller launches it alone (fiber.cpp).
+bool fiber_group_contract(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C, int S,
+                          __nv_bfloat16* panels, int32_t* exps, bool prep_b);
 // The tensor-core variant of the split-precision GEMM (ozaki_tc.cu): digit
 // panels staged into shared memory, tcgen05.mma with the diagonal sums in
 // tensor memory. Panels and exponents must be in place (the prep has run).

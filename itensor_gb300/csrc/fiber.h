@@ -24,10 +24,29 @@ struct Fiber {
     std::shared_ptr<BlockCache> cache;      // the solve's block cache
     std::shared_ptr<BlockCache> live_cache; // the thread's cache when the fiber last yielded
     bool live_bypass = false;               // the thread's cache bypass when the fiber last yielded
+    bool group_wait = false;                // handed a contraction to the next grouped launch
+    cudaEvent_t group_ready = nullptr;      // its inputs are ready on its stream
+    std::string group_error;                // set when the grouped launch failed
     Fiber();
     ~Fiber();
     Fiber(Fiber const&) = delete;
     Fiber& operator=(Fiber const&) = delete;
+};
+
+struct Ctx;
+struct Plan;
+// A split-precision contraction a fiber handed to the thread's next grouped launch.
+struct GroupRequest {
+    Fiber* fiber;
+    Ctx* ctx;
+    Plan const* plan;
+    double const* A;
+    double const* B;
+    double* C;
+    int S;
+    __nv_bfloat16* panels;
+    int32_t* exps;
+    bool prep_b;
 };
 
 // One per worker thread.
@@ -39,6 +58,27 @@ struct FiberScheduler {
     // Resumes f if its wait is over; returns true if it ran.
     bool poll(Fiber& f);
     static FiberScheduler*& of_thread();
+
+    // Cross-solve grouping: while `grouping` is on, the fibers' split-precision
+    // contractions wait in `pending` (each fiber yields) until the thread has
+    // nothing else to run; flush() then enqueues all of them as one grouped
+    // prep launch and one grouped GEMM launch on the thread's group stream,
+    // ordered after each contraction's inputs and before each stream's next work.
+    bool grouping = false;
+    std::vector<GroupRequest> pending;
+    void flush();
+    uint64_t grouped_launches = 0, grouped_contractions = 0;
+    ~FiberScheduler();
+
+private:
+    cudaStream_t gstream_ = nullptr;
+    cudaEvent_t gdone_ = nullptr;
+    void* ref_dev_ = nullptr;                // device GroupRef array
+    size_t ref_cap_ = 0;                     // its capacity (records)
+    static constexpr int NSTAGE = 4;         // pinned staging slots for the records
+    void* ref_host_[NSTAGE] = {};
+    cudaEvent_t ref_ev_[NSTAGE] = {};
+    int ref_slot_ = 0;
 };
 
 }  // namespace itg

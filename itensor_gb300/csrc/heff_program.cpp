@@ -141,12 +141,16 @@ void HeffProgram::launch_steps(Ctx& ctx) {
                 p.flops >= AUTOTUNE_MIN_FLOPS &&
                 (use_graph || p.split_uses.fetch_add(1, std::memory_order_relaxed) + 1 >= AUTOTUNE_MIN_USES))
                 autotune_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps);
-            launch_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps, !st.operand_sliced);
+            // in a solver-pool fiber that groups launches: one launch with the other solves' contractions
+            const bool grouped = !use_graph && !ctx.profiling &&
+                                 fiber_group_contract(ctx, p, a, st.operand.data(), c, slices, panels, exps,
+                                                   !st.operand_sliced);
+            if (!grouped) launch_ozaki(ctx, p, a, st.operand.data(), c, slices, panels, exps, !st.operand_sliced);
             if (ctx.profiling) {
                 ITG_CHECK_CUDA(cudaEventRecord(pr.stop, ctx.stream));
                 ctx.prof.push_back(pr);
             }
-            ctx.kernel_launches += (!st.operand_sliced || p.nprepA > 0) ? 2 : 1;
+            if (!grouped) ctx.kernel_launches += (!st.operand_sliced || p.nprepA > 0) ? 2 : 1;
             ctx.flops_done += p.flops;
             st.operand_sliced = true;
         } else {

@@ -78,14 +78,12 @@ __device__ __forceinline__ void oz_digit_vals(double x, int emax, int (&dig)[S])
 // so a warp writes 256 contiguous bytes per plane. Rows past the block's end
 // get zero digits.
 template <int S>
-__global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restrict__ items, int nitems,
-                                                         const OpBlockRec* __restrict__ ops,
-                                                         const int32_t* __restrict__ tab, const double* __restrict__ A,
-                                                         const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
-                                                         int64_t plane, int32_t* __restrict__ exps) {
+__device__ __forceinline__ void prep_item(PrepItem const& pi, const OpBlockRec* __restrict__ ops,
+                                          const int32_t* __restrict__ tab, const double* __restrict__ A,
+                                          const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
+                                          int64_t plane, int32_t* __restrict__ exps) {
     __shared__ int rexp[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const PrepItem pi = items[blockIdx.x];
     const OpBlockRec ob = ops[pi.op];
     const double* __restrict__ base = (pi.which ? B : A) + ob.src;
     // row exponents: warp w takes row r0 + w
@@ -129,6 +127,15 @@ __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restr
             *reinterpret_cast<uint2*>(dst + s * plane) = v;
         }
     }
+}
+
+template <int S>
+__global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restrict__ items, int nitems,
+                                                         const OpBlockRec* __restrict__ ops,
+                                                         const int32_t* __restrict__ tab, const double* __restrict__ A,
+                                                         const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
+                                                         int64_t plane, int32_t* __restrict__ exps) {
+    prep_item<S>(items[blockIdx.x], ops, tab, A, B, panels, plane, exps);
 }
 
 // v * 2^e as FP64, built with integer instructions (round to nearest, ties to
@@ -337,6 +344,57 @@ gemm_ozaki_kernel(const ItemRec* __restrict__ items, int nitems, const PairRec* 
     } else {
         oz_tile<S, WM>(items[blockIdx.x], pairs, cblk, ops, tab, panels, plane, exps, C, oz_smem);
     }
+}
+
+// ---------------------------------------------------------------- grouped launches
+// Split-precision contractions of several independent solves in one launch
+// (the solver pool's cross-solve grouping): the grid covers the prep items,
+// or the 32 x 32 output tiles, of every contraction in the group; a CTA finds
+// its contraction by binary search over the prefix positions and runs the
+// same per-item code as a lone launch, so every output is bit-identical to it.
+__device__ __forceinline__ int group_of(const GroupRef* __restrict__ refs, int nrefs, int b, bool tiles) {
+    int lo = 0, hi = nrefs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if ((tiles ? refs[mid].tile_start : refs[mid].prep_start) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int S>
+__global__ void __launch_bounds__(256) ozaki_prep_group_kernel(const GroupRef* __restrict__ refs, int nrefs) {
+    const GroupRef& g = refs[group_of(refs, nrefs, blockIdx.x, false)];
+    prep_item<S>(g.prep[blockIdx.x - g.prep_start], g.ops, g.tab, g.A, g.B, g.panels, g.plane, g.exps);
+}
+
+template <int S>
+__global__ void __launch_bounds__(128, 4) gemm_ozaki_group_kernel(const GroupRef* __restrict__ refs, int nrefs) {
+    extern __shared__ __align__(16) unsigned char oz_smem[];
+    const GroupRef& g = refs[group_of(refs, nrefs, blockIdx.x, true)];
+    oz_tile<S, 2>(g.items[blockIdx.x - g.tile_start], g.pairs, g.cblk, g.ops, g.tab, g.panels, g.plane, g.exps, g.C,
+                  oz_smem);
+}
+
+void launch_ozaki_group(cudaStream_t stream, GroupRef const* refs, int nrefs, int total_prep, int total_tiles, int S) {
+    auto go = [&](auto prep, auto gemm, size_t smem) {
+        if (total_prep > 0) prep<<<total_prep, 256, 0, stream>>>(refs, nrefs);
+        if (total_tiles > 0) {
+            static const bool attr = [&] {
+                cudaFuncSetAttribute(gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                return true;
+            }();
+            (void)attr;
+            gemm<<<total_tiles, 128, smem, stream>>>(refs, nrefs);
+        }
+    };
+    switch (S) {
+        case 3: go(ozaki_prep_group_kernel<3>, gemm_ozaki_group_kernel<3>, oz_smem_bytes<3, 2>()); break;
+        case 4: go(ozaki_prep_group_kernel<4>, gemm_ozaki_group_kernel<4>, oz_smem_bytes<4, 2>()); break;
+        case 5: go(ozaki_prep_group_kernel<5>, gemm_ozaki_group_kernel<5>, oz_smem_bytes<5, 2>()); break;
+        default: go(ozaki_prep_group_kernel<6>, gemm_ozaki_group_kernel<6>, oz_smem_bytes<6, 2>()); break;
+    }
+    ITG_CHECK_CUDA(cudaGetLastError());
 }
 
 // ---------------------------------------------------------------- tensor-core (tcgen05) variant

@@ -125,6 +125,12 @@ void SolverPool::start() {
     }
 }
 
+void SolverPool::set_grouping(bool on) {
+    std::lock_guard<std::mutex> g(mu_);
+    ITG_REQUIRE(!started_, "pool: grouping is set before start");
+    grouping_ = on;
+}
+
 void SolverPool::drain() {
     std::unique_lock<std::mutex> lk(mu_);
     ITG_REQUIRE(started_, "pool: drain before start");
@@ -141,6 +147,8 @@ PoolStats SolverPool::stats() {
     std::lock_guard<std::mutex> g(mu_);
     PoolStats s = st_;
     s.elapsed = now();
+    s.grouped_launches = grouped_launches_.load();
+    s.grouped_contractions = grouped_contractions_.load();
     return s;
 }
 
@@ -214,6 +222,7 @@ void run_solve(Ctx& ctx, SolveRecord& rec, SolverPool const& pool) {
 void SolverPool::worker_main(int w) {
     std::vector<std::unique_ptr<Slot>> slots;
     FiberScheduler sched;
+    sched.grouping = grouping_;
     try {
         ITG_CHECK_CUDA(cudaSetDevice(device_));
         for (int i = 0; i < slots_; ++i) {
@@ -278,6 +287,15 @@ void SolverPool::worker_main(int w) {
             if (!queue_.empty()) wait_s = std::clamp(queue_.front()->t_arrive - now(), 2e-4, 0.05);
             cv_work_.wait_for(lk, std::chrono::duration<double>(wait_s));
             continue;
+        }
+        if (!progressed && !sched.pending.empty()) {
+            // every solve here waits (for its stream or for a grouped launch):
+            // enqueue the waiting contractions as one grouped launch
+            const uint64_t l0 = sched.grouped_launches, c0 = sched.grouped_contractions;
+            sched.flush();
+            grouped_launches_ += (int64_t)(sched.grouped_launches - l0);
+            grouped_contractions_ += (int64_t)(sched.grouped_contractions - c0);
+            progressed = true;
         }
         if (progressed) {
             idle_spins = 0;

@@ -67,6 +67,8 @@ struct PoolStats {
     int64_t reserved_bytes = 0, peak_reserved_bytes = 0;
     int running = 0, peak_running = 0;
     double elapsed = 0;          // seconds since start
+    // grouped launches (split-precision prep + GEMM of several solves' contractions each)
+    int64_t grouped_launches = 0, grouped_contractions = 0;
 };
 
 class SolverPool {
@@ -75,6 +77,10 @@ public:
     ~SolverPool();
     int64_t submit(SolveRequest req);  // thread-safe, before or after start()
     void start();
+    // Cross-solve grouping (before start; on by default): the split-precision
+    // contractions that a worker's solves reach while all of them wait run as
+    // one grouped launch instead of one launch each.
+    void set_grouping(bool on);
     void drain();                      // blocks until every submitted request has finished
     SolveRecord record(int64_t id);
     PoolStats stats();
@@ -91,6 +97,8 @@ private:
     void finish(std::shared_ptr<SolveRecord> const& rec);
 
     int device_, workers_, slots_;
+    bool grouping_ = true;
+    std::atomic<int64_t> grouped_launches_{0}, grouped_contractions_{0};
     int64_t budget_;
     std::shared_ptr<PlanCache> plans_ = std::make_shared<PlanCache>();
     std::mutex mu_;

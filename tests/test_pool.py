@@ -133,3 +133,31 @@ def test_pool_admission_and_arrivals(ctx):
             assert abs(rec.energy - ref.energy) <= MIX_ENERGY_TOL
     finally:
         pool.close()
+
+
+@pytest.mark.gpu
+def test_grouped_launches_across_solves_change_nothing():
+    """Cross-solve grouping: with several solves on one worker, their
+    split-precision contractions run as grouped launches (one prep and one
+    GEMM launch covering every solve's blocks). Results are bit-identical to
+    the pool without grouping, and the groups do carry several solves each."""
+    reqs = [(dict(type=0, N=n, J=1.0, Jz=jz), SW_SMALL) for n, jz in ((14, 0.5), (16, 1.0), (12, 1.5), (18, 0.8),
+                                                                     (16, 0.2), (14, 1.2))]
+    runs = {}
+    for grouping in (False, True):
+        pool = itg.Pool(0, workers=1, slots_per_worker=len(reqs), budget_bytes=8 << 30, grouping=grouping)
+        try:
+            ids = [pool.submit(m, sw, itg.PREC_OZAKI_BF16) for m, sw in reqs]
+            pool.start()
+            pool.drain()
+            runs[grouping] = [pool.result(i) for i in ids]
+            launches, contractions = pool.grouping_stats()
+        finally:
+            pool.close()
+        if grouping:
+            assert launches > 0 and contractions > launches / 2, (launches, contractions)
+        else:
+            assert launches == 0
+    for a, b in zip(runs[False], runs[True]):
+        assert a.energy == b.energy
+        assert [x[3:] for x in a.bonds] == [x[3:] for x in b.bonds]
