@@ -131,6 +131,8 @@ int itg_plan_output(const itg_plan* plan, int32_t* rank, int32_t* nblocks, int64
 int itg_plan_output_blocks(const itg_plan* plan, int32_t* coords, int64_t* offsets);
 int itg_plan_flops(const itg_plan* plan, double* flops);
 int itg_contract_exec(itg_ctx* ctx, const itg_plan* plan, const double* A, const double* B, double* C, int precision);
+/* A plan's device tables belong to the context that built it and are freed on
+ * its stream: free a plan only after the work of every context that ran it. */
 void itg_plan_free(itg_plan* plan);
 
 /* No counterpart in the reference: an allocation-free variant of
@@ -338,10 +340,10 @@ int itg_pool_submit_mpo(itg_pool* p, itg_ctx* ctx, int32_t nsites, const itg_ten
                         double arrival_s, int keep_mps, int64_t* id);
 /* No counterpart in the reference (it has no batched mode; the nearest is the
  * per-output-block loop of itensor/itdata/qutil.h:330-348). Cross-solve
- * grouping, on by default, set before itg_pool_start: the split-precision
- * contractions that a worker's solves reach while all of them wait run as one
- * grouped prep launch and one grouped GEMM launch covering every solve's
- * blocks, instead of one launch each. Results are identical either way.
+ * grouping, off by default, set before itg_pool_start: the block GEMMs (FP64,
+ * or split precision: prep and GEMM) that a worker's solves reach while all
+ * of them wait run as one grouped launch covering every solve's blocks,
+ * instead of one launch each. Results are identical either way.
  * itg_pool_grouping_stats counts the grouped launches and the contractions
  * they carried. */
 int itg_pool_set_grouping(itg_pool* p, int on);

@@ -677,7 +677,7 @@ class Pool:
     """Solver pool (itg_pool_*): many ground-state solves on one GPU with
     continuous batching and admission by device-memory estimate."""
 
-    def __init__(self, device=0, workers=4, slots_per_worker=4, budget_bytes=None, grouping=True):
+    def __init__(self, device=0, workers=4, slots_per_worker=4, budget_bytes=None, grouping=False):
         if budget_bytes is None:
             budget_bytes = 64 << 30
         h = C.c_void_p()

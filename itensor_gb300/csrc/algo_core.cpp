@@ -401,20 +401,37 @@ static int64_t dense_size(Tensor const& t) {
     return s;
 }
 
+// Scalar slots of one Davidson call (Ctx::NSCALAR slots per context).
+namespace {
+enum DavSlot : int { S_NRM = 0, S_E0 = 1, S_Q = 2, S_G = 3, S_VQ = 8, S_M = 40, S_PZ = 72 };
+static_assert(S_PZ + VecList::MAX <= Ctx::NSCALAR, "davidson: scalar slots");
+}
+
+// The reductions stay on the device: dot products and norms land in scalar
+// slots that the next kernels read as coefficients, and the host reads them
+// only where the reference's control flow branches on them. A call with
+// niter 2 waits for its stream four times: <phi|H|phi> and the first
+// residual; the new vector's Gram-Schmidt norm with the projected matrix's
+// new column (twice); the second residual. The arithmetic is that of the
+// host-driven form (the same kernels, coefficients formed by the same
+// products), so the results are bit-identical to it.
 double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double errgoal, int miniter, int prec,
                 int* applies) {
     const double approx0 = 1e-12;
     const int64_t n = phi.lay->size;
     int napply = 0;
-    double nrm = tensor_norm(ctx, phi);
-    int guard = 0;
-    while (nrm == 0.0 && guard++ < 4) {
-        launch_random(ctx, phi.data(), n, 0x5eed + guard);
-        nrm = tensor_norm(ctx, phi);
+    ctx.ensure_scalars();
+    double const* scal = ctx.scal_host;
+    Tensor phi_in = phi;
+    // |phi|^2 to the device; phi scaled there. A zero phi shows at the first
+    // wait and takes the reference's re-randomising start instead.
+    {
+        VecList L;
+        L.add(phi.data(), 0.0);
+        dots_async(ctx, L, phi.data(), n, S_NRM);
     }
-    ITG_REQUIRE(nrm > 0, "davidson: zero initial vector");
     phi = copy_tensor(ctx, phi);
-    launch_scale(ctx, phi.data(), n, 1.0 / nrm);
+    scale_rnorm(ctx, phi.data(), n, S_NRM);
     const int64_t maxsize = dense_size(phi);
     const int actual_maxiter = (int)std::min<int64_t>(maxiter, maxsize - 1);
     const int msz = actual_maxiter + 2;
@@ -431,7 +448,6 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
         ITG_REQUIRE((*op.proj)[j].lay->size == n, "davidson: projector not in phi's layout");
         pptr[j] = (*op.proj)[j].data();
     }
-    std::vector<double> pz(std::max(nproj, 1));
     // the other MPOs of a sum, each its own prepared program, added to y
     std::vector<std::shared_ptr<HeffProgram>> more;
     if (op.terms)
@@ -445,22 +461,36 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
             p->run(ctx, x.data(), tmp.data());
             VecList X;
             X.add(tmp.data(), 1.0);
-            combo(ctx, y.data(), 1.0, X, n, false);
+            combo_async(ctx, y.data(), 1.0, X, n, -1);
         }
         if (nproj) {
-            // y += w sum_j P_j (P_j . x)
-            dots(ctx, pptr.data(), nproj, x.data(), n, pz.data());
-            VecList X;
-            for (int j = 0; j < nproj; ++j) X.add(pptr[j], op.proj_weight * pz[j]);
-            combo(ctx, y.data(), 1.0, X, n, false);
+            // y += w sum_j P_j (P_j . x), the dot products left on the device
+            VecList P, X;
+            for (int j = 0; j < nproj; ++j) P.add(pptr[j], 0.0);
+            dots_async(ctx, P, x.data(), n, S_PZ);
+            for (int j = 0; j < nproj; ++j) X.add(pptr[j], op.proj_weight, S_PZ + j);
+            combo_async(ctx, y.data(), 1.0, X, n, -1);
         }
         ++napply;
         return y;
     };
+    // Gram-Schmidt of q against V[0..ni-1] and normalisation, on the device
+    auto gs_device = [&](Tensor& q, int ni) {
+        VecList Lv, Lg;
+        for (int k = 0; k < ni; ++k) Lv.add(V[k].data(), 0.0);
+        dots_async(ctx, Lv, q.data(), n, S_VQ);
+        for (int k = 0; k < ni; ++k) Lg.add(V[k].data(), -1.0, S_VQ + k);
+        combo_async(ctx, q.data(), 1.0, Lg, n, S_G);
+        scale_rnorm(ctx, q.data(), n, S_G);
+    };
     V[0] = phi;
     AV[0] = apply(V[0]);
-    const double initEn = dot(ctx, V[0].data(), AV[0].data(), n);
-    double last_lambda = 1000.0, lambda = initEn;
+    {
+        VecList L;
+        L.add(V[0].data(), 0.0);
+        dots_async(ctx, L, AV[0].data(), n, S_E0);
+    }
+    double initEn = 0, last_lambda = 1000.0, lambda = 0;
     Tensor phi_t = phi;
     std::vector<double> D, U;
     int ii = 0;
@@ -469,13 +499,29 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
         Tensor q(phi.lay, ctx.stream);
         double qnorm2 = 0;
         if (ii == 0) {
-            lambda = initEn;
-            Mat(0, 0) = lambda;
-            // q = H V0 - lambda V0 and |q|^2, one launch
+            // q = H V0 - lambda V0 and |q|^2, lambda = <V0|H|V0> from its slot
             VecList L;
             L.add(AV[0].data(), 1.0);
-            L.add(V[0].data(), -lambda);
-            qnorm2 = combo(ctx, q.data(), 0.0, L, n, true);
+            L.add(V[0].data(), -1.0, S_E0);
+            combo_async(ctx, q.data(), 0.0, L, n, S_Q);
+            ctx.sync();
+            if (!(scal[S_NRM] > 0.0)) {
+                // zero starting vector: the reference's random restart
+                // (itensor/iterativesolvers.h), which needs the host in the loop
+                phi = phi_in;
+                double nrm = tensor_norm(ctx, phi);
+                int guard = 0;
+                while (nrm == 0.0 && guard++ < 4) {
+                    launch_random(ctx, phi.data(), n, 0x5eed + guard);
+                    nrm = tensor_norm(ctx, phi);
+                }
+                ITG_REQUIRE(nrm > 0, "davidson: zero initial vector");
+                return davidson(ctx, op, phi, maxiter, errgoal, miniter, prec, applies);
+            }
+            initEn = scal[S_E0];
+            lambda = initEn;
+            Mat(0, 0) = lambda;
+            qnorm2 = scal[S_Q];
         } else {
             std::vector<double> Msub((size_t)(ii + 1) * (ii + 1));
             for (int j = 0; j <= ii; ++j) for (int i = 0; i <= ii; ++i) Msub[(size_t)j * (ii + 1) + i] = Mat(i, j);
@@ -490,44 +536,65 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
                 Lq.add(AV[k].data(), sgn * U[k]);
             }
             Lq.add(pt.data(), -lambda);
-            combo(ctx, pt.data(), 0.0, Lp, n, false);
-            qnorm2 = combo(ctx, q.data(), 0.0, Lq, n, true);
+            combo_async(ctx, pt.data(), 0.0, Lp, n, -1);
             phi_t = pt;
+            // the last iteration stops whatever the residual: it is not needed
+            if (ii == actual_maxiter) break;
+            combo_async(ctx, q.data(), 0.0, Lq, n, S_Q);
+            ctx.sync();
+            qnorm2 = scal[S_Q];
         }
         const double qnorm = std::sqrt(std::max(qnorm2, 0.0));
         const bool converged = (qnorm < errgoal && std::abs(lambda - last_lambda) < errgoal) ||
                                qnorm < std::max(approx0, errgoal * 1e-3);
         last_lambda = lambda;
         if (qnorm < 1e-20 || (converged && ii >= miniter) || ii == actual_maxiter) break;
-        // one Gram-Schmidt pass (re-randomise a dependent vector)
-        int pass = 1, tot_pass = 0;
-        bool done = false;
-        while (pass <= 1) {
-            ++tot_pass;
-            std::vector<double const*> vp(ni);
-            for (int k = 0; k < ni; ++k) vp[k] = V[k].data();
-            std::vector<double> Vq(ni);
-            dots(ctx, vp.data(), ni, q.data(), n, Vq.data());
-            VecList Lg;
-            for (int k = 0; k < ni; ++k) Lg.add(V[k].data(), -Vq[k]);
-            double qnrm = std::sqrt(std::max(combo(ctx, q.data(), 1.0, Lg, n, true), 0.0));
-            if (qnrm < 1e-10) {
-                launch_random(ctx, q.data(), n, 0x9e3779b9ull * (ni + 7 * tot_pass));
-                qnrm = norm(ctx, q.data(), n);
-                --pass;
-                if (ni >= maxsize || tot_pass > 3) { done = true; break; }
-            }
-            launch_scale(ctx, q.data(), n, 1.0 / qnrm);
-            ++pass;
-        }
-        if (done) break;
+        // one Gram-Schmidt pass on the device, the next vector applied and its
+        // column of the projected matrix formed before the host looks at the norm
+        gs_device(q, ni);
         V[ni] = q;
         AV[ni] = apply(V[ni]);
-        std::vector<double const*> vp(ni + 1);
-        for (int k = 0; k <= ni; ++k) vp[k] = V[k].data();
-        std::vector<double> nc(ni + 1);
-        dots(ctx, vp.data(), ni + 1, AV[ni].data(), n, nc.data());
-        for (int k = 0; k <= ni; ++k) { Mat(k, ni) = nc[k]; Mat(ni, k) = nc[k]; }
+        {
+            VecList Lv;
+            for (int k = 0; k <= ni; ++k) Lv.add(V[k].data(), 0.0);
+            dots_async(ctx, Lv, AV[ni].data(), n, S_M);
+        }
+        ctx.sync();
+        double qnrm = std::sqrt(std::max(scal[S_G], 0.0));
+        if (qnrm < 1e-10) {
+            // q depended on V: the pass above divided by a tiny norm. Redo it
+            // the reference's way from there (re-randomise; rare)
+            --napply;
+            int pass = 1, tot_pass = 1;
+            bool done = false;
+            for (;;) {
+                if (qnrm < 1e-10) {
+                    launch_random(ctx, q.data(), n, 0x9e3779b9ull * (ni + 7 * tot_pass));
+                    qnrm = norm(ctx, q.data(), n);
+                    --pass;
+                    if (ni >= maxsize || tot_pass > 3) { done = true; break; }
+                }
+                launch_scale(ctx, q.data(), n, 1.0 / qnrm);
+                ++pass;
+                if (pass > 1) break;
+                ++tot_pass;
+                std::vector<double const*> vp(ni);
+                for (int k = 0; k < ni; ++k) vp[k] = V[k].data();
+                std::vector<double> Vq(ni);
+                dots(ctx, vp.data(), ni, q.data(), n, Vq.data());
+                VecList Lg;
+                for (int k = 0; k < ni; ++k) Lg.add(V[k].data(), -Vq[k]);
+                qnrm = std::sqrt(std::max(combo(ctx, q.data(), 1.0, Lg, n, true), 0.0));
+            }
+            if (done) break;
+            V[ni] = q;
+            AV[ni] = apply(V[ni]);
+            VecList Lv;
+            for (int k = 0; k <= ni; ++k) Lv.add(V[k].data(), 0.0);
+            dots_async(ctx, Lv, AV[ni].data(), n, S_M);
+            ctx.sync();
+        }
+        for (int k = 0; k <= ni; ++k) { Mat(k, ni) = scal[S_M + k]; Mat(ni, k) = scal[S_M + k]; }
     }
     phi = phi_t;
     if (applies) *applies += napply;

@@ -318,6 +318,7 @@ int itg_contract_plan(itg_ctx* c, const itg_layout_desc* A, const int32_t* label
         Layout LA = build(A, labelsA, 0), LB = build(B, labelsB, 1);
         Match mt = match_indices(LA.inds, LB.inds);
         auto p = get_plan(c->ctx, LA, LB, mt);
+        c->ctx.sync();  // the tables are resident before the plan is handed out (any stream may run it)
         *plan = new itg_plan{p, p->C};
     });
 }

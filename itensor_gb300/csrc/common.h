@@ -81,11 +81,30 @@ struct MemAccount {
 // Account charged by the calling thread's allocations (empty: none).
 std::shared_ptr<MemAccount>& current_account();
 
-// Blocks a solve has freed on its stream, kept for its next allocations on
-// that stream: reuse in stream order needs no synchronisation, and the solver
+// Device allocations are rounded up to size classes: eight per power of two
+// (at most 12.5% over the request), 512 B at least. Blocks freed by one
+// tensor then fit the next request of about the same size, so caches hit.
+inline size_t alloc_class(size_t n) {
+    if (n <= 512) return 512;
+    const int k = 63 - __builtin_clzll((unsigned long long)(n - 1));  // 2^k < n <= 2^(k+1)
+    const size_t step = size_t(1) << (k - 3);
+    return (n + step - 1) / step * step;
+}
+
+// Process-wide allocator counters (diagnostics): requests served by a block
+// cache, and the driver's allocation and free calls.
+struct AllocCounters {
+    std::atomic<uint64_t> cached{0}, driver_allocs{0}, driver_frees{0};
+    std::atomic<uint64_t> bypass{0}, nocache{0}, full{0};  // driver allocations without a cache; frees a full cache refused
+};
+AllocCounters& alloc_counters();
+
+// Blocks freed on a context's stream, kept for its next allocations on that
+// stream: reuse in stream order needs no synchronisation, and the solver
 // pool's many threads then make far fewer allocator calls (which serialise
 // on the driver). Blocks are reused for requests of half their size or more;
-// the cache holds at most `limit` bytes and is emptied when the solve ends.
+// the cache holds at most `limit` bytes. In the solver pool it outlives the
+// solves of its slot and is trimmed when each solve ends.
 struct BlockCache {
     std::mutex mu;
     cudaStream_t stream = nullptr;
@@ -109,7 +128,8 @@ struct BlockCache {
         held += n;
         return true;
     }
-    void release();  // frees every cached block (on the stream while it lives)
+    void release() { trim(0); }  // frees every cached block (on the stream while it lives)
+    void trim(size_t keep);       // frees the largest blocks until at most `keep` bytes stay
     ~BlockCache() { release(); }
 };
 // Cache serving the calling thread's allocations (empty: none).
@@ -126,17 +146,27 @@ struct DevBuf {
     DevBuf() = default;
     DevBuf(size_t n, cudaStream_t s) : bytes(n), stream(s) {
         if (n) {
+            const size_t cls = alloc_class(n);
             std::shared_ptr<BlockCache> c;
             if (!cache_bypass()) {
-                c = current_cache();                // a pool solve's own cache
+                c = current_cache();                // the cache of a pool solve's slot
                 if (!c || c->stream != s) c = stream_cache(s);  // else the stream's context cache
             }
             if (c && c->stream == s) {
                 cache = c;
                 size_t got = 0;
-                if ((p = c->take(n, &got))) bytes = got;
+                if ((p = c->take(cls, &got))) {
+                    bytes = got;
+                    alloc_counters().cached.fetch_add(1, std::memory_order_relaxed);
+                }
             }
-            if (!p) ITG_CHECK_CUDA(cudaMallocAsync(&p, n, s));
+            if (!p) {
+                ITG_CHECK_CUDA(cudaMallocAsync(&p, cls, s));
+                bytes = cls;
+                alloc_counters().driver_allocs.fetch_add(1, std::memory_order_relaxed);
+                if (cache_bypass()) alloc_counters().bypass.fetch_add(1, std::memory_order_relaxed);
+                else if (!cache) alloc_counters().nocache.fetch_add(1, std::memory_order_relaxed);
+            }
             acct = current_account();
             if (acct) acct->add((int64_t)bytes);
         }
@@ -146,6 +176,8 @@ struct DevBuf {
         if (acct) acct->sub((int64_t)bytes);
         // (a cache frees its blocks itself, checking its stream then)
         if (cache && cache->put(p, bytes)) return;
+        alloc_counters().driver_frees.fetch_add(1, std::memory_order_relaxed);
+        if (cache) alloc_counters().full.fetch_add(1, std::memory_order_relaxed);
         if (stream_alive(stream)) cudaFreeAsync(p, stream);
         else cudaFree(p);
     }

@@ -650,10 +650,16 @@ Ctx::~Ctx() {
     for (auto& r : prof) { cudaEventDestroy(r.start); cudaEventDestroy(r.stop); }
     plans.reset();
     split_scratch.reset();
+    reduce_buf.reset();
+    scal_dev.reset();
+    if (scal_host) cudaFreeHost(scal_host);
     if (sync_event) cudaEventDestroy(sync_event);
     if (err_host) cudaFreeHost(err_host);
     if (pin) cudaFreeHost(pin);
     if (stage) cudaFreeHost(stage);
+    if (ring) cudaFreeHost(ring);
+    for (int i = 0; i < 2; ++i)
+        if (ring_ev[i]) cudaEventDestroy(ring_ev[i]);
     if (stream) {
         stream_unregister(stream);
         if (cache) cache->release();  // while the stream lives
@@ -688,6 +694,50 @@ void Ctx::sync() {
     }
 }
 
+void Ctx::wait_event(cudaEvent_t ev) {
+    if (fiber_active()) fiber_wait_event(ev);
+    else ITG_CHECK_CUDA(cudaEventSynchronize(ev));
+}
+
+char* Ctx::stage_ring(size_t n) {
+    n = (n + 255) / 256 * 256;
+    if (n > ring_half) {
+        // grow: the copies from the old ring must have run
+        sync();
+        if (ring) cudaFreeHost(ring);
+        ring = nullptr;
+        ring_half = std::max<size_t>({n, size_t(256) << 10, 2 * ring_half});
+        ITG_CHECK_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ring), 2 * ring_half, cudaHostAllocDefault));
+        for (int i = 0; i < 2; ++i) {
+            if (!ring_ev[i]) ITG_CHECK_CUDA(cudaEventCreateWithFlags(&ring_ev[i], cudaEventDisableTiming));
+            ring_pending[i] = false;
+        }
+        ring_off = 0;
+        ring_cur = 0;
+    }
+    if (ring_off + n > ring_half) {
+        // every copy from this half has been enqueued: mark its end, go to the other half
+        ITG_CHECK_CUDA(cudaEventRecord(ring_ev[ring_cur], stream));
+        ring_pending[ring_cur] = true;
+        ring_cur ^= 1;
+        ring_off = 0;
+        if (ring_pending[ring_cur]) {
+            wait_event(ring_ev[ring_cur]);
+            ring_pending[ring_cur] = false;
+        }
+    }
+    char* p = ring + (size_t)ring_cur * ring_half + ring_off;
+    ring_off += n;
+    return p;
+}
+
+void Ctx::upload(void* dst, void const* src, size_t n) {
+    if (!n) return;
+    char* p = stage_ring(n);
+    std::memcpy(p, src, n);
+    ITG_CHECK_CUDA(cudaMemcpyAsync(dst, p, n, cudaMemcpyHostToDevice, stream));
+}
+
 void Ctx::d2h(void* dst, void const* src, size_t bytes) {
     if (!bytes) return;
     ensure_pin(bytes);
@@ -712,15 +762,23 @@ std::shared_ptr<BlockCache>& current_cache() {
     return cache;
 }
 
-void BlockCache::release() {
+AllocCounters& alloc_counters() {
+    static AllocCounters c;
+    return c;
+}
+
+void BlockCache::trim(size_t keep) {
     std::lock_guard<std::mutex> g(mu);
+    if (held <= keep) return;
     const bool alive = stream_alive(stream);
-    for (auto& kv : free) {
-        if (alive) cudaFreeAsync(kv.second, stream);
-        else cudaFree(kv.second);
+    while (held > keep && !free.empty()) {
+        auto it = std::prev(free.end());
+        if (alive) cudaFreeAsync(it->second, stream);
+        else cudaFree(it->second);
+        alloc_counters().driver_frees.fetch_add(1, std::memory_order_relaxed);
+        held -= it->first;
+        free.erase(it);
     }
-    free.clear();
-    held = 0;
 }
 
 void Ctx::ensure_stage(size_t bytes) {
@@ -815,6 +873,97 @@ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 }  // namespace
 
+// Contractions with at most this many candidate block pairs are planned on
+// the host (plan_host); larger ones by plan_kernel. ITG_HOST_PLAN_PAIRS moves
+// the threshold (0: every plan on the device).
+static long long host_plan_pairs() {
+    const char* e = std::getenv("ITG_HOST_PLAN_PAIRS");
+    return e ? std::max(0LL, std::atoll(e)) : (1LL << 16);
+}
+
+// Host form of plan_kernel: the same keys, the same stable orders, the same
+// pairs in the same sequence (B-key groups, A in key order, B within the
+// group), hence the same output blocks, offsets and pair-to-block map.
+static void plan_host(Layout const& A, Layout const& B, Match const& mt, std::vector<int32_t> const& bits,
+                      std::vector<int32_t> const& cdims, std::vector<int32_t> const& cdstart, std::vector<int32_t>& pa,
+                      std::vector<int32_t>& pb, std::vector<int32_t>& pc, std::vector<int32_t>& ccoords,
+                      std::vector<int64_t>& coff, int64_t& csize) {
+    const int nA = A.nblocks(), nB = B.nblocks(), rA = A.rank(), rB = B.rank();
+    const int ncon = (int)mt.a_con.size(), nau = (int)mt.a_unc.size(), nbu = (int)mt.b_unc.size();
+    auto pack = [&](int32_t const* c, std::vector<int> const& pos, int b0) {
+        uint64_t k = 0;
+        int sh = 0;
+        for (size_t i = 0; i < pos.size(); ++i) {
+            k |= (uint64_t)(uint32_t)c[pos[i]] << sh;
+            sh += bits[b0 + i];
+        }
+        return k;
+    };
+    int bitsA = 0;
+    for (int i = 0; i < nau; ++i) bitsA += bits[ncon + i];
+    std::vector<uint64_t> keyA(nA), conA(nA), keyB(nB), conB(nB);
+    for (int i = 0; i < nA; ++i) {
+        int32_t const* c = A.coords.data() + (size_t)i * rA;
+        keyA[i] = pack(c, mt.a_unc, ncon);
+        conA[i] = pack(c, mt.a_con, 0);
+    }
+    for (int j = 0; j < nB; ++j) {
+        int32_t const* c = B.coords.data() + (size_t)j * rB;
+        keyB[j] = pack(c, mt.b_unc, ncon + nau);
+        conB[j] = pack(c, mt.b_con, 0);
+    }
+    std::vector<int32_t> sA(nA), sB(nB);
+    std::iota(sA.begin(), sA.end(), 0);
+    std::iota(sB.begin(), sB.end(), 0);
+    std::stable_sort(sA.begin(), sA.end(), [&](int x, int y) { return keyA[x] < keyA[y]; });
+    std::stable_sort(sB.begin(), sB.end(), [&](int x, int y) { return keyB[x] < keyB[y]; });
+    const int rC = nau + nbu;
+    pa.clear(); pb.clear(); pc.clear(); ccoords.clear(); coff.clear();
+    uint64_t last = 0;
+    for (int g0 = 0; g0 < nB;) {
+        int g1 = g0 + 1;
+        while (g1 < nB && keyB[sB[g1]] == keyB[sB[g0]]) ++g1;
+        for (int r = 0; r < nA; ++r) {
+            const int ia = sA[r];
+            for (int t = g0; t < g1; ++t) {
+                const int jb = sB[t];
+                if (conA[ia] != conB[jb]) continue;
+                const uint64_t pk = keyA[ia] | (keyB[jb] << bitsA);
+                if (pa.empty() || pk != last) {
+                    // a new output block: coordinates and size from this pair
+                    int32_t const* ca = A.coords.data() + (size_t)ia * rA;
+                    int32_t const* cb = B.coords.data() + (size_t)jb * rB;
+                    int64_t size = 1;
+                    for (int i = 0; i < nau; ++i) {
+                        const int sct = ca[mt.a_unc[i]];
+                        ccoords.push_back(sct);
+                        size *= cdims[cdstart[i] + sct];
+                    }
+                    for (int i = 0; i < nbu; ++i) {
+                        const int sct = cb[mt.b_unc[i]];
+                        ccoords.push_back(sct);
+                        size *= cdims[cdstart[nau + i] + sct];
+                    }
+                    coff.push_back(size);
+                    last = pk;
+                }
+                pa.push_back(ia);
+                pb.push_back(jb);
+                pc.push_back((int32_t)coff.size() - 1);
+            }
+        }
+        g0 = g1;
+    }
+    (void)rC;
+    int64_t tot = 0;
+    for (auto& o : coff) {
+        const int64_t sz = o;
+        o = tot;
+        tot += sz;
+    }
+    csize = tot;
+}
+
 std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match const& mt,
                                std::shared_ptr<Layout> target) {
     const int nau = (int)mt.a_unc.size(), nbu = (int)mt.b_unc.size(), ncon = (int)mt.a_con.size();
@@ -842,20 +991,14 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
     put(key, (int32_t)(target ? 1 : 0));
     if (target) { put_layout_structure(key, *target); putv(key, perm); }
     if (auto hit = ctx.plans->find(key)) { ctx.plan_hits++; return hit; }
-    // plan tables outlive the solve that builds them (the cache is shared):
-    // they are not charged to its memory account
-    // (nor taken from its block cache, which is emptied when the solve ends)
+    // Plan tables belong to the context's plan cache, not to the solve that
+    // builds them: they are not charged to its memory account. They come from
+    // the context's block cache like its other buffers and are read only by
+    // launches on its stream (which also orders their upload and their free).
     struct Uncharged {
         std::shared_ptr<MemAccount> saved;
-        bool saved_bypass;
-        Uncharged() : saved(std::move(current_account())), saved_bypass(cache_bypass()) {
-            current_account().reset();
-            cache_bypass() = true;
-        }
-        ~Uncharged() {
-            current_account() = std::move(saved);
-            cache_bypass() = saved_bypass;
-        }
+        Uncharged() : saved(std::move(current_account())) { current_account().reset(); }
+        ~Uncharged() { current_account() = std::move(saved); }
     } uncharged;
 
     const int nA = A.nblocks(), nB = B.nblocks(), rA = A.rank(), rB = B.rank();
@@ -883,69 +1026,82 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
     static const bool plan_timing = std::getenv("ITG_PLAN_TIME") != nullptr;
     auto pt0 = std::chrono::steady_clock::now();
     if (nA > 0 && nB > 0) {
-        // inputs -> device (one staged copy)
-        size_t o_ac = 0, o_bc = align16(o_ac + sizeof(int32_t) * std::max<size_t>(1, A.coords.size()));
-        size_t o_pos = align16(o_bc + sizeof(int32_t) * std::max<size_t>(1, B.coords.size()));
-        size_t o_bits = align16(o_pos + sizeof(int32_t) * std::max<size_t>(1, pos.size()));
-        size_t o_cd = align16(o_bits + sizeof(int32_t) * std::max<size_t>(1, bits.size()));
-        size_t o_cs = align16(o_cd + sizeof(int32_t) * std::max<size_t>(1, cdims.size()));
-        size_t in_bytes = align16(o_cs + sizeof(int32_t) * std::max<size_t>(1, cdstart.size()));
-        ctx.ensure_stage(in_bytes);
-        char* st = static_cast<char*>(ctx.stage);
-        auto cp = [&](size_t o, auto const& v) { if (!v.empty()) std::memcpy(st + o, v.data(), v.size() * sizeof(v[0])); };
-        cp(o_ac, A.coords); cp(o_bc, B.coords); cp(o_pos, pos); cp(o_bits, bits); cp(o_cd, cdims); cp(o_cs, cdstart);
-        size_t o_keyA = align16(in_bytes), o_keyB = align16(o_keyA + 8 * (size_t)nA);
-        size_t o_conA = align16(o_keyB + 8 * (size_t)nB), o_conB = align16(o_conA + 8 * (size_t)nA);
-        size_t o_sA = align16(o_conB + 8 * (size_t)nB), o_sB = align16(o_sA + 4 * (size_t)nA);
-        size_t o_gs = align16(o_sB + 4 * (size_t)nB), o_pk = align16(o_gs + 4 * (size_t)(nB + 1));
-        size_t dev_bytes = align16(o_pk + 8 * (size_t)cap);
-        DevBuf scratch(dev_bytes, ctx.stream);
-        char* dv = scratch.as<char>();
-        ITG_CHECK_CUDA(cudaMemcpyAsync(dv, st, in_bytes, cudaMemcpyHostToDevice, ctx.stream));
-        // outputs in host-mapped memory
-        size_t p_cnt = 0, p_pa = 16, p_pb = align16(p_pa + 4 * (size_t)cap), p_pc = align16(p_pb + 4 * (size_t)cap);
-        size_t p_cc = align16(p_pc + 4 * (size_t)cap), p_co = align16(p_cc + 4 * (size_t)cap * std::max(rC, 1));
-        size_t out_bytes = align16(p_co + 8 * ((size_t)cap + 1));
-        ctx.ensure_pin(out_bytes);
-        char* hp = static_cast<char*>(ctx.pin);
-        char* dp = static_cast<char*>(ctx.pin_dev);
-        PlanArgs a;
-        a.nA = nA; a.nB = nB; a.rA = rA; a.rB = rB; a.ncon = ncon; a.nau = nau; a.nbu = nbu;
-        a.Acoords = reinterpret_cast<const int32_t*>(dv + o_ac);
-        a.Bcoords = reinterpret_cast<const int32_t*>(dv + o_bc);
-        a.pos = reinterpret_cast<const int32_t*>(dv + o_pos);
-        a.bits = reinterpret_cast<const int32_t*>(dv + o_bits);
-        a.cdims = reinterpret_cast<const int32_t*>(dv + o_cd);
-        a.cdstart = reinterpret_cast<const int32_t*>(dv + o_cs);
-        a.keyA = reinterpret_cast<uint64_t*>(dv + o_keyA); a.keyB = reinterpret_cast<uint64_t*>(dv + o_keyB);
-        a.conA = reinterpret_cast<uint64_t*>(dv + o_conA); a.conB = reinterpret_cast<uint64_t*>(dv + o_conB);
-        a.sortA = reinterpret_cast<int32_t*>(dv + o_sA); a.sortB = reinterpret_cast<int32_t*>(dv + o_sB);
-        a.gstart = reinterpret_cast<int32_t*>(dv + o_gs); a.pkey = reinterpret_cast<uint64_t*>(dv + o_pk);
-        a.out_counts = reinterpret_cast<int32_t*>(dp + p_cnt);
-        a.pair_a = reinterpret_cast<int32_t*>(dp + p_pa); a.pair_b = reinterpret_cast<int32_t*>(dp + p_pb);
-        a.pair_c = reinterpret_cast<int32_t*>(dp + p_pc);
-        a.c_coords = reinterpret_cast<int32_t*>(dp + p_cc);
-        a.c_off = reinterpret_cast<int64_t*>(dp + p_co);
-        a.cap_pairs = cap; a.cap_c = cap;
-        plan_kernel<<<1, 1024, 0, ctx.stream>>>(a);
-        ITG_CHECK_CUDA(cudaGetLastError());
-        ctx.kernel_launches++;
-        ctx.sync();
-        int32_t const* cnt = reinterpret_cast<int32_t const*>(hp + p_cnt);
-        if (cnt[2]) throw Error(ERR_INTERNAL, "contract planner: capacity overflow");
-        const int np = cnt[0], nc = cnt[1];
-        auto pt1 = std::chrono::steady_clock::now();
-        std::vector<int32_t> pa(reinterpret_cast<int32_t*>(hp + p_pa), reinterpret_cast<int32_t*>(hp + p_pa) + np);
-        std::vector<int32_t> pb(reinterpret_cast<int32_t*>(hp + p_pb), reinterpret_cast<int32_t*>(hp + p_pb) + np);
-        std::vector<int32_t> pc(reinterpret_cast<int32_t*>(hp + p_pc), reinterpret_cast<int32_t*>(hp + p_pc) + np);
+        std::vector<int32_t> pa, pb, pc;
         auto natural = std::make_shared<Layout>();
         natural->inds = cinds;
-        if (rC > 0) {
-            natural->coords.assign(reinterpret_cast<int32_t*>(hp + p_cc), reinterpret_cast<int32_t*>(hp + p_cc) + (size_t)nc * rC);
-            natural->offs.assign(reinterpret_cast<int64_t*>(hp + p_co), reinterpret_cast<int64_t*>(hp + p_co) + nc);
-            natural->size = reinterpret_cast<int64_t*>(hp + p_co)[nc];
+        int np = 0, nc = 0;
+        auto pt1 = pt0;
+        if (cap <= host_plan_pairs()) {
+            // few candidate pairs: the same planner on the host, no launch and no wait
+            plan_host(A, B, mt, bits, cdims, cdstart, pa, pb, pc, natural->coords, natural->offs, natural->size);
+            np = (int)pa.size();
+            nc = (int)natural->offs.size();
+            if (rC == 0) natural->finish();
+            pt1 = std::chrono::steady_clock::now();
         } else {
-            natural->finish();  // one scalar block
+            // inputs -> device (one staged copy)
+            size_t o_ac = 0, o_bc = align16(o_ac + sizeof(int32_t) * std::max<size_t>(1, A.coords.size()));
+            size_t o_pos = align16(o_bc + sizeof(int32_t) * std::max<size_t>(1, B.coords.size()));
+            size_t o_bits = align16(o_pos + sizeof(int32_t) * std::max<size_t>(1, pos.size()));
+            size_t o_cd = align16(o_bits + sizeof(int32_t) * std::max<size_t>(1, bits.size()));
+            size_t o_cs = align16(o_cd + sizeof(int32_t) * std::max<size_t>(1, cdims.size()));
+            size_t in_bytes = align16(o_cs + sizeof(int32_t) * std::max<size_t>(1, cdstart.size()));
+            ctx.ensure_stage(in_bytes);
+            char* st = static_cast<char*>(ctx.stage);
+            auto cp = [&](size_t o, auto const& v) { if (!v.empty()) std::memcpy(st + o, v.data(), v.size() * sizeof(v[0])); };
+            cp(o_ac, A.coords); cp(o_bc, B.coords); cp(o_pos, pos); cp(o_bits, bits); cp(o_cd, cdims); cp(o_cs, cdstart);
+            size_t o_keyA = align16(in_bytes), o_keyB = align16(o_keyA + 8 * (size_t)nA);
+            size_t o_conA = align16(o_keyB + 8 * (size_t)nB), o_conB = align16(o_conA + 8 * (size_t)nA);
+            size_t o_sA = align16(o_conB + 8 * (size_t)nB), o_sB = align16(o_sA + 4 * (size_t)nA);
+            size_t o_gs = align16(o_sB + 4 * (size_t)nB), o_pk = align16(o_gs + 4 * (size_t)(nB + 1));
+            size_t dev_bytes = align16(o_pk + 8 * (size_t)cap);
+            DevBuf scratch(dev_bytes, ctx.stream);
+            char* dv = scratch.as<char>();
+            ITG_CHECK_CUDA(cudaMemcpyAsync(dv, st, in_bytes, cudaMemcpyHostToDevice, ctx.stream));
+            // outputs in host-mapped memory
+            size_t p_cnt = 0, p_pa = 16, p_pb = align16(p_pa + 4 * (size_t)cap), p_pc = align16(p_pb + 4 * (size_t)cap);
+            size_t p_cc = align16(p_pc + 4 * (size_t)cap), p_co = align16(p_cc + 4 * (size_t)cap * std::max(rC, 1));
+            size_t out_bytes = align16(p_co + 8 * ((size_t)cap + 1));
+            ctx.ensure_pin(out_bytes);
+            char* hp = static_cast<char*>(ctx.pin);
+            char* dp = static_cast<char*>(ctx.pin_dev);
+            PlanArgs a;
+            a.nA = nA; a.nB = nB; a.rA = rA; a.rB = rB; a.ncon = ncon; a.nau = nau; a.nbu = nbu;
+            a.Acoords = reinterpret_cast<const int32_t*>(dv + o_ac);
+            a.Bcoords = reinterpret_cast<const int32_t*>(dv + o_bc);
+            a.pos = reinterpret_cast<const int32_t*>(dv + o_pos);
+            a.bits = reinterpret_cast<const int32_t*>(dv + o_bits);
+            a.cdims = reinterpret_cast<const int32_t*>(dv + o_cd);
+            a.cdstart = reinterpret_cast<const int32_t*>(dv + o_cs);
+            a.keyA = reinterpret_cast<uint64_t*>(dv + o_keyA); a.keyB = reinterpret_cast<uint64_t*>(dv + o_keyB);
+            a.conA = reinterpret_cast<uint64_t*>(dv + o_conA); a.conB = reinterpret_cast<uint64_t*>(dv + o_conB);
+            a.sortA = reinterpret_cast<int32_t*>(dv + o_sA); a.sortB = reinterpret_cast<int32_t*>(dv + o_sB);
+            a.gstart = reinterpret_cast<int32_t*>(dv + o_gs); a.pkey = reinterpret_cast<uint64_t*>(dv + o_pk);
+            a.out_counts = reinterpret_cast<int32_t*>(dp + p_cnt);
+            a.pair_a = reinterpret_cast<int32_t*>(dp + p_pa); a.pair_b = reinterpret_cast<int32_t*>(dp + p_pb);
+            a.pair_c = reinterpret_cast<int32_t*>(dp + p_pc);
+            a.c_coords = reinterpret_cast<int32_t*>(dp + p_cc);
+            a.c_off = reinterpret_cast<int64_t*>(dp + p_co);
+            a.cap_pairs = cap; a.cap_c = cap;
+            plan_kernel<<<1, 1024, 0, ctx.stream>>>(a);
+            ITG_CHECK_CUDA(cudaGetLastError());
+            ctx.kernel_launches++;
+            ctx.sync();
+            int32_t const* cnt = reinterpret_cast<int32_t const*>(hp + p_cnt);
+            if (cnt[2]) throw Error(ERR_INTERNAL, "contract planner: capacity overflow");
+            np = cnt[0];
+            nc = cnt[1];
+            pt1 = std::chrono::steady_clock::now();
+            pa.assign(reinterpret_cast<int32_t*>(hp + p_pa), reinterpret_cast<int32_t*>(hp + p_pa) + np);
+            pb.assign(reinterpret_cast<int32_t*>(hp + p_pb), reinterpret_cast<int32_t*>(hp + p_pb) + np);
+            pc.assign(reinterpret_cast<int32_t*>(hp + p_pc), reinterpret_cast<int32_t*>(hp + p_pc) + np);
+            if (rC > 0) {
+                natural->coords.assign(reinterpret_cast<int32_t*>(hp + p_cc), reinterpret_cast<int32_t*>(hp + p_cc) + (size_t)nc * rC);
+                natural->offs.assign(reinterpret_cast<int64_t*>(hp + p_co), reinterpret_cast<int64_t*>(hp + p_co) + nc);
+                natural->size = reinterpret_cast<int64_t*>(hp + p_co)[nc];
+            } else {
+                natural->finish();  // one scalar block
+            }
         }
         plan->C = target ? target : natural;
         // ---- map natural blocks to target blocks
@@ -1149,8 +1305,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         size_t t_ptc = align16(t_itc + sizeof(TcTile) * items_tc.size());
         size_t t_tab = align16(t_ptc + sizeof(TcPair) * pairs_tc.size());
         size_t tbytes = align16(t_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size()));
-        ctx.ensure_stage(tbytes);
-        st = static_cast<char*>(ctx.stage);
+        char* st = ctx.stage_ring(tbytes);
         if (!sitems.empty()) std::memcpy(st + t_items, sitems.data(), sizeof(ItemRec) * sitems.size());
         if (!items64.empty()) std::memcpy(st + t_i64, items64.data(), sizeof(ItemRec) * items64.size());
         if (!items_tc.empty()) std::memcpy(st + t_itc, items_tc.data(), sizeof(TcTile) * items_tc.size());
@@ -1171,7 +1326,6 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->dev = dev_alloc(tbytes, ctx.stream);
         char* db = plan->dev->as<char>();
         ITG_CHECK_CUDA(cudaMemcpyAsync(db, st, tbytes, cudaMemcpyHostToDevice, ctx.stream));
-        ctx.sync();  // staging buffer is reused by the next plan
         plan->d_items = reinterpret_cast<ItemRec*>(db + t_items);
         plan->d_pairs = reinterpret_cast<PairRec*>(db + t_pairs);
         plan->d_cblk = reinterpret_cast<CBlockRec*>(db + t_cblk);
@@ -1220,15 +1374,13 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         size_t t_items = 0, t_cblk = align16(sizeof(ItemRec) * std::max<size_t>(1, items.size()));
         size_t t_tab = align16(t_cblk + sizeof(CBlockRec) * std::max<size_t>(1, cblk.size()));
         size_t tbytes = align16(t_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size()));
-        ctx.ensure_stage(tbytes);
-        char* st = static_cast<char*>(ctx.stage);
+        char* st = ctx.stage_ring(tbytes);
         if (!items.empty()) std::memcpy(st + t_items, items.data(), sizeof(ItemRec) * items.size());
         if (!cblk.empty()) std::memcpy(st + t_cblk, cblk.data(), sizeof(CBlockRec) * cblk.size());
         if (!tab.empty()) std::memcpy(st + t_tab, tab.data(), sizeof(int32_t) * tab.size());
         plan->dev = dev_alloc(tbytes, ctx.stream);
         char* db = plan->dev->as<char>();
         ITG_CHECK_CUDA(cudaMemcpyAsync(db, st, tbytes, cudaMemcpyHostToDevice, ctx.stream));
-        ctx.sync();
         plan->d_items = reinterpret_cast<ItemRec*>(db + t_items);
         plan->d_pairs = nullptr;
         plan->d_cblk = reinterpret_cast<CBlockRec*>(db + t_cblk);

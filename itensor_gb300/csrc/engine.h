@@ -144,27 +144,43 @@ struct Plan {
 // solver pool shares one across its slots): lookups and inserts are locked,
 // builds are not (two contexts may build the same plan; the second insert is
 // dropped). A plan's tables are immutable once inserted.
+// Plans by block structure, shared by a context or by all slots of a solver
+// pool. Split into shards by key hash, each with its own lock, so the pool's
+// threads rarely touch the same lock word.
 struct PlanCache {
-    std::shared_mutex mu;   // lookups (the common case) share the lock
-    std::unordered_map<std::string, std::shared_ptr<Plan>> map;
-    size_t limit = 16384;
+    static constexpr int NSHARD = 32;
+    struct alignas(128) Shard {
+        std::shared_mutex mu;   // lookups (the common case) share the lock
+        std::unordered_map<std::string, std::shared_ptr<Plan>> map;
+    };
+    Shard shard[NSHARD];
+    size_t limit = 32768;       // plans in all shards together
+    Shard& of(std::string const& key) { return shard[std::hash<std::string>{}(key) % NSHARD]; }
     std::shared_ptr<Plan> find(std::string const& key) {
-        std::shared_lock<std::shared_mutex> g(mu);
-        auto it = map.find(key);
-        return it == map.end() ? nullptr : it->second;
+        Shard& s = of(key);
+        std::shared_lock<std::shared_mutex> g(s.mu);
+        auto it = s.map.find(key);
+        return it == s.map.end() ? nullptr : it->second;
     }
     std::shared_ptr<Plan> insert(std::string key, std::shared_ptr<Plan> p) {
-        std::unique_lock<std::shared_mutex> g(mu);
-        if (map.size() >= limit) map.clear();
-        return map.emplace(std::move(key), std::move(p)).first->second;
+        Shard& s = of(key);
+        std::unique_lock<std::shared_mutex> g(s.mu);
+        if (s.map.size() >= limit / NSHARD) s.map.clear();
+        return s.map.emplace(std::move(key), std::move(p)).first->second;
     }
     size_t size() {
-        std::shared_lock<std::shared_mutex> g(mu);
-        return map.size();
+        size_t n = 0;
+        for (auto& s : shard) {
+            std::shared_lock<std::shared_mutex> g(s.mu);
+            n += s.map.size();
+        }
+        return n;
     }
     void clear() {
-        std::unique_lock<std::shared_mutex> g(mu);
-        map.clear();
+        for (auto& s : shard) {
+            std::unique_lock<std::shared_mutex> g(s.mu);
+            s.map.clear();
+        }
     }
 };
 
@@ -188,6 +204,13 @@ struct Ctx {
     // pinned staging buffer for host->device table uploads
     void* stage = nullptr;
     size_t stage_bytes = 0;
+    // Pinned staging ring for uploads that do not wait for the stream: two
+    // halves, a half reused only after the copies enqueued from it completed.
+    char* ring = nullptr;
+    size_t ring_half = 0, ring_off = 0;
+    int ring_cur = 0;
+    cudaEvent_t ring_ev[2] = {};
+    bool ring_pending[2] = {};
     std::shared_ptr<PlanCache> plans = std::make_shared<PlanCache>();
     // split-precision digit panels of exec_plan: one growing buffer per context
     // (launches on this stream are ordered, so every exec reuses it)
@@ -203,6 +226,14 @@ struct Ctx {
     // partial sums + completion counter of the fused reductions (ops.cu)
     DevBufPtr reduce_buf;
     void ensure_reduce();
+    // Scalar slots of the device-resident reductions (Davidson): each result
+    // is written to device memory, where later kernels read it as a
+    // coefficient, and to a host-mapped mirror the host reads after a sync().
+    static constexpr int NSCALAR = 128;
+    double* scal_host = nullptr;   // host view of the mapped mirror
+    double* scal_map = nullptr;    // device view of the mapped mirror
+    DevBufPtr scal_dev;            // device copy (read by kernels)
+    void ensure_scalars();
     // side streams for independent launches inside one operation (created on
     // first use; work forked to them is joined back before the operation
     // returns, and uses only buffers allocated on `stream` before the fork)
@@ -226,6 +257,13 @@ struct Ctx {
     ~Ctx();
     void ensure_pin(size_t bytes);
     void ensure_stage(size_t bytes);
+    // n bytes of the staging ring, valid until the copies enqueued from them
+    // on `stream` have run (the caller enqueues them before its next take)
+    char* stage_ring(size_t n);
+    // host -> device copy through the ring, without waiting
+    void upload(void* dst, void const* src, size_t n);
+    // waits for an event recorded on this context's streams (yields in a fiber)
+    void wait_event(cudaEvent_t ev);
     // Waits for the stream. Inside a solver-pool fiber the wait yields to the
     // thread's other solves until the stream's work is done.
     void sync();
@@ -345,17 +383,27 @@ void launch_axpby(Ctx& ctx, double* y, double const* x, int64_t n, double a, dou
 void dots(Ctx& ctx, double const* const* V, int nv, double const* x, int64_t n, double* out);
 double dot(Ctx& ctx, double const* a, double const* b, int64_t n);
 double norm(Ctx& ctx, double const* a, int64_t n);
-// Up to MAX device vectors with coefficients, passed to kernels by value.
+// Up to MAX device vectors with coefficients, passed to kernels by value. A
+// coefficient is c[k], or c[k] times scalar slot cs[k] of the context when
+// cs[k] >= 0 (a value an earlier kernel left on the device).
 struct VecList {
     static constexpr int MAX = 24;
     double const* p[MAX];
     double c[MAX];
+    int cs[MAX];
     int n = 0;
-    void add(double const* x, double a) { p[n] = x; c[n] = a; ++n; }
+    void add(double const* x, double a, int slot = -1) { p[n] = x; c[n] = a; cs[n] = slot; ++n; }
 };
 // y = a0 y + sum_k c_k X_k in one launch (y is not read when a0 == 0); returns
 // |y|^2 when want_norm (then waits for the stream), else 0.
 double combo(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, bool want_norm);
+// The same without waiting: |y|^2 goes to scalar slot norm_slot (none if < 0).
+void combo_async(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, int norm_slot);
+// Dot products of x with each vector of V into scalar slots slot, slot+1, ...
+// (no wait; coefficients of V are ignored).
+void dots_async(Ctx& ctx, VecList const& V, double const* x, int64_t n, int slot);
+// x *= 1 / sqrt(max(s, 0)), s = scalar slot norm_slot (no wait).
+void scale_rnorm(Ctx& ctx, double* x, int64_t n, int norm_slot);
 // General block permute / gather: dst[dst_off[e]] = src[src_off[e]] described per
 // block by offset tables (see ops.cu). Used for combiner, uncombine and
 // layout changes.

@@ -150,16 +150,25 @@ double norm(Ctx& ctx, double const* a, int64_t n) {
 // optionally |y|^2: per-CTA partial sums in a fixed order, reduced by the last
 // CTA to finish (deterministic whichever CTA that is). Pointers and
 // coefficients travel as kernel parameters: no upload, one launch.
+// Coefficients may come from scalar slots `sd` (VecList::cs): c[k] * sd[cs[k]].
+// |y|^2 goes to `out` (and to `out2` when given).
 __global__ void combo_kernel(double* __restrict__ y, double a0, VecList X, int64_t n, int want_norm,
-                             double* __restrict__ part, unsigned int* __restrict__ counter, double* __restrict__ out) {
+                             double* __restrict__ part, unsigned int* __restrict__ counter, double* __restrict__ out,
+                             double* __restrict__ out2, double const* __restrict__ sd) {
     __shared__ double sh[32];
+    __shared__ double cf[VecList::MAX];
     __shared__ bool last;
+    if (threadIdx.x < X.n) {
+        const int k = threadIdx.x;
+        cf[k] = X.cs[k] >= 0 ? X.c[k] * sd[X.cs[k]] : X.c[k];
+    }
+    __syncthreads();
     double s2 = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double v = (a0 == 0.0) ? 0.0 : (a0 == 1.0 ? y[i] : a0 * y[i]);
         int k = 0;
-        if (a0 == 0.0 && X.n > 0) { v = X.c[0] * X.p[0][i]; k = 1; }
-        for (; k < X.n; ++k) v = fma(X.c[k], X.p[k][i], v);
+        if (a0 == 0.0 && X.n > 0) { v = cf[0] * X.p[0][i]; k = 1; }
+        for (; k < X.n; ++k) v = fma(cf[k], X.p[k][i], v);
         y[i] = v;
         s2 = fma(v, v, s2);
     }
@@ -181,6 +190,7 @@ __global__ void combo_kernel(double* __restrict__ y, double a0, VecList X, int64
         double t = 0;
         for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(part + b);
         *out = t;
+        if (out2) *out2 = t;
         *counter = 0;  // ready for the next launch on this stream
     }
 }
@@ -188,7 +198,8 @@ __global__ void combo_kernel(double* __restrict__ y, double a0, VecList X, int64
 // Dot products of x with every vector of V in one launch: partials per CTA in
 // a fixed order, the last CTA to finish reduces them in CTA order.
 __global__ void dots_fused_kernel(VecList V, double const* __restrict__ x, int64_t n, double* __restrict__ part,
-                                  unsigned int* __restrict__ counter, double* __restrict__ out) {
+                                  unsigned int* __restrict__ counter, double* __restrict__ out,
+                                  double* __restrict__ out2) {
     __shared__ double sh[32];
     __shared__ bool last;
     for (int v = 0; v < V.n; ++v) {
@@ -217,6 +228,7 @@ __global__ void dots_fused_kernel(VecList V, double const* __restrict__ x, int64
         double t = 0;
         for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(part + (size_t)v * gridDim.x + b);
         out[v] = t;
+        if (out2) out2[v] = t;
     }
     __syncthreads();
     if (threadIdx.x == 0) *counter = 0;  // ready for the next launch on this stream
@@ -238,11 +250,58 @@ void dots_fused(Ctx& ctx, VecList const& V, double const* x, int64_t n, double* 
     double* part = ctx.reduce_buf->as<double>();
     unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
-    dots_fused_kernel<<<nb, 256, 0, ctx.stream>>>(V, x, n, part, counter, static_cast<double*>(ctx.pin_dev));
+    dots_fused_kernel<<<nb, 256, 0, ctx.stream>>>(V, x, n, part, counter, static_cast<double*>(ctx.pin_dev), nullptr);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
     ctx.sync();
     std::memcpy(out, ctx.pin, sizeof(double) * V.n);
+}
+
+void Ctx::ensure_scalars() {
+    if (scal_host) return;
+    ITG_CHECK_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&scal_host), sizeof(double) * NSCALAR, cudaHostAllocMapped));
+    ITG_CHECK_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&scal_map), scal_host, 0));
+    scal_dev = dev_alloc(sizeof(double) * NSCALAR, stream);
+}
+
+void dots_async(Ctx& ctx, VecList const& V, double const* x, int64_t n, int slot) {
+    ITG_REQUIRE(slot >= 0 && slot + V.n <= Ctx::NSCALAR, "dots_async: scalar slots out of range");
+    if (V.n == 0) return;
+    ctx.ensure_reduce();
+    ctx.ensure_scalars();
+    double* part = ctx.reduce_buf->as<double>();
+    unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
+    dots_fused_kernel<<<nb, 256, 0, ctx.stream>>>(V, x, n, part, counter, ctx.scal_map + slot,
+                                                  ctx.scal_dev->as<double>() + slot);
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches++;
+}
+
+__global__ void scale_rnorm_kernel(double* x, int64_t n, double const* __restrict__ s) {
+    __shared__ double a;
+    if (threadIdx.x == 0) a = 1.0 / sqrt(fmax(*s, 0.0));
+    __syncthreads();
+    const double f = a;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] *= f;
+}
+
+void scale_rnorm(Ctx& ctx, double* x, int64_t n, int norm_slot) {
+    ITG_REQUIRE(norm_slot >= 0 && norm_slot < Ctx::NSCALAR, "scale_rnorm: scalar slot out of range");
+    if (n <= 0) return;
+    ctx.ensure_scalars();
+    scale_rnorm_kernel<<<grid_for(ctx, n), 256, 0, ctx.stream>>>(x, n, ctx.scal_dev->as<double>() + norm_slot);
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches++;
+}
+
+static bool uses_slots(VecList const& X) {
+    for (int k = 0; k < X.n; ++k)
+        if (X.cs[k] >= 0) {
+            ITG_REQUIRE(X.cs[k] < Ctx::NSCALAR, "combo: scalar slot out of range");
+            return true;
+        }
+    return false;
 }
 
 double combo(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, bool want_norm) {
@@ -250,16 +309,36 @@ double combo(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, bool w
     if (n <= 0) return 0.0;
     ctx.ensure_reduce();
     ctx.ensure_pin(sizeof(double));
+    if (uses_slots(X)) ctx.ensure_scalars();
     double* part = ctx.reduce_buf->as<double>();
     unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
     combo_kernel<<<nb, 256, 0, ctx.stream>>>(y, a0, X, n, want_norm ? 1 : 0, part, counter,
-                                             static_cast<double*>(ctx.pin_dev));
+                                             static_cast<double*>(ctx.pin_dev), nullptr,
+                                             ctx.scal_dev ? ctx.scal_dev->as<double>() : nullptr);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
     if (!want_norm) return 0.0;
     ctx.sync();
     return *static_cast<double*>(ctx.pin);
+}
+
+void combo_async(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, int norm_slot) {
+    ITG_REQUIRE(X.n >= 0 && X.n <= VecList::MAX, "combo: too many terms");
+    ITG_REQUIRE(norm_slot < Ctx::NSCALAR, "combo: scalar slot out of range");
+    if (n <= 0) return;
+    ctx.ensure_reduce();
+    ctx.ensure_scalars();
+    uses_slots(X);
+    double* part = ctx.reduce_buf->as<double>();
+    unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
+    const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
+    double* sd = ctx.scal_dev->as<double>();
+    combo_kernel<<<nb, 256, 0, ctx.stream>>>(y, a0, X, n, norm_slot >= 0 ? 1 : 0, part, counter,
+                                             norm_slot >= 0 ? ctx.scal_map + norm_slot : nullptr,
+                                             norm_slot >= 0 ? sd + norm_slot : nullptr, sd);
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches++;
 }
 
 // ------------------------------------------------------------------ gather
@@ -277,13 +356,11 @@ __global__ void gather_kernel(GatherItem const* __restrict__ items, int32_t cons
 void GatherPlan::upload(Ctx& ctx) {
     size_t o_items = 0, o_tab = ((sizeof(GatherItem) * std::max<size_t>(1, items.size()) + 15) / 16) * 16;
     size_t bytes = o_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size());
-    ctx.ensure_stage(bytes);
-    char* st = static_cast<char*>(ctx.stage);
+    char* st = ctx.stage_ring(bytes);
     if (!items.empty()) std::memcpy(st + o_items, items.data(), sizeof(GatherItem) * items.size());
     if (!tab.empty()) std::memcpy(st + o_tab, tab.data(), sizeof(int32_t) * tab.size());
     dev = dev_alloc(bytes, ctx.stream);
     ITG_CHECK_CUDA(cudaMemcpyAsync(dev->as<char>(), st, bytes, cudaMemcpyHostToDevice, ctx.stream));
-    ctx.sync();
     d_items = reinterpret_cast<GatherItem*>(dev->as<char>() + o_items);
     d_tab = reinterpret_cast<int32_t*>(dev->as<char>() + o_tab);
     nitems = (int)items.size();
@@ -345,13 +422,13 @@ void launch_noisy_rho(Ctx& ctx, std::vector<std::vector<NoiseBlock>> const& pass
     if (passes.empty() || passes[0].empty()) return;
     const size_t nb = passes[0].size(), pbytes = sizeof(NoiseBlock) * nb;
     const size_t bytes = pbytes * passes.size();
-    ctx.ensure_stage(bytes);
+    char* st = ctx.stage_ring(bytes);
     for (size_t k = 0; k < passes.size(); ++k) {
         ITG_REQUIRE(passes[k].size() == nb, "noisy_rho: passes over different block lists");
-        std::memcpy(static_cast<char*>(ctx.stage) + k * pbytes, passes[k].data(), pbytes);
+        std::memcpy(st + k * pbytes, passes[k].data(), pbytes);
     }
     DevBuf tab(bytes + 16, ctx.stream);
-    ITG_CHECK_CUDA(cudaMemcpyAsync(tab.as<char>(), ctx.stage, bytes, cudaMemcpyHostToDevice, ctx.stream));
+    ITG_CHECK_CUDA(cudaMemcpyAsync(tab.as<char>(), st, bytes, cudaMemcpyHostToDevice, ctx.stream));
     double* dtr = reinterpret_cast<double*>(tab.as<char>() + bytes);
     // pass 0: out = rho + noise (D_0 + D_0^T)/2; pass k: out += noise (D_k + D_k^T)/2 (in place)
     for (size_t k = 0; k < passes.size(); ++k) {
@@ -365,8 +442,6 @@ void launch_noisy_rho(Ctx& ctx, std::vector<std::vector<NoiseBlock>> const& pass
     trace_normalise_kernel<<<grid_for(ctx, out_size), 256, 0, ctx.stream>>>(out, out_size, dtr);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches += passes.size() + 2;
-    // the staging buffer is reused by the next upload: wait until the copy has read it
-    ctx.sync();
 }
 
 // Deterministic pseudo-random fill in [0,1) (splitmix64 of the element index

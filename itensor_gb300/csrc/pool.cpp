@@ -70,6 +70,16 @@ SolverPool::~SolverPool() {
     }
     cv_work_.notify_all();
     for (auto& t : threads_) t.join();
+    if (started_ && std::getenv("ITG_ALLOC_LOG"))
+        std::fprintf(stderr,
+                     "itg pool allocations: %llu from block caches, %llu driver allocations (%llu bypassing the caches, "
+                     "%llu on streams without one), %llu driver frees (%llu refused by a full cache)\n",
+                     (unsigned long long)(alloc_counters().cached.load() - alloc0_[0]),
+                     (unsigned long long)(alloc_counters().driver_allocs.load() - alloc0_[1]),
+                     (unsigned long long)(alloc_counters().bypass.load() - alloc0_[3]),
+                     (unsigned long long)(alloc_counters().nocache.load() - alloc0_[4]),
+                     (unsigned long long)(alloc_counters().driver_frees.load() - alloc0_[2]),
+                     (unsigned long long)(alloc_counters().full.load() - alloc0_[5]));
 }
 
 double SolverPool::now() const {
@@ -110,6 +120,12 @@ void SolverPool::start() {
         ITG_REQUIRE(!started_, "pool: already started");
         t0_ = std::chrono::steady_clock::now();
         started_ = true;
+        alloc0_[0] = alloc_counters().cached.load();
+        alloc0_[1] = alloc_counters().driver_allocs.load();
+        alloc0_[2] = alloc_counters().driver_frees.load();
+        alloc0_[3] = alloc_counters().bypass.load();
+        alloc0_[4] = alloc_counters().nocache.load();
+        alloc0_[5] = alloc_counters().full.load();
         init_pending_ = workers_;
     }
     for (int w = 0; w < workers_; ++w) threads_.emplace_back(&SolverPool::worker_main, this, w);
@@ -228,7 +244,6 @@ void SolverPool::worker_main(int w) {
         for (int i = 0; i < slots_; ++i) {
             auto s = std::make_unique<Slot>();
             s->ctx = std::make_unique<Ctx>(device_);
-            s->ctx->plans = plans_;
             s->ctx->ensure_pin(1 << 20);
             s->ctx->ensure_stage(8 << 20);
             slots.push_back(std::move(s));
@@ -245,6 +260,9 @@ void SolverPool::worker_main(int w) {
     cv_done_.notify_all();
     if (slots.empty()) return;
     FiberScheduler::of_thread() = &sched;
+    // freed blocks a slot keeps between its solves: an eighth of its share of
+    // the budget, at most 256 MiB (not counted against the budget)
+    const size_t retain = (size_t)std::min<int64_t>(int64_t(256) << 20, budget_ / (8 * (int64_t)workers_ * slots_));
     int idle_spins = 0;
     for (;;) {
         bool progressed = false;
@@ -257,7 +275,7 @@ void SolverPool::worker_main(int w) {
                     rec->worker = w;
                     rec->slot = i;
                     s.fiber.acct = std::make_shared<MemAccount>();
-                    s.fiber.cache = std::make_shared<BlockCache>(s.ctx->stream);
+                    s.fiber.cache = s.ctx->cache;  // the slot's cache, kept across its solves
                     Ctx* ctx = s.ctx.get();
                     SolveRecord* r = rec.get();
                     sched.start(s.fiber, [ctx, r, this] { run_solve(*ctx, *r, *this); });
@@ -272,7 +290,12 @@ void SolverPool::worker_main(int w) {
                 s.rec.reset();
                 s.fiber.acct.reset();
                 s.fiber.live_acct.reset();
-                if (s.fiber.cache) s.fiber.cache->release();  // blocks still held by the context return later
+                // the next solve on this slot reuses the freed blocks; what the cache
+                // keeps beyond the slot's share of the budget goes back to the driver
+                // plans are per slot (their tables are read on its stream only);
+                // a finished solve's plans rarely fit the next one
+                s.ctx->plans->clear();
+                if (s.fiber.cache) s.fiber.cache->trim(retain);
                 s.fiber.cache.reset();
                 s.fiber.live_cache.reset();
             }

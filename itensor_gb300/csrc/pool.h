@@ -77,9 +77,9 @@ public:
     ~SolverPool();
     int64_t submit(SolveRequest req);  // thread-safe, before or after start()
     void start();
-    // Cross-solve grouping (before start; on by default): the split-precision
-    // contractions that a worker's solves reach while all of them wait run as
-    // one grouped launch instead of one launch each.
+    // Cross-solve grouping (before start; off by default): the block GEMMs
+    // (FP64 or split precision) that a worker's solves reach while all of them
+    // wait run as one grouped launch instead of one launch each.
     void set_grouping(bool on);
     void drain();                      // blocks until every submitted request has finished
     SolveRecord record(int64_t id);
@@ -97,10 +97,9 @@ private:
     void finish(std::shared_ptr<SolveRecord> const& rec);
 
     int device_, workers_, slots_;
-    bool grouping_ = true;
+    bool grouping_ = false;
     std::atomic<int64_t> grouped_launches_{0}, grouped_contractions_{0};
     int64_t budget_;
-    std::shared_ptr<PlanCache> plans_ = std::make_shared<PlanCache>();
     std::mutex mu_;
     std::condition_variable cv_done_, cv_work_;
     std::deque<std::shared_ptr<SolveRecord>> queue_;        // by arrival time
@@ -108,6 +107,7 @@ private:
     PoolStats st_;
     bool started_ = false, stop_ = false;
     std::chrono::steady_clock::time_point t0_;
+    uint64_t alloc0_[6] = {0, 0, 0, 0, 0, 0};  // allocator counters at start (ITG_ALLOC_LOG)
     std::vector<std::thread> threads_;
     std::string init_error_;
     int init_pending_ = 0;

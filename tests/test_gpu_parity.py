@@ -348,6 +348,21 @@ def test_denmat_large_blocks(ctx, tri_min, monkeypatch):
         assert abs(nrm2 - np.sum(probs)) < 1e-10 * np.sum(probs)
 
 
+@pytest.mark.parametrize("pairs", ["0", "1000000"])
+def test_planners_agree(golden, pairs, monkeypatch):
+    """Every plan by the device planner (threshold 0), then every plan by the
+    host one: the contraction fixtures and a DMRG run match the reference
+    either way (block lists, offsets and index order exact)."""
+    import itensor_gb300 as itg
+    monkeypatch.setenv("ITG_HOST_PLAN_PAIRS", pairs)
+    c = itg.Context(0)  # a fresh plan cache
+    try:
+        test_contract_golden(c, golden, 0)
+        test_dmrg_golden(c, golden, "hubbard4x2")
+    finally:
+        c.close()
+
+
 @pytest.mark.parametrize("name", ["heis20", "hubbard4x2", "heis20_noise"])
 def test_dmrg_golden_tridiagonal_eigh(ctx, golden, name, monkeypatch):
     """Every density-matrix block through the tridiagonal path (down to 1x1)."""
