@@ -499,6 +499,26 @@ def run_profile_dmrg(args):
     return 0
 
 
+def run_profile_pool(args):
+    """A small pool for ncu's launch list: the first `--profile-pool` chains of
+    the batched set through the solver pool in plain FP64, one worker with
+    eight slots and cross-solve grouping on, so the grouped launches show."""
+    import itensor_gb300 as itg
+    chains = j1j2_chains(args.profile_pool)
+    pool = itg.Pool(0, workers=1, slots_per_worker=8, budget_bytes=8 << 30, grouping=True)
+    try:
+        ids = [pool.submit(m, sw, itg.PREC_F64) for m, sw in chains]
+        t0 = time.perf_counter()
+        pool.start()
+        pool.drain()
+        el = time.perf_counter() - t0
+        print(json.dumps({"solves": len(ids), "seconds": el, "grouping": pool.grouping_stats(),
+                          "failed": pool.stats()["failed"]}))
+    finally:
+        pool.close()
+    return 0
+
+
 def cylinder_sweeps(maxdim):
     """The sweep table of the reference's 2D Hubbard sample (sample/hubbard_2d.cc:43-46):
     maxdim 20, 60, 100, 100, 200, 400, 800, 2000, 3000 (capped at `maxdim`), noise
@@ -561,6 +581,8 @@ def run_profile(args):
     from itensor_gb300 import workloads
     ctx = itg.Context(0)
     ctx.set_precision(itg.PREC_OZAKI_BF16, args.slices)
+    if args.gemm_variant >= 0:
+        ctx.set_gemm_variant(args.gemm_variant)
     wl = workloads.heff_workload(M_BOND, K_SECT, SIGMA, SEED)
     dev = {k: workloads.to_device(ctx, wl[k]) for k in ("psi", "L", "W1", "W2", "R")}
     for prec in (itg.PREC_OZAKI_BF16, itg.PREC_F64):
@@ -590,6 +612,10 @@ def main():
                     help="profiling run for ncu: one J1-J2 chain N=48, J2=0.3, maxdim 64/128/256, split precision")
     ap.add_argument("--profile", type=int, default=0,
                     help="profiling run for ncu: N prepared applies per arithmetic, no graph, no timing")
+    ap.add_argument("--gemm-variant", type=int, default=-1,
+                    help="with --profile: force the split-precision GEMM variant (0..3 mma.sync, 4 tcgen05)")
+    ap.add_argument("--profile-pool", type=int, default=0,
+                    help="profiling run for ncu: this many chains through a one-worker pool with grouping on")
     ap.add_argument("--cylinder", type=int, default=0,
                     help="Hubbard 4x16 cylinder DMRG up to this maxdim (3000 in the workload), split and FP64")
     ap.add_argument("--cyl-runs", default="split,fp64", help="with --cylinder: which arithmetics to run")
@@ -600,6 +626,8 @@ def main():
         return run_reference(args)
     if args.profile:
         return run_profile(args)
+    if args.profile_pool:
+        return run_profile_pool(args)
     if args.profile_dmrg:
         return run_profile_dmrg(args)
     if args.cylinder:

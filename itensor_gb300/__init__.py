@@ -354,7 +354,7 @@ class Context:
         self._ok(lib().itg_set_precision(self.h, mode, slices), self.h)
 
     def set_gemm_variant(self, variant):
-        """-1: autotuned; 0..3: forced split-GEMM tile variant."""
+        """-1: autotuned; 0..3: forced mma.sync split-GEMM tile variant; 4: the tcgen05 kernel."""
         self._ok(lib().itg_set_gemm_variant(self.h, variant), self.h)
 
     def stats(self):

@@ -60,13 +60,63 @@ __device__ __forceinline__ void round_pair(int r, int k, int np, int& p, int& q)
     q = max(a, b);
 }
 
+// Rotation (c, s, t) that annihilates a_pq, or false when the pair is
+// skipped (|a_pq| <= max(1e-15 sqrt(|a_pp a_qq|), abs_floor)). t is the root
+// of smaller magnitude of a_pq t^2 + (a_qq - a_pp) t - a_pq = 0 (Golub & Van
+// Loan 8.4.2), c = 1/sqrt(1 + t^2), s = t c.
+//
+// fast: the dependent chain of one rotation holds no FP64 division or square
+// root (each a long sequence of dependent FP64 instructions, and FP64 issues
+// at about two per clock per SM here). The operands are scaled by a power of
+// two (exact) so that |a_pq| lies in [1, 2); t is seeded in FP32 and refined
+// by two Newton steps on the quadratic in FP64 with a fixed FP32 inverse
+// slope (relative error ~2^-22, then ~2^-44, then rounding); 1/sqrt(1 + t^2)
+// is seeded by the FP32 reciprocal square root and refined by two Newton
+// steps y <- y + y (1 - x y^2) / 2. The skip test compares squares in the
+// scaled units. Off: the textbook formulas with IEEE division and square root.
+__device__ __forceinline__ bool jacobi_pivot(double app, double aqq, double apq, double abs_floor, bool fast,
+                                             double& c, double& s, double& t) {
+    if (!(fabs(apq) > abs_floor)) return false;
+    const int ex = ((__double2hiint(apq) >> 20) & 0x7ff) - 1023;
+    if (fast && ex > -1000 && ex < 1000) {
+        const double sc = __hiloint2double((1023 - ex) << 20, 0);  // 2^-ex, exact
+        const double as = apq * sc, ds = (aqq - app) * sc;
+        if (!(as * as > 1e-30 * fabs((app * sc) * (aqq * sc)))) return false;
+        const float asf = (float)as, dsf = (float)ds;
+        const float tauf = dsf / (2.0f * asf);
+        const float t0 = copysignf(1.0f, tauf) / (fabsf(tauf) + sqrtf(fmaf(tauf, tauf, 1.0f)));
+        const double r = (double)(1.0f / fmaf(2.0f * asf, t0, dsf));
+        double tt = (double)t0;
+        double g = fma(fma(as, tt, ds), tt, -as);
+        tt = fma(-g, r, tt);
+        g = fma(fma(as, tt, ds), tt, -as);
+        tt = fma(-g, r, tt);
+        const double x = fma(tt, tt, 1.0);
+        double y = (double)rsqrtf((float)x);
+        double e = fma(-x * y, y, 1.0);
+        y = fma(0.5 * y, e, y);
+        e = fma(-x * y, y, 1.0);
+        y = fma(0.5 * y, e, y);
+        t = tt;
+        c = y;
+        s = tt * y;
+        return true;
+    }
+    if (!(fabs(apq) > 1e-15 * sqrt(fabs(app * aqq)))) return false;
+    const double tau = (aqq - app) / (2.0 * apq);
+    t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+    c = 1.0 / sqrt(1.0 + t * t);
+    s = t * c;
+    return true;
+}
+
 // Runs sweeps on the symmetric n x n matrix A (element (i,j) at A[j*lda+i]).
 // Rotations are accumulated into V (element (i,j) at V[j*ldv+i]) when V is
 // given, and logged as (c, s) per pair and round when rlog is given. Returns
 // the number of sweeps run; *converged tells whether the last one skipped
 // every pair.
 __device__ int jacobi_run(double* A, int lda, double* V, int ldv, double2* rlog, int n, int np, double abs_floor,
-                          JacobiShared sh, bool* converged) {
+                          bool fast, JacobiShared sh, bool* converged) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int half = np / 2;
     *converged = false;
@@ -82,13 +132,7 @@ __device__ int jacobi_run(double* A, int lda, double* V, int ldv, double2* rlog,
                 if (q < n) {
                     const double apq = A[(size_t)q * lda + p];
                     const double app = A[(size_t)p * lda + p], aqq = A[(size_t)q * lda + q];
-                    if (fabs(apq) > fmax(1e-15 * sqrt(fabs(app * aqq)), abs_floor)) {
-                        const double tau = (aqq - app) / (2.0 * apq);
-                        t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                        c = 1.0 / sqrt(1.0 + t * t);
-                        s = t * c;
-                        *sh.rotated = 1;
-                    }
+                    if (jacobi_pivot(app, aqq, apq, abs_floor, fast, c, s, t)) *sh.rotated = 1;
                 }
                 sh.cst[3 * k] = c;
                 sh.cst[3 * k + 1] = s;
@@ -172,7 +216,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigJob const* __res
                                                              double* __restrict__ vout, double* __restrict__ wout,
                                                              double* __restrict__ scratch, double2* __restrict__ rlog,
                                                              int* __restrict__ ranks, int* __restrict__ sweeps_out,
-                                                             int* __restrict__ status) {
+                                                             int* __restrict__ status, int fast) {
     extern __shared__ __align__(16) unsigned char eig_smem[];
     __shared__ int rotated;
     __shared__ double red[32];
@@ -215,7 +259,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigJob const* __res
     bool converged = true;
     int nsw = 0;
     if (n > 1)
-        nsw = jacobi_run(A, lda, V, n, logv ? rlog + it.r_off : nullptr, n, np, 0x1p-52 * normA,
+        nsw = jacobi_run(A, lda, V, n, logv ? rlog + it.r_off : nullptr, n, np, 0x1p-52 * normA, fast != 0,
                          JacobiShared{cst, pq, &rotated}, &converged);
     // eigenvalues descending (ties by position); eigenvector columns follow
     for (int i = tid; i < n; i += blockDim.x) {
@@ -323,8 +367,10 @@ void launch_eig(Ctx& ctx, int njobs, size_t smem, EigJob const* d_jobs, double c
                 double* scratch, double2* rlog, int* ranks, int* sweeps, int* d_stat) {
     if (smem > 48 * 1024)
         ITG_CHECK_CUDA(cudaFuncSetAttribute(jacobi_kernel<SA, SV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // ITG_EIG_IEEE_ROT: rotations by IEEE division and square root (diagnostics)
+    static const int fast = std::getenv("ITG_EIG_IEEE_ROT") ? 0 : 1;
     jacobi_kernel<SA, SV><<<njobs, EIG_THREADS, smem, ctx.stream>>>(d_jobs, src, vout, wout, scratch, rlog, ranks, sweeps,
-                                                                    d_stat);
+                                                                    d_stat, fast);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
