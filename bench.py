@@ -30,6 +30,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 M_BOND, K_SECT, SIGMA, SEED = 1024, 15, 6.0, 20241204
+# DRAM traffic of the dominant launches of this workload, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum; the outputs stay in L2): the
+# split form's psi*L prep + GEMM pair, and the plain FP64 psi*L GEMM
+PSI_L_SPLIT_DRAM_BYTES = 1671680 + 7174656
+PSI_L_F64_DRAM_BYTES = 3777280
 METRIC = "H_eff TFLOP/s (isolated apply, m=1024, 31 Sz sectors)"
 UNIT = "TFLOP/s"
 CONFIG = {"workload": "isolated H_eff apply: U(1) block-sparse L(m x 5 x m) W W R psi, m=1024 over 31 Sz "
@@ -730,7 +735,10 @@ def main():
     achieved = dm_flops / (dm_ms / 1e3) / 1e12
     nsl = args.slices * (args.slices + 1) // 2
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+                "frac": achieved / peaks["bf16_tflops"], "traffic": PSI_L_SPLIT_DRAM_BYTES,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the psi*L prep + GEMM "
+                                  "launches of this workload (profiles/heff_apply_m1024_launch_list.md), bytes "
+                                  "per launch pair",
                 "kernel": "ozaki_prep<%d> x2 + gemm_ozaki_kernel<%d> (psi*L block GEMM)" % (args.slices, args.slices),
                 "note": "achieved = algorithmic FP64-equivalent flops of the psi*L contraction / CUDA-event duration "
                         "of its launches (per-launch events, same steps as the timed region without graph replay); "
@@ -753,7 +761,9 @@ def main():
     f64_ach = d64_flops / (d64_ms / 1e3) / 1e12
     f64_peak = roofline.get("fp64_ffma_tflops_measured")
     f64_roofline = {"bound": "fp64", "achieved": f64_ach, "peak": f64_peak, "unit": "TFLOP/s",
-                    "frac": f64_ach / f64_peak if f64_peak else None, "traffic": None,
+                    "frac": f64_ach / f64_peak if f64_peak else None, "traffic": PSI_L_F64_DRAM_BYTES,
+                    "traffic_source": "ncu DRAM bytes of the psi*L gemm_f64_kernel launch of this workload "
+                                      "(profiles/heff_apply_m1024_launch_list.md)",
                     "kernel": "gemm_f64_kernel (psi*L block GEMM)",
                     "note": "peak = FP64 FFMA rate measured by itg_measure_peaks on this GPU (of measured)"}
 

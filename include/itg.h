@@ -348,6 +348,19 @@ int itg_pool_submit_mpo(itg_pool* p, itg_ctx* ctx, int32_t nsites, const itg_ten
  * they carried. */
 int itg_pool_set_grouping(itg_pool* p, int on);
 int itg_pool_grouping_stats(itg_pool* p, int64_t* grouped_launches, int64_t* grouped_contractions);
+/* No counterpart in the reference. Calibrated admission, set before
+ * itg_pool_start (off with min_solves 0, the default): once min_solves
+ * requests of a model family (model type, local and MPO bond dimensions,
+ * precision) have finished, that family's requests are admitted by
+ * estimate x safety x the largest measured peak/estimate ratio of the family
+ * (at least 16 MiB, at most the estimate; safety >= 1). A request admitted
+ * below its estimate that runs out of device memory is queued again, first in
+ * line, by its full estimate. itg_pool_record_admission gives the bytes a
+ * request was admitted by and whether it was re-run; itg_pool_calibration_stats
+ * counts calibrated admissions and re-runs. */
+int itg_pool_set_calibration(itg_pool* p, int32_t min_solves, double safety);
+int itg_pool_calibration_stats(itg_pool* p, int64_t* calibrated_admissions, int64_t* retried);
+int itg_pool_record_admission(itg_pool* p, int64_t id, double* admitted_bytes, int32_t* retries);
 int itg_pool_start(itg_pool* p);
 int itg_pool_drain(itg_pool* p);   /* waits until every submitted request has finished */
 /* status: -1 queued, -2 running, 0 done, else the request's error code (message in itg_pool_error).

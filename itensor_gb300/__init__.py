@@ -134,6 +134,9 @@ SIGNATURES = {
                                         _f64p]),
     "itg_pool_set_grouping": (C.c_int, [C.c_void_p, C.c_int]),
     "itg_pool_grouping_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "itg_pool_set_calibration": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),
+    "itg_pool_calibration_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "itg_pool_record_admission": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "itg_pool_start": (C.c_int, [C.c_void_p]),
     "itg_pool_drain": (C.c_int, [C.c_void_p]),
     "itg_pool_record": (C.c_int, [C.c_void_p, C.c_int64, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _i32p]),
@@ -684,6 +687,24 @@ class Pool:
         _check(lib().itg_pool_create(device, workers, slots_per_worker, float(budget_bytes), C.byref(h)))
         self.h = h
         _check(lib().itg_pool_set_grouping(self.h, int(grouping)))
+
+    def set_calibration(self, min_solves, safety=2.0):
+        """Calibrated admission (before start): after `min_solves` finished
+        requests of a model family, admit that family by estimate x safety x
+        the largest measured peak/estimate ratio; 0 turns it off."""
+        _check(lib().itg_pool_set_calibration(self.h, int(min_solves), float(safety)))
+
+    def calibration_stats(self):
+        """(calibrated admissions, re-runs after running out of memory)."""
+        a, b = C.c_int64(), C.c_int64()
+        _check(lib().itg_pool_calibration_stats(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def admission(self, i):
+        """(bytes the request was admitted by, re-runs)."""
+        a, r = C.c_double(), C.c_int32()
+        _check(lib().itg_pool_record_admission(self.h, i, C.byref(a), C.byref(r)))
+        return a.value, r.value
 
     def grouping_stats(self):
         """(grouped launches, contractions they carried)."""

@@ -801,6 +801,31 @@ int itg_pool_grouping_stats(itg_pool* p, int64_t* grouped_launches, int64_t* gro
     });
 }
 
+int itg_pool_set_calibration(itg_pool* p, int32_t min_solves, double safety) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p, "null pool");
+        p->pool.set_calibration(min_solves, safety);
+    });
+}
+
+int itg_pool_calibration_stats(itg_pool* p, int64_t* calibrated_admissions, int64_t* retried) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p, "null pool");
+        PoolStats s = p->pool.stats();
+        if (calibrated_admissions) *calibrated_admissions = s.calibrated;
+        if (retried) *retried = s.retried;
+    });
+}
+
+int itg_pool_record_admission(itg_pool* p, int64_t id, double* admitted_bytes, int32_t* retries) {
+    return guard(nullptr, [&] {
+        ITG_REQUIRE(p, "null pool");
+        SolveRecord r = p->pool.record(id);
+        if (admitted_bytes) *admitted_bytes = (double)r.adm_bytes;
+        if (retries) *retries = r.retries;
+    });
+}
+
 int itg_pool_start(itg_pool* p) {
     return guard(nullptr, [&] { ITG_REQUIRE(p, "null pool"); p->pool.start(); });
 }

@@ -10,10 +10,19 @@ int64_t solve_footprint_estimate(ModelSpec const& m, std::vector<SweepSpec> cons
     return solve_footprint_estimate(H.N, H.st.d(), mpo_bond_dim(H), sweeps, prec);
 }
 
-int64_t solve_footprint_estimate(SolveRequest const& r) {
-    if (!r.mpo) return solve_footprint_estimate(r.model, r.sweeps, r.prec);
-    const int N = (int)r.mpo->W.size();
-    int d = 1, D = 1;
+namespace {
+// Sites, local dimension and MPO bond dimension of a request.
+void request_dims(SolveRequest const& r, int& N, int& d, int& D) {
+    if (!r.mpo) {
+        Hamiltonian H = make_hamiltonian(r.model);
+        N = H.N;
+        d = H.st.d();
+        D = mpo_bond_dim(H);
+        return;
+    }
+    N = (int)r.mpo->W.size();
+    d = 1;
+    D = 1;
     for (int j = 0; j < N; ++j) {
         auto const& W = *r.mpo->W[j].lay;
         for (auto const& I : W.inds) {
@@ -23,6 +32,19 @@ int64_t solve_footprint_estimate(SolveRequest const& r) {
             else D = std::max<int>(D, (int)I.dim());
         }
     }
+}
+
+std::string request_family(SolveRequest const& r, int d, int D) {
+    return (r.mpo ? std::string("mpo") : "model" + std::to_string(r.model.type)) + ":d" + std::to_string(d) + ":D" +
+           std::to_string(D) + ":p" + std::to_string(r.prec);
+}
+
+bool out_of_memory(SolveRecord const& r) { return r.status == ERR_OOM; }
+}  // namespace
+
+int64_t solve_footprint_estimate(SolveRequest const& r) {
+    int N, d, D;
+    request_dims(r, N, d, D);
     return solve_footprint_estimate(N, d, D, r.sweeps, r.prec);
 }
 
@@ -89,7 +111,12 @@ double SolverPool::now() const {
 
 int64_t SolverPool::submit(SolveRequest req) {
     auto rec = std::make_shared<SolveRecord>();
-    rec->est_bytes = solve_footprint_estimate(req);
+    {
+        int N, d, D;
+        request_dims(req, N, d, D);
+        rec->est_bytes = solve_footprint_estimate(N, d, D, req.sweeps, req.prec);
+        rec->family = request_family(req, d, D);
+    }
     ITG_REQUIRE(!req.sweeps.empty(), "pool: empty sweep schedule");
     {
         std::lock_guard<std::mutex> g(mu_);
@@ -141,6 +168,14 @@ void SolverPool::start() {
     }
 }
 
+void SolverPool::set_calibration(int min_solves, double safety) {
+    std::lock_guard<std::mutex> g(mu_);
+    ITG_REQUIRE(!started_, "pool: calibration is set before start");
+    ITG_REQUIRE(min_solves >= 0 && safety >= 1.0, "pool: calibration needs min_solves >= 0 and safety >= 1");
+    cal_min_ = min_solves;
+    cal_safety_ = safety;
+}
+
 void SolverPool::set_grouping(bool on) {
     std::lock_guard<std::mutex> g(mu_);
     ITG_REQUIRE(!started_, "pool: grouping is set before start");
@@ -175,11 +210,21 @@ std::shared_ptr<SolveRecord> SolverPool::try_admit() {
     const double t = now();
     if (rec->t_arrive > t) return nullptr;
     // first come, first served: the head waits until its memory estimate fits
-    if (st_.running > 0 && st_.reserved_bytes + rec->est_bytes > budget_) return nullptr;
+    int64_t eff = rec->est_bytes;
+    if (cal_min_ > 0 && !rec->full_est) {
+        auto it = fam_.find(rec->family);
+        if (it != fam_.end() && it->second.second >= cal_min_) {
+            const double cal = (double)rec->est_bytes * it->second.first * cal_safety_;
+            eff = std::min<int64_t>(rec->est_bytes, std::max<int64_t>(int64_t(16) << 20, (int64_t)cal));
+        }
+    }
+    if (st_.running > 0 && st_.reserved_bytes + eff > budget_) return nullptr;
     queue_.pop_front();
     rec->t_admit = t;
     rec->status = -2;
-    st_.reserved_bytes += rec->est_bytes;
+    rec->adm_bytes = eff;
+    if (eff < rec->est_bytes) st_.calibrated++;
+    st_.reserved_bytes += eff;
     st_.peak_reserved_bytes = std::max(st_.peak_reserved_bytes, st_.reserved_bytes);
     st_.running++;
     st_.peak_running = std::max(st_.peak_running, st_.running);
@@ -189,10 +234,27 @@ std::shared_ptr<SolveRecord> SolverPool::try_admit() {
 void SolverPool::finish(std::shared_ptr<SolveRecord> const& rec) {
     {
         std::lock_guard<std::mutex> g(mu_);
-        st_.reserved_bytes -= rec->est_bytes;
+        st_.reserved_bytes -= rec->adm_bytes;
         st_.running--;
-        if (rec->status == 0) st_.done++;
-        else st_.failed++;
+        if (rec->status == 0) {
+            st_.done++;
+            if (rec->est_bytes > 0) {
+                auto& f = fam_[rec->family];
+                f.first = std::max(f.first, (double)rec->peak_bytes / (double)rec->est_bytes);
+                f.second++;
+            }
+        } else if (out_of_memory(*rec) && rec->adm_bytes < rec->est_bytes && rec->retries == 0) {
+            // admitted below its full estimate and out of memory: again, first in line, by the full estimate
+            rec->status = -1;
+            rec->error.clear();
+            rec->result = DmrgResult{};
+            rec->full_est = true;
+            rec->retries++;
+            st_.retried++;
+            queue_.push_front(rec);
+        } else {
+            st_.failed++;
+        }
     }
     cv_done_.notify_all();
     cv_work_.notify_all();

@@ -8,15 +8,16 @@
 // Each worker thread owns several slots; a slot is a context (its own stream)
 // and a fiber that runs the plain DMRG sweep loop (itensor/mps/dmrg.h:336-467).
 // While one solve waits for its stream the thread runs the others, so the
-// device sees the kernels of every admitted solve at once. All slots share
-// one plan cache: solves of the same model family reuse contraction plans.
-// A solve's result does not depend on what runs beside it: kernels are
-// deterministic and no state is shared between solves but read-only plans.
+// device sees the kernels of every admitted solve at once. Each slot keeps its
+// own contraction plans and freed device blocks (read and reused on its own
+// stream only). A solve's result does not depend on what runs beside it:
+// kernels are deterministic and solves share no device state.
 #pragma once
 #include "algo.h"
 #include "fiber.h"
 #include <condition_variable>
 #include <deque>
+#include <map>
 #include <thread>
 
 namespace itg {
@@ -49,6 +50,10 @@ struct SolveRecord {
     DmrgResult result;
     double t_arrive = 0, t_admit = 0, t_done = 0;   // seconds after the pool started
     int64_t est_bytes = 0, peak_bytes = 0;
+    int64_t adm_bytes = 0;       // what admission reserved (the estimate, or its calibrated form)
+    std::string family;          // model family and precision (calibration key)
+    bool full_est = false;       // admit by the full estimate (after an out-of-memory retry)
+    int retries = 0;
     int worker = -1, slot = -1;
 };
 
@@ -69,6 +74,8 @@ struct PoolStats {
     double elapsed = 0;          // seconds since start
     // grouped launches (split-precision prep + GEMM of several solves' contractions each)
     int64_t grouped_launches = 0, grouped_contractions = 0;
+    // admissions by a calibrated estimate; solves re-run after running out of memory
+    int64_t calibrated = 0, retried = 0;
 };
 
 class SolverPool {
@@ -81,6 +88,14 @@ public:
     // (FP64 or split precision) that a worker's solves reach while all of them
     // wait run as one grouped launch instead of one launch each.
     void set_grouping(bool on);
+    // Calibrated admission (before start; off with min_solves 0, the default).
+    // Once min_solves requests of a model family (model type, local and MPO
+    // bond dimensions, precision) have finished, the family's requests are
+    // admitted by estimate x safety x the largest measured peak/estimate ratio
+    // of that family (at least 16 MiB, at most the estimate). A solve admitted
+    // that way that runs out of device memory is queued again, first in line,
+    // with its full estimate.
+    void set_calibration(int min_solves, double safety);
     void drain();                      // blocks until every submitted request has finished
     SolveRecord record(int64_t id);
     PoolStats stats();
@@ -98,6 +113,9 @@ private:
 
     int device_, workers_, slots_;
     bool grouping_ = false;
+    int cal_min_ = 0;
+    double cal_safety_ = 2.0;
+    std::map<std::string, std::pair<double, int>> fam_;    // family -> (largest peak/estimate, finished)
     std::atomic<int64_t> grouped_launches_{0}, grouped_contractions_{0};
     int64_t budget_;
     std::mutex mu_;

@@ -161,3 +161,38 @@ def test_grouped_launches_across_solves_change_nothing():
     for a, b in zip(runs[False], runs[True]):
         assert a.energy == b.energy
         assert [x[3:] for x in a.bonds] == [x[3:] for x in b.bonds]
+
+
+@pytest.mark.gpu
+def test_calibrated_admission_packs_more_solves(ctx):
+    """Calibrated admission: with a budget that the dense estimate fills with
+    one solve, the first two solves of the family run one at a time; after
+    them the family is admitted by 2 x its measured peak/estimate ratio and
+    several run at once. Results stay identical to lone runs, and no solve
+    needs more than it was admitted by."""
+    # estimates of ~48 MiB, above the 16 MiB floor of a calibrated admission
+    sw = [dict(maxdim=m, mindim=1, cutoff=1e-10, niter=2) for m in (32, 64, 128, 128)]
+    models = [dict(type=0, N=32, J=1.0, Jz=0.6 + 0.1 * k) for k in range(10)]
+    est = max(itg.pool_estimate(m, sw) for m in models)
+    assert est > 32 << 20
+    pool = itg.Pool(0, workers=2, slots_per_worker=4, budget_bytes=int(1.5 * est))
+    pool.set_calibration(2, 2.0)
+    try:
+        ids = [pool.submit(m, sw, 0) for m in models]
+        pool.start()
+        pool.drain()
+        st = pool.stats()
+        assert st["done"] == len(models) and st["failed"] == 0
+        calibrated, retried = pool.calibration_stats()
+        assert calibrated >= len(models) - 2 and retried == 0
+        assert st["peak_running"] >= 2
+        assert st["peak_reserved_bytes"] <= int(1.5 * est)
+        for k, i in enumerate(ids):
+            rec = pool.record(i)
+            adm, reruns = pool.admission(i)
+            assert rec.status == 0 and reruns == 0
+            assert 0 < rec.peak_bytes <= adm <= rec.est_bytes
+            ref = ctx.dmrg(models[k], sw, precision=0)
+            assert abs(rec.energy - ref.energy) <= MIX_ENERGY_TOL
+    finally:
+        pool.close()
