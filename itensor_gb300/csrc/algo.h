@@ -85,8 +85,10 @@ struct HeffProgram {
     void run(Ctx& ctx, double const* in_ptr, double* out_ptr, bool host = false);
     void launch_steps(Ctx& ctx);
 };
+// fuse_mpo: contract the two MPO tensors once and run one MPO step per apply
+// (for programs applied many times; it is skipped where it costs more flops)
 std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shared_ptr<Layout> phi_layout, int prec,
-                                          bool into_phi_layout, bool use_graph);
+                                          bool into_phi_layout, bool use_graph, bool fuse_mpo = false);
 
 // davidson, block size 1 (itensor/iterativesolvers.h:99-451); phi is replaced by the
 // normalised lowest Ritz vector; returns the Ritz value.

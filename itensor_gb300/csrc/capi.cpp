@@ -378,7 +378,7 @@ int itg_heff_create(itg_ctx* c, const itg_tensor* L, const itg_tensor* W1, const
     return guard(c, [&] {
         ITG_REQUIRE(W1 && W2 && phi && out, "heff_create: null argument");
         LocalOp op{opt(L), &W1->t, &W2->t, opt(R)};
-        auto p = heff_prepare(c->ctx, op, phi->t.lay, precision, false, use_graph != 0);
+        auto p = heff_prepare(c->ctx, op, phi->t.lay, precision, false, use_graph != 0, true);
         *out = new itg_heff{p};
         if (out_size) *out_size = p->out_size;
         if (flops) *flops = p->flops;

@@ -528,8 +528,83 @@ __global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_kernel(const I
     }
 }
 
+// For skinny plans with few rows in all (too few 256-row tiles to fill the
+// SMs): a CTA takes 32 rows of one output block, and its eight warps take
+// every eighth block pair each (lane = row), so a thread's chain of dependent
+// loads covers an eighth of the pairs. The eight partial sums of an output are
+// added in warp order (deterministic).
+constexpr int WIDE_ROWS = 32, WIDE_WARPS = SKINNY_THREADS / 32;
+
+template <int NN>
+__device__ __forceinline__ void skinny_item_wide(ItemRec const& it, CBlockRec const& cb,
+                                                 const PairRec* __restrict__ pairs, const int32_t* __restrict__ tab,
+                                                 const double* __restrict__ A, const double* __restrict__ B,
+                                                 double* __restrict__ C, double (*part)[WIDE_ROWS][SKINNY_N]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int m = it.m0 + lane;
+    double acc[NN];
+#pragma unroll
+    for (int n = 0; n < NN; ++n) acc[n] = 0.0;
+    if (m < cb.M) {
+        for (int p = it.p0 + warp; p < it.p1; p += WIDE_WARPS) {
+            const PairRec pr = pairs[p];
+            const int arow = tab_at(tab, pr.tam, m);
+            int bcol[NN];
+#pragma unroll
+            for (int n = 0; n < NN; ++n) bcol[n] = tab_at(tab, pr.tbn, n);
+            for (int k = 0; k < pr.K; ++k) {
+                const int ko = tab_at(tab, pr.tak, k);
+                const int64_t bk = pr.boff + tab_at(tab, pr.tbk, k);
+                const double a = A[pr.aoff + arow + ko];
+#pragma unroll
+                for (int n = 0; n < NN; ++n) {
+                    const double b = __ldg(B + bk + bcol[n]);
+                    if (nonzero_bits(b)) acc[n] = fma(a, b, acc[n]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int n = 0; n < NN; ++n) part[warp][lane][n] = acc[n];
+    __syncthreads();
+    // thread t sums output (row t % 32, column t / 32) over the warps in order
+    const int row = threadIdx.x % WIDE_ROWS, n = threadIdx.x / WIDE_ROWS;
+    if (n < NN && it.m0 + row < cb.M) {
+        double v = part[0][row][n];
+        for (int w = 1; w < WIDE_WARPS; ++w) v += part[w][row][n];
+        C[cb.coff + tab_at(tab, cb.tcm, it.m0 + row) + tab_at(tab, cb.tcn, n)] = v;
+    }
+}
+
+__global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_wide_kernel(const ItemRec* __restrict__ items,
+                                                                              const PairRec* __restrict__ pairs,
+                                                                              const CBlockRec* __restrict__ cblk,
+                                                                              const int32_t* __restrict__ tab,
+                                                                              const double* __restrict__ A,
+                                                                              const double* __restrict__ B,
+                                                                              double* __restrict__ C) {
+    __shared__ double part[WIDE_WARPS][WIDE_ROWS][SKINNY_N];
+    const ItemRec it = items[blockIdx.x];
+    const CBlockRec cb = cblk[it.c];
+    switch (cb.N) {
+        case 1: skinny_item_wide<1>(it, cb, pairs, tab, A, B, C, part); break;
+        case 2: skinny_item_wide<2>(it, cb, pairs, tab, A, B, C, part); break;
+        case 3: skinny_item_wide<3>(it, cb, pairs, tab, A, B, C, part); break;
+        case 4: skinny_item_wide<4>(it, cb, pairs, tab, A, B, C, part); break;
+        case 5: skinny_item_wide<5>(it, cb, pairs, tab, A, B, C, part); break;
+        case 6: skinny_item_wide<6>(it, cb, pairs, tab, A, B, C, part); break;
+        case 7: skinny_item_wide<7>(it, cb, pairs, tab, A, B, C, part); break;
+        default: skinny_item_wide<8>(it, cb, pairs, tab, A, B, C, part); break;
+    }
+}
+
 // Launches the skinny kernel with the plan's rows per thread.
 static void launch_skinny(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C) {
+    if (p.skinny_wide) {
+        gemm_f64_skinny_wide_kernel<<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk,
+                                                                                 p.d_tab, A, B, C);
+        return;
+    }
     if (p.max_pair_K <= SKINNY_K) {
         switch (p.skinny_r) {
             case 1:
@@ -872,6 +947,83 @@ std::vector<int64_t> block_strides(Layout const& L, int b) {
 size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 }  // namespace
+
+void ensure_variant_tables(Ctx& ctx, Plan const& p) {
+    if (p.skinny || p.variants_ready.load(std::memory_order_acquire)) return;
+    std::lock_guard<std::mutex> g(p.vmu);
+    if (p.variants_ready.load(std::memory_order_relaxed)) return;
+    ITG_REQUIRE(p.vsrc, "plan: no source for the variant tile tables");
+    Plan::VariantSource const& v = *p.vsrc;
+    const int ncb = (int)v.cblk.size();
+    // 64-row tiles, most expensive first (stable, as the 32-row list)
+    std::vector<ItemRec> items64;
+    {
+        std::vector<ItemRec> raw;
+        std::vector<double> cost;
+        for (int c = 0; c < ncb; ++c)
+            for (int m0 = 0; m0 < v.cblk[c].M; m0 += 64)
+                for (int n0 = 0; n0 < v.cblk[c].N; n0 += GEMM_TILE) {
+                    raw.push_back(ItemRec{c, m0, n0, v.cp0[c], v.cp1[c]});
+                    cost.push_back(v.cost[c]);
+                }
+        std::vector<int> o(raw.size());
+        std::iota(o.begin(), o.end(), 0);
+        std::stable_sort(o.begin(), o.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+        for (int i : o) items64.push_back(raw[i]);
+    }
+    // tensor-core tiles: 128 rows along each block's longer side, TC_TILE_N
+    // columns along the other; the pairs seen from each block's rows and columns
+    std::vector<TcTile> items_tc;
+    std::vector<TcPair> pairs_tc(v.pia.size());
+    {
+        std::vector<TcTile> raw;
+        std::vector<double> cost;
+        for (int c = 0; c < ncb; ++c) {
+            CBlockRec const& cb = v.cblk[c];
+            const int swap = cb.N > cb.M ? 1 : 0;
+            const int R = swap ? cb.N : cb.M, W = swap ? cb.M : cb.N;
+            for (int q = v.cp0[c]; q < v.cp1[c]; ++q) {
+                OpBlockRec const& orow = v.ops[swap ? v.pib[q] : v.pia[q]];
+                OpBlockRec const& ocol = v.ops[swap ? v.pia[q] : v.pib[q]];
+                pairs_tc[q] = TcPair{orow.panel, ocol.panel, orow.exp, ocol.exp, panel_row_groups(orow.rows),
+                                     panel_row_groups(ocol.rows), orow.Kp / 16, 0};
+            }
+            for (int r0 = 0; r0 < R; r0 += TC_TILE_M)
+                for (int c0 = 0; c0 < W; c0 += TC_TILE_N) {
+                    raw.push_back(TcTile{cb.coff, swap ? cb.tcn : cb.tcm, swap ? cb.tcm : cb.tcn, R, W, r0, c0,
+                                         v.cp0[c], v.cp1[c], swap, 0});
+                    cost.push_back(v.cost[c]);
+                }
+        }
+        std::vector<int> o(raw.size());
+        std::iota(o.begin(), o.end(), 0);
+        std::stable_sort(o.begin(), o.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+        for (int i : o) items_tc.push_back(raw[i]);
+    }
+    const size_t t_i64 = 0, t_itc = align16(sizeof(ItemRec) * items64.size());
+    const size_t t_ptc = align16(t_itc + sizeof(TcTile) * items_tc.size());
+    const size_t bytes = align16(t_ptc + sizeof(TcPair) * std::max<size_t>(1, pairs_tc.size()));
+    // like the plan's own tables: the plan's memory, not the calling solve's
+    std::shared_ptr<MemAccount> saved = std::move(current_account());
+    current_account().reset();
+    DevBufPtr dev = dev_alloc(bytes, ctx.stream);
+    current_account() = std::move(saved);
+    char* st = ctx.stage_ring(bytes);
+    if (!items64.empty()) std::memcpy(st + t_i64, items64.data(), sizeof(ItemRec) * items64.size());
+    if (!items_tc.empty()) std::memcpy(st + t_itc, items_tc.data(), sizeof(TcTile) * items_tc.size());
+    if (!pairs_tc.empty()) std::memcpy(st + t_ptc, pairs_tc.data(), sizeof(TcPair) * pairs_tc.size());
+    ITG_CHECK_CUDA(cudaMemcpyAsync(dev->p, st, bytes, cudaMemcpyHostToDevice, ctx.stream));
+    ctx.sync();  // resident before any stream launches with them
+    char* db = dev->as<char>();
+    p.d_items64 = reinterpret_cast<ItemRec*>(db + t_i64);
+    p.nitems64 = (int)items64.size();
+    p.d_items_tc = reinterpret_cast<TcTile*>(db + t_itc);
+    p.d_pairs_tc = reinterpret_cast<TcPair*>(db + t_ptc);
+    p.nitems_tc = (int)items_tc.size();
+    p.dev_variants = std::move(dev);
+    p.vsrc.reset();
+    p.variants_ready.store(true, std::memory_order_release);
+}
 
 // Contractions with at most this many candidate block pairs are planned on
 // the host (plan_host); larger ones by plan_kernel. ITG_HOST_PLAN_PAIRS moves
@@ -1237,8 +1389,14 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
                 if (n_items >= 2 * (int64_t)ctx.sm_count) break;
                 plan->skinny_r /= 2;
             }
+            if (plan->skinny_r == 1 && plan->max_pair_K <= SKINNY_K && !std::getenv("ITG_SKINNY_NO_WIDE")) {
+                int64_t n_items = 0;
+                for (int c = 0; c < ncb; ++c) n_items += (cblk[c].M + SKINNY_THREADS - 1) / SKINNY_THREADS;
+                plan->skinny_wide = n_items < 2 * (int64_t)ctx.sm_count;
+            }
         }
-        const int tm = plan->skinny ? SKINNY_THREADS * plan->skinny_r : GEMM_TILE, tn = plan->skinny ? SKINNY_N : GEMM_TILE;
+        const int tm = plan->skinny_wide ? WIDE_ROWS : plan->skinny ? SKINNY_THREADS * plan->skinny_r : GEMM_TILE;
+        const int tn = plan->skinny ? SKINNY_N : GEMM_TILE;
         for (int c = 0; c < ncb; ++c)
             for (int m0 = 0; m0 < cblk[c].M; m0 += tm)
                 for (int n0 = 0; n0 < cblk[c].N; n0 += tn) {
@@ -1250,66 +1408,29 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });
         std::vector<ItemRec> sitems(items.size());
         for (size_t i = 0; i < ord.size(); ++i) sitems[i] = items[ord[i]];
-        // 64-row tiles for the wider split-precision variant, in the same cost order
-        std::vector<ItemRec> items64;
+        // the other split-precision tile shapes are built on first use from this
         if (!plan->skinny) {
-            std::vector<ItemRec> raw;
-            std::vector<double> cost64;
-            for (int c = 0; c < ncb; ++c)
-                for (int m0 = 0; m0 < cblk[c].M; m0 += 64)
-                    for (int n0 = 0; n0 < cblk[c].N; n0 += GEMM_TILE) {
-                        raw.push_back(ItemRec{c, m0, n0, cp0[c], cp1[c]});
-                        cost64.push_back(cK[c] + 1.0);
-                    }
-            std::vector<int> o64(raw.size());
-            std::iota(o64.begin(), o64.end(), 0);
-            std::stable_sort(o64.begin(), o64.end(), [&](int x, int y) { return cost64[x] > cost64[y]; });
-            for (int i : o64) items64.push_back(raw[i]);
-        }
-        // tensor-core tiles: 128 rows along each block's longer side, TC_TILE_N columns along the
-        // other; the pairs seen from each block's rows and columns
-        std::vector<TcTile> items_tc;
-        std::vector<TcPair> pairs_tc;
-        if (!plan->skinny) {
-            std::vector<TcTile> raw;
-            std::vector<double> ctc;
-            pairs_tc.resize(pairs.size());
-            for (int c = 0; c < ncb; ++c) {
-                const int swap = cblk[c].N > cblk[c].M ? 1 : 0;
-                const int R = swap ? cblk[c].N : cblk[c].M, W = swap ? cblk[c].M : cblk[c].N;
-                for (int q = cp0[c]; q < cp1[c]; ++q) {
-                    OpBlockRec const& orow = ops[swap ? pairs[q].ib : pairs[q].ia];
-                    OpBlockRec const& ocol = ops[swap ? pairs[q].ia : pairs[q].ib];
-                    pairs_tc[q] = TcPair{orow.panel, ocol.panel, orow.exp, ocol.exp, panel_row_groups(orow.rows),
-                                         panel_row_groups(ocol.rows), orow.Kp / 16, 0};
-                }
-                for (int r0 = 0; r0 < R; r0 += TC_TILE_M)
-                    for (int c0 = 0; c0 < W; c0 += TC_TILE_N) {
-                        raw.push_back(TcTile{cblk[c].coff, swap ? cblk[c].tcn : cblk[c].tcm,
-                                             swap ? cblk[c].tcm : cblk[c].tcn, R, W, r0, c0, cp0[c], cp1[c], swap, 0});
-                        ctc.push_back(cK[c] + 1.0);
-                    }
-            }
-            std::vector<int> otc(raw.size());
-            std::iota(otc.begin(), otc.end(), 0);
-            std::stable_sort(otc.begin(), otc.end(), [&](int x, int y) { return ctc[x] > ctc[y]; });
-            for (int i : otc) items_tc.push_back(raw[i]);
+            auto vs = std::make_shared<Plan::VariantSource>();
+            vs->cblk = cblk;
+            vs->cp0 = cp0;
+            vs->cp1 = cp1;
+            vs->cost.resize(ncb);
+            for (int c = 0; c < ncb; ++c) vs->cost[c] = cK[c] + 1.0;
+            vs->pia.resize(pairs.size());
+            vs->pib.resize(pairs.size());
+            for (size_t q = 0; q < pairs.size(); ++q) { vs->pia[q] = pairs[q].ia; vs->pib[q] = pairs[q].ib; }
+            vs->ops = ops;
+            plan->vsrc = std::move(vs);
         }
         // upload
         size_t t_items = 0, t_pairs = align16(sizeof(ItemRec) * sitems.size());
         size_t t_cblk = align16(t_pairs + sizeof(PairRec) * pairs.size());
         size_t t_ops = align16(t_cblk + sizeof(CBlockRec) * cblk.size());
         size_t t_prep = align16(t_ops + sizeof(OpBlockRec) * ops.size());
-        size_t t_i64 = align16(t_prep + sizeof(PrepItem) * prep.size());
-        size_t t_itc = align16(t_i64 + sizeof(ItemRec) * items64.size());
-        size_t t_ptc = align16(t_itc + sizeof(TcTile) * items_tc.size());
-        size_t t_tab = align16(t_ptc + sizeof(TcPair) * pairs_tc.size());
+        size_t t_tab = align16(t_prep + sizeof(PrepItem) * prep.size());
         size_t tbytes = align16(t_tab + sizeof(int32_t) * std::max<size_t>(1, tab.size()));
         char* st = ctx.stage_ring(tbytes);
         if (!sitems.empty()) std::memcpy(st + t_items, sitems.data(), sizeof(ItemRec) * sitems.size());
-        if (!items64.empty()) std::memcpy(st + t_i64, items64.data(), sizeof(ItemRec) * items64.size());
-        if (!items_tc.empty()) std::memcpy(st + t_itc, items_tc.data(), sizeof(TcTile) * items_tc.size());
-        if (!pairs_tc.empty()) std::memcpy(st + t_ptc, pairs_tc.data(), sizeof(TcPair) * pairs_tc.size());
         if (!pairs.empty()) std::memcpy(st + t_pairs, pairs.data(), sizeof(PairRec) * pairs.size());
         if (!cblk.empty()) std::memcpy(st + t_cblk, cblk.data(), sizeof(CBlockRec) * cblk.size());
         if (!ops.empty()) std::memcpy(st + t_ops, ops.data(), sizeof(OpBlockRec) * ops.size());
@@ -1332,11 +1453,6 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->d_ops = reinterpret_cast<OpBlockRec*>(db + t_ops);
         plan->d_prep = reinterpret_cast<PrepItem*>(db + t_prep);
         plan->d_tab = reinterpret_cast<int32_t*>(db + t_tab);
-        plan->d_items64 = reinterpret_cast<ItemRec*>(db + t_i64);
-        plan->nitems64 = (int)items64.size();
-        plan->d_items_tc = reinterpret_cast<TcTile*>(db + t_itc);
-        plan->d_pairs_tc = reinterpret_cast<TcPair*>(db + t_ptc);
-        plan->nitems_tc = (int)items_tc.size();
         plan->nitems = (int)sitems.size();
         plan->npairs = np;
         plan->ncblk = ncb;

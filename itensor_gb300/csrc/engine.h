@@ -119,6 +119,7 @@ struct Plan {
     bool scalar = false;             // rank-0 result
     bool skinny = false;             // every output block is <= 8 columns wide (row tiles)
     int skinny_r = 4;                // rows per thread of the skinny kernel (row tile = 256 * skinny_r)
+    bool skinny_wide = false;        // few rows: 32-row tiles, the block pairs spread over a CTA's warps
     // split-precision operand panels (A blocks, then B blocks)
     OpBlockRec* d_ops = nullptr;
     PrepItem* d_prep = nullptr;
@@ -127,18 +128,36 @@ struct Plan {
     int64_t panel_elems = 0;         // bf16 elements per digit plane set (all blocks)
     int64_t exp_elems = 0;
     int max_rows = 0;
+    // Tables of the other split-GEMM tile shapes, built on their first use
+    // (autotuning or a forced variant; ensure_variant_tables) from what the
+    // planner keeps here: most plans only ever run the 32 x 32 tiles.
+    struct VariantSource {
+        std::vector<CBlockRec> cblk;
+        std::vector<int> cp0, cp1;           // pair range of each output block
+        std::vector<double> cost;            // tile order key of each output block
+        std::vector<int> pia, pib;           // operand blocks of each pair
+        std::vector<OpBlockRec> ops;
+    };
+    mutable std::shared_ptr<VariantSource> vsrc;
+    mutable DevBufPtr dev_variants;
+    mutable std::mutex vmu;
+    mutable std::atomic<bool> variants_ready{false};
     // 64-row tiles of the same output blocks (the 64 x 32 split-precision variant)
-    ItemRec* d_items64 = nullptr;
-    int nitems64 = 0;
+    mutable ItemRec* d_items64 = nullptr;
+    mutable int nitems64 = 0;
     // 128 x TC_TILE_N tiles of the tensor-core (tcgen05) variant and its view of the pairs
-    TcTile* d_items_tc = nullptr;
-    TcPair* d_pairs_tc = nullptr;
-    int nitems_tc = 0;
+    mutable TcTile* d_items_tc = nullptr;
+    mutable TcPair* d_pairs_tc = nullptr;
+    mutable int nitems_tc = 0;
     // split-precision GEMM variant picked by the autotuner (-1: not tuned, run variant 0)
     mutable std::atomic<int> oz_variant{-1};
     // split-precision executions so far (a plan is tuned only once it is reused)
     mutable std::atomic<int> split_uses{0};
 };
+struct Ctx;
+// Builds and uploads the 64-row and tcgen05 tile tables of a plan if they are
+// not there yet (waits for the upload, so any stream may then use them).
+void ensure_variant_tables(Ctx& ctx, Plan const& p);
 
 // Plans keyed by block structure. One cache may serve several contexts (the
 // solver pool shares one across its slots): lookups and inserts are locked,

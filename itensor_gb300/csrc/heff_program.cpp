@@ -12,7 +12,7 @@ HeffProgram::~HeffProgram() {
 }
 
 std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shared_ptr<Layout> phi_layout, int prec,
-                                          bool into_phi_layout, bool use_graph) {
+                                          bool into_phi_layout, bool use_graph, bool fuse_mpo) {
     ITG_REQUIRE(op.W1 && op.W2 && phi_layout, "heff_prepare: missing operand");
     auto P = std::make_shared<HeffProgram>();
     P->prec = prec < 0 ? ctx.precision : prec;
@@ -40,6 +40,7 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
     // The layouts the reference's chain produces, step by step (plans only,
     // nothing runs): ((phi L) W1) W2 R. Their flops are the algorithmic work.
     std::vector<std::shared_ptr<Layout>> ref_out;
+    std::vector<double> ref_flops;
     {
         std::shared_ptr<Layout> cur = phi_layout;
         for (size_t s = 0; s < chain.size(); ++s) {
@@ -53,6 +54,7 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
                 for (int j : mt.b_unc) outL->inds.push_back(chain[s]->inds()[j]);
             }
             P->flops += plan->flops;
+            ref_flops.push_back(plan->flops);
             ref_out.push_back(outL);
             cur = outL;
         }
@@ -61,16 +63,31 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
     // from the right end), so an apply runs one MPO-tensor step instead of two
     // and one intermediate less goes through memory. That step writes the
     // layout the reference's second MPO step produces (same index order, same
-    // blocks), so everything after it is unchanged.
+    // blocks), so everything after it is unchanged. The fused step sums over
+    // both sites' indices and the outer MPO link at once, so its flops are about
+    // d/2 times those of the two steps it replaces (d the site dimension): it
+    // is taken only where it costs no more flops than they do (spin-1/2 models;
+    // not the Hubbard model's d = 4).
+    // Only a program made for many applies fuses (fuse_mpo): the fusion builds
+    // two plans the plain chain does not need, which the two or three applies
+    // of one Davidson call do not pay back.
     Tensor Wf;
     size_t wpos = 0;
-    for (size_t s = 0; s + 1 < chain.size(); ++s)
+    for (size_t s = 0; fuse_mpo && s + 1 < chain.size(); ++s)
         if ((chain[s] == op.W1 && chain[s + 1] == op.W2) || (chain[s] == op.W2 && chain[s + 1] == op.W1)) wpos = s + 1;
     if (wpos > 0) {
         Wf = contract(ctx, *chain[wpos - 1], *chain[wpos], PREC_F64);
-        chain.erase(chain.begin() + (long)wpos);
-        chain[wpos - 1] = &Wf;
-        ref_out.erase(ref_out.begin() + (long)(wpos - 1));  // the fused step writes the second step's layout
+        std::shared_ptr<Layout> in = wpos >= 2 ? ref_out[wpos - 2] : phi_layout;
+        Match mf = match_indices(in->inds, Wf.inds());
+        const bool last = (wpos + 1 == chain.size());
+        auto pf = get_plan(ctx, *in, *Wf.lay, mf, (last && target) ? target : ref_out[wpos]);
+        if (pf->flops <= 1.05 * (ref_flops[wpos - 1] + ref_flops[wpos])) {
+            chain.erase(chain.begin() + (long)wpos);
+            chain[wpos - 1] = &Wf;
+            ref_out.erase(ref_out.begin() + (long)(wpos - 1));  // the fused step writes the second step's layout
+        } else {
+            wpos = 0;
+        }
     }
     std::shared_ptr<Layout> cur = phi_layout;
     for (size_t s = 0; s < chain.size(); ++s) {

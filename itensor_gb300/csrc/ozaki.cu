@@ -459,6 +459,7 @@ void launch_tc(Ctx& ctx, Plan const& p, double* C, __nv_bfloat16 const* panels, 
 template <int S>
 void launch_variant(Ctx& ctx, Plan const& p, int v, double* C, __nv_bfloat16 const* panels, int64_t plane,
                     int32_t const* exps) {
+    if (v == 1 || v == 3 || v == 4) ensure_variant_tables(ctx, p);  // 64-row or tcgen05 tiles
     switch (v) {
         case 4: launch_tc<S>(ctx, p, C, panels, plane, exps); break;
         case 1: launch_gemm<S, 4, false>(ctx, p, C, panels, plane, exps); break;
