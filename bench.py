@@ -768,8 +768,10 @@ def main():
                     "note": "peak = FP64 FFMA rate measured by itg_measure_peaks on this GPU (of measured)"}
 
     # end-to-end through the C-ABI with host buffers: psi host -> device, apply, result -> host
-    psi_host = np.ascontiguousarray(wl["psi"]["data"])
-    out_host = np.empty(out_n)
+    # (pinned host memory, as a caller that streams states through the apply would hold them)
+    psi_pin = torch.from_numpy(np.ascontiguousarray(wl["psi"]["data"])).pin_memory()
+    out_pin = torch.empty(out_n, dtype=torch.float64).pin_memory()
+    psi_host, out_host = psi_pin.numpy(), out_pin.numpy()
     he = H[(itg.PREC_OZAKI_BF16, True)]
     e2e_t = 0.0
     for i in range(args.warmup + args.steps):
@@ -794,7 +796,7 @@ def main():
     e2e = {"value": flops_apply * args.steps / e2e_t / 1e12, "unit": UNIT,
            "h2d_bytes_per_step": int(8 * psi_host.size), "d2h_bytes_per_step": int(8 * out_n),
            "ms_per_step": e2e_t / args.steps * 1e3,
-           "api": "itg_heff_run(host=1): host psi -> device, graph-replayed apply, result -> host",
+           "api": "itg_heff_run(host=1): pinned host psi -> device, graph-replayed apply, result -> pinned host",
            "unprepared_call": {"value": flops_apply * args.steps / e2u_t / 1e12,
                                "ms_per_step": e2u_t / args.steps * 1e3,
                                "api": "itg_tensor_create(host data) + itg_heff_apply + itg_tensor_read"}}

@@ -1364,6 +1364,11 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         // prep items: one row group of the tiled panel (8 rows, whole rows so the
         // row exponents are complete) each, one warp per item; A's items first
         std::vector<PrepItem> prep;
+        {
+            size_t np8 = 0;
+            for (auto const& op8 : ops) np8 += (size_t)(op8.rows + 7) / 8;
+            prep.reserve(np8);
+        }
         for (int o = 0; o < (int)ops.size(); ++o) {
             const int rows = ops[o].rows;
             for (int r0 = 0; r0 < rows; r0 += 8)

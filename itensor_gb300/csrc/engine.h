@@ -174,7 +174,14 @@ struct PlanCache {
     };
     Shard shard[NSHARD];
     size_t limit = 32768;       // plans in all shards together
-    Shard& of(std::string const& key) { return shard[std::hash<std::string>{}(key) % NSHARD]; }
+    // the shard from the key's length and a sample of its bytes (keys run to
+    // tens of kilobytes; the map hashes the whole key once more itself)
+    Shard& of(std::string const& key) {
+        uint64_t h = key.size() * 0x9E3779B97F4A7C15ull;
+        const size_t step = key.size() / 16 + 1;
+        for (size_t i = 0; i < key.size(); i += step) h = (h ^ (unsigned char)key[i]) * 0x100000001B3ull;
+        return shard[(h >> 7) % NSHARD];
+    }
     std::shared_ptr<Plan> find(std::string const& key) {
         Shard& s = of(key);
         std::shared_lock<std::shared_mutex> g(s.mu);

@@ -41,6 +41,7 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
     // nothing runs): ((phi L) W1) W2 R. Their flops are the algorithmic work.
     std::vector<std::shared_ptr<Layout>> ref_out;
     std::vector<double> ref_flops;
+    std::vector<std::shared_ptr<Plan>> ref_plans;  // reused below when the chain runs as it is
     {
         std::shared_ptr<Layout> cur = phi_layout;
         for (size_t s = 0; s < chain.size(); ++s) {
@@ -55,6 +56,7 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
             }
             P->flops += plan->flops;
             ref_flops.push_back(plan->flops);
+            ref_plans.push_back(plan);
             ref_out.push_back(outL);
             cur = outL;
         }
@@ -94,7 +96,10 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
         const bool last = (s + 1 == chain.size());
         Match mt = match_indices(cur->inds, chain[s]->inds());
         const bool fused = wpos > 0 && s == wpos - 1;
-        auto plan = get_plan(ctx, *cur, *chain[s]->lay, mt, (last && target) ? target : (fused ? ref_out[s] : nullptr));
+        // unfused, step s is the reference chain's step s: its plan is already resolved
+        auto plan = wpos == 0 ? ref_plans[s]
+                              : get_plan(ctx, *cur, *chain[s]->lay, mt,
+                                         (last && target) ? target : (fused ? ref_out[s] : nullptr));
         std::shared_ptr<Layout> outL;
         if (last && target) {
             outL = target;
