@@ -1268,6 +1268,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
                 nat2t[c] = tb;
             }
         }
+        const auto pq_map = std::chrono::steady_clock::now();
         // ---- tables
         std::vector<int32_t> tab;
         std::vector<int> tamA(nA, -1), takA(nA, -1), tbkB(nB, -1), tbnB(nB, -1);
@@ -1334,7 +1335,13 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             maxK = std::max(maxK, ksum);
             sumK += ksum;
         }
+        const auto pq_pairs = std::chrono::steady_clock::now();
+        // narrow outputs (N <= SKINNY_N) make a skinny plan: row tiles, FP64 only
+        int maxN = 0;
+        for (int c = 0; c < ncb; ++c) maxN = std::max(maxN, cblk[c].N);
+        plan->skinny = (maxN <= SKINNY_N);
         // operand panels for the split-precision path: every A and B block in use
+        // (a skinny plan never takes that path and builds none)
         std::vector<OpBlockRec> ops;
         std::vector<int> ia_of(nA, -1), ib_of(nB, -1);
         int64_t panel = 0, expo = 0;
@@ -1356,10 +1363,12 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             return r;
         };
         for (int ab = 0; ab < nA; ++ab)
-            if (tamA[ab] >= 0) ia_of[ab] = add_op(A.offs[ab], rows_of(A, ab, mt.a_unc), rows_of(A, ab, mt.a_con), tamA[ab], takA[ab]);
+            if (!plan->skinny && tamA[ab] >= 0)
+                ia_of[ab] = add_op(A.offs[ab], rows_of(A, ab, mt.a_unc), rows_of(A, ab, mt.a_con), tamA[ab], takA[ab]);
         const int nopsA = (int)ops.size();
         for (int bb = 0; bb < nB; ++bb)
-            if (tbkB[bb] >= 0) ib_of[bb] = add_op(B.offs[bb], rows_of(B, bb, mt.b_unc), rows_of(B, bb, mt.b_con), tbnB[bb], tbkB[bb]);
+            if (!plan->skinny && tbkB[bb] >= 0)
+                ib_of[bb] = add_op(B.offs[bb], rows_of(B, bb, mt.b_unc), rows_of(B, bb, mt.b_con), tbnB[bb], tbkB[bb]);
         const int nopsB = (int)ops.size() - nopsA;
         // prep items: one row group of the tiled panel (8 rows, whole rows so the
         // row exponents are complete) each, one warp per item; A's items first
@@ -1379,10 +1388,8 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             for (int c = 0; c < ncb; ++c)
                 for (int p : bypc[c]) { pairs[q].ia = ia_of[pa[p]]; pairs[q].ib = ib_of[pb[p]]; ++q; }
         }
-        // tiles, most expensive first; narrow outputs (N <= SKINNY_N) get row tiles
-        int maxN = 0;
-        for (int c = 0; c < ncb; ++c) maxN = std::max(maxN, cblk[c].N);
-        plan->skinny = (maxN <= SKINNY_N);
+        const auto pq_ops = std::chrono::steady_clock::now();
+        // tiles, most expensive first; a skinny plan gets row tiles
         std::vector<ItemRec> items;
         std::vector<double> cost;
         if (plan->skinny) {
@@ -1413,6 +1420,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });
         std::vector<ItemRec> sitems(items.size());
         for (size_t i = 0; i < ord.size(); ++i) sitems[i] = items[ord[i]];
+        const auto pq_items = std::chrono::steady_clock::now();
         // the other split-precision tile shapes are built on first use from this
         if (!plan->skinny) {
             auto vs = std::make_shared<Plan::VariantSource>();
@@ -1427,6 +1435,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
             vs->ops = ops;
             plan->vsrc = std::move(vs);
         }
+        const auto pq_vsrc = std::chrono::steady_clock::now();
         // upload
         size_t t_items = 0, t_pairs = align16(sizeof(ItemRec) * sitems.size());
         size_t t_cblk = align16(t_pairs + sizeof(PairRec) * pairs.size());
@@ -1467,9 +1476,12 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->avgK = ncb ? sumK / ncb : 0;
         if (plan_timing) {
             auto pt2 = std::chrono::steady_clock::now();
-            std::fprintf(stderr, "itg plan: nA %d nB %d pairs %d C %d device %.3f ms host %.3f ms\n", nA, nB, np, nc,
-                         std::chrono::duration<double, std::milli>(pt1 - pt0).count(),
-                         std::chrono::duration<double, std::milli>(pt2 - pt1).count());
+            auto ms = [](auto a, auto b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+            std::fprintf(stderr,
+                         "itg plan: nA %d nB %d pairs %d C %d device %.3f ms host %.3f ms (block map %.3f, offset "
+                         "tables and pairs %.3f, operand panels %.3f, tiles %.3f, variant source %.3f, upload %.3f)\n",
+                         nA, nB, np, nc, ms(pt0, pt1), ms(pt1, pt2), ms(pt1, pq_map), ms(pq_map, pq_pairs),
+                         ms(pq_pairs, pq_ops), ms(pq_ops, pq_items), ms(pq_items, pq_vsrc), ms(pq_vsrc, pt2));
         }
     } else {
         // an empty operand: the output has no blocks (or is the scalar 0)
