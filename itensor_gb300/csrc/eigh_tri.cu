@@ -66,6 +66,26 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// sum_i x[i] y[i] over i = i0, i0 + step, ... < n with four independent
+// accumulators (a single chain of dependent FP64 FMAs leaves the FP64 pipe
+// mostly idle: each FMA waits for the previous one), added in a fixed order.
+__device__ __forceinline__ double dot4(double const* __restrict__ x, double const* __restrict__ y, int i0, int n,
+                                       int step) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int i = i0;
+    const int step4 = 4 * step;
+    for (; i + 3 * step < n; i += step4) {
+        double const* xp = x + i;
+        double const* yp = y + i;
+        a0 = fma(xp[0], yp[0], a0);
+        a1 = fma(xp[step], yp[step], a1);
+        a2 = fma(xp[2 * step], yp[2 * step], a2);
+        a3 = fma(xp[3 * step], yp[3 * step], a3);
+    }
+    for (; i < n; i += step) a0 = fma(x[i], y[i], a0);
+    return (a0 + a1) + (a2 + a3);
+}
+
 // Sum over the CTA (a fixed tree: lanes, then the warps' sums); every thread
 // gets the same value. The warps' sums are combined by shuffles, not by a
 // serial loop in every warp: each FP64 instruction costs a warp tens of cycles.
@@ -87,8 +107,7 @@ __device__ void tri_reflector(int k, int n, double* A, double* d, double* e, dou
     __shared__ double sc[3];   // beta, tau, 1 / (alpha - beta): computed once, by thread 0
     double* col = A + (size_t)k * n;
     const double alpha = col[k + 1];
-    double ss = 0.0;
-    for (int i = k + 2 + threadIdx.x; i < n; i += blockDim.x) ss = fma(col[i], col[i], ss);
+    double ss = dot4(col, col, k + 2 + threadIdx.x, n, blockDim.x);
     ss = cta_sum(ss, red);
     if (threadIdx.x == 0) {
         double t = 0.0, beta = alpha, scal = 0.0;
@@ -116,7 +135,7 @@ __device__ void tri_reflector(int k, int n, double* A, double* d, double* e, dou
     }
 }
 
-__global__ void __launch_bounds__(TRI_THREADS) tri_reduce_kernel(TriJob const* __restrict__ jobs,
+__global__ void __launch_bounds__(TRI_THREADS, 1) tri_reduce_kernel(TriJob const* __restrict__ jobs,
                                                                  double const* __restrict__ src,
                                                                  double* __restrict__ scratch,
                                                                  double* __restrict__ aux) {
@@ -151,11 +170,27 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_reduce_kernel(TriJob const* _
         __syncthreads();
         double mine = 0.0;
         if (tk != 0.0) {
-            for (int j = j0 + warp * C; j < n; j += nw * C) {
-                double const* col = A + (size_t)j * n;
-                double acc = 0.0;
-                for (int i = k + 1 + lane; i < n; i += 32) acc = fma(col[i], vs[i], acc);
-                const double pj = tk * warp_sum(acc);
+            // two columns at a time: their dot products and warp reductions
+            // interleave (each reduction is a chain of dependent shuffles and adds)
+            const int js = nw * C;
+            int j = j0 + warp * C;
+            for (; j + js < n; j += 2 * js) {
+                double s1 = dot4(A + (size_t)j * n, vs, k + 1 + lane, n, 32);
+                double s2 = dot4(A + (size_t)(j + js) * n, vs, k + 1 + lane, n, 32);
+                for (int o = 16; o > 0; o >>= 1) {
+                    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+                    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+                }
+                if (lane == 0) {
+                    const double p1 = tk * s1, p2 = tk * s2;
+                    __stcg(pg + j, p1);
+                    mine = fma(p1, vs[j], mine);
+                    __stcg(pg + j + js, p2);
+                    mine = fma(p2, vs[j + js], mine);
+                }
+            }
+            if (j < n) {
+                const double pj = tk * warp_sum(dot4(A + (size_t)j * n, vs, k + 1 + lane, n, 32));
                 if (lane == 0) {
                     __stcg(pg + j, pj);
                     mine = fma(pj, vs[j], mine);
@@ -175,6 +210,7 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_reduce_kernel(TriJob const* _
             for (int j = j0 + warp * C; j < n; j += nw * C) {
                 double* col = A + (size_t)j * n;
                 const double vj = vs[j], wj = ws[j];
+#pragma unroll 4
                 for (int i = k + 1 + lane; i < n; i += 32) col[i] = fma(-vs[i], wj, fma(-ws[i], vj, col[i]));
             }
         }
@@ -222,11 +258,10 @@ __global__ void __launch_bounds__(TRI_APPLYQ_WARPS * 32) tri_applyq_kernel(ColJo
         const double t = tau[k];
         if (t == 0.0) continue;
         double const* v = Rf + (size_t)k * n;
-        double acc = 0.0;
-        for (int i = k + 2 + lane; i < n; i += 32) acc = fma(v[i], y[i], acc);
-        const double dt = t * (warp_sum(acc) + y[k + 1]);
+        const double dt = t * (warp_sum(dot4(v, y, k + 2 + lane, n, 32)) + y[k + 1]);
         __syncwarp();
         if (lane == 0) y[k + 1] -= dt;
+#pragma unroll 4
         for (int i = k + 2 + lane; i < n; i += 32) y[i] = fma(-dt, v[i], y[i]);
         __syncwarp();
     }
@@ -628,6 +663,8 @@ void tri_eigh_finish(Ctx& ctx, TriPending& P, std::vector<int> const& keep, doub
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;
     }
+    if (timing) ctx.sync();
+    auto t1b = std::chrono::steady_clock::now();
     // 2. back to the block's basis: the Householder reflectors applied to each kept column
     {
         const size_t smem = sizeof(double) * TRI_APPLYQ_WARPS * (size_t)P.nmax;
@@ -644,9 +681,10 @@ void tri_eigh_finish(Ctx& ctx, TriPending& P, std::vector<int> const& keep, doub
         auto t2 = std::chrono::steady_clock::now();
         size_t kept = 0, tot = 0;
         for (int b = 0; b < nj; ++b) { kept += P.jobs[b].keep; tot += items[b].n; }
-        std::fprintf(stderr, "itg tri finish (ms): host %.3f device %.3f; kept %zu of %zu\n",
+        std::fprintf(stderr, "itg tri finish (ms): host %.3f device %.3f (rotations %.3f); kept %zu of %zu\n",
                      std::chrono::duration<double, std::milli>(t1 - t0).count(),
-                     std::chrono::duration<double, std::milli>(t2 - t1).count(), kept, tot);
+                     std::chrono::duration<double, std::milli>(t2 - t1).count(),
+                     std::chrono::duration<double, std::milli>(t1b - t1).count(), kept, tot);
     }
 }
 
