@@ -35,6 +35,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <unistd.h>
 #include <thread>
 
 namespace cg = cooperative_groups;
@@ -386,23 +390,91 @@ struct TriPending {
 void TriPendingFree::operator()(TriPending* p) const { delete p; }
 
 namespace {
-// Runs f(b) for b < n on the calling thread, or on up to 8 host threads when the
-// work is large and the caller is not a solver-pool fiber (whose workers already
-// run one solve each).
+// Persistent host threads for the per-block host stages (the QL recurrence,
+// the rotation schedules). One caller at a time uses them; a caller that
+// finds them busy runs its blocks itself. Spawning threads per bond split
+// cost about 0.5 ms each time.
+class HostPool {
+public:
+    static HostPool& get() {
+        static HostPool p;
+        return p;
+    }
+    // Runs f(b) for every b < n on the pool and the calling thread; false if
+    // the pool is busy (nothing ran).
+    bool run(int n, std::function<void(int)> const& f) {
+        // (a forked child has none of the parent's threads)
+        if (getpid() != pid_) return false;
+        std::unique_lock<std::mutex> busy(use_, std::try_to_lock);
+        if (!busy.owns_lock() || threads_.empty()) return false;
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            job_ = &f;
+            n_ = n;
+            next_.store(0);
+            pending_ = (int)threads_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> g(mu_);
+        done_.wait(g, [&] { return pending_ == 0; });
+        job_ = nullptr;
+        return true;
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : threads_) t.join();
+    }
+
+private:
+    HostPool() : pid_(getpid()) {
+        const unsigned hc = std::thread::hardware_concurrency();
+        const int nt = std::max(0, std::min(15, (int)hc - 1));
+        for (int t = 0; t < nt; ++t) threads_.emplace_back([this] { loop(); });
+    }
+    void work() {
+        for (int b; (b = next_.fetch_add(1)) < n_;) (*job_)(b);
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> g(mu_);
+                cv_.wait(g, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+            }
+            work();
+            std::lock_guard<std::mutex> g(mu_);
+            if (--pending_ == 0) done_.notify_all();
+        }
+    }
+    std::vector<std::thread> threads_;
+    std::mutex use_, mu_;
+    std::condition_variable cv_, done_;
+    std::function<void(int)> const* job_ = nullptr;
+    std::atomic<int> next_{0};
+    int n_ = 0, pending_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+    pid_t pid_;
+};
+
+// Runs f(b) for b < n on the calling thread, or on the host pool as well when
+// the work is large and the caller is not a solver-pool fiber (whose workers
+// already run one solve each).
 template <typename F>
 void for_blocks(int n, double work, F const& f) {
-    const int nthreads = (!fiber_active() && work > 2e5) ? std::min<int>(n, 8) : 1;
-    if (nthreads > 1) {
-        std::atomic<int> next{0};
-        std::vector<std::thread> pool;
-        for (int t = 0; t < nthreads; ++t)
-            pool.emplace_back([&] {
-                for (int b; (b = next.fetch_add(1)) < n;) f(b);
-            });
-        for (auto& t : pool) t.join();
-    } else {
-        for (int b = 0; b < n; ++b) f(b);
+    if (n > 1 && !fiber_active() && work > 2e5) {
+        std::function<void(int)> fn = [&](int b) { f(b); };
+        if (HostPool::get().run(n, fn)) return;
     }
+    for (int b = 0; b < n; ++b) f(b);
 }
 size_t a16(size_t x) { return (x + 15) / 16 * 16; }
 }  // namespace
