@@ -95,10 +95,10 @@ int main() {
                 worst_res = std::max(worst_res, std::fabs(ty - d[j] * Z[(size_t)c * n + j]));
             }
         // 2. lockstep schedules
+        for (int W : {8, 16})
         for (int K : {1, 4, 8}) {
             std::vector<int32_t> woff;
             std::vector<QlStart> ent;
-            const int W = 8;
             const int nsteps = ql_schedule(n, sw, W, K, woff, ent);
             for (bool rev : {false, true}) {
                 std::vector<double> Y((size_t)n * n, 0.0);
