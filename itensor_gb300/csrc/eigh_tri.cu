@@ -18,8 +18,8 @@
 //      rotations; the eigenvalues go back to the caller, which truncates;
 //   3. tri_rot_kernel: only the kept eigenvectors of the tridiagonal matrices:
 //      the recorded rotations applied in reverse to unit vectors, a tile of
-//      vectors per CTA in shared memory, the CTA's sixteen warps applying
-//      rotations of sixteen sweeps at once on a lockstep schedule from the host;
+//      vectors per CTA in shared memory, the CTA's 32 warps applying
+//      rotations of 32 sweeps at once on a lockstep schedule from the host;
 //   4. tri_applyq_kernel: the Householder reflectors applied to each kept
 //      vector (one warp per vector), written to the output in eigenvalue order.
 // The FP64 work is ~n^3 FMA for the reduction, then ~n^2 rotations and ~2n^2
@@ -48,7 +48,7 @@ namespace itg {
 namespace {
 constexpr int TRI_THREADS = 256;
 constexpr int TRI_APPLYQ_WARPS = 4;       // kept vectors per CTA in the reflector stage (one warp each)
-constexpr int TRI_ROT_WARPS = 16;        // sweeps applied at once to one row tile
+constexpr int TRI_ROT_WARPS = 32;        // sweeps applied at once to one row tile
 constexpr int TRI_ROT_WINDOW = 4;        // lockstep steps between barriers
 constexpr size_t TRI_SMEM_LIMIT = 200 * 1024;
 

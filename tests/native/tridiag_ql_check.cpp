@@ -95,7 +95,7 @@ int main() {
                 worst_res = std::max(worst_res, std::fabs(ty - d[j] * Z[(size_t)c * n + j]));
             }
         // 2. lockstep schedules
-        for (int W : {8, 16})
+        for (int W : {8, 16, 32})
         for (int K : {1, 4, 8}) {
             std::vector<int32_t> woff;
             std::vector<QlStart> ent;
