@@ -70,12 +70,16 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
     // d/2 times those of the two steps it replaces (d the site dimension): it
     // is taken only where it costs no more flops than they do (spin-1/2 models;
     // not the Hubbard model's d = 4).
-    // Only a program made for many applies fuses (fuse_mpo): the fusion builds
-    // two plans the plain chain does not need, which the two or three applies
-    // of one Davidson call do not pay back.
+    // Site dimensions above 2 are ruled out before any plan is built (the
+    // check below needs two extra plans); the caller turns fusion on
+    // (fuse_mpo: the prepared programs of the C-ABI, and Davidson outside a
+    // solver pool).
+    int dsite = 0;
+    for (auto const& I : op.W1->inds())
+        if (phi_layout->find_index(I) >= 0) dsite = std::max(dsite, (int)I.dim());
     Tensor Wf;
     size_t wpos = 0;
-    for (size_t s = 0; fuse_mpo && s + 1 < chain.size(); ++s)
+    for (size_t s = 0; fuse_mpo && dsite <= 2 && s + 1 < chain.size(); ++s)
         if ((chain[s] == op.W1 && chain[s + 1] == op.W2) || (chain[s] == op.W2 && chain[s + 1] == op.W1)) wpos = s + 1;
     if (wpos > 0) {
         Wf = contract(ctx, *chain[wpos - 1], *chain[wpos], PREC_F64);
