@@ -440,10 +440,10 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
     std::vector<double> M((size_t)msz * msz, std::numeric_limits<double>::quiet_NaN());
     auto Mat = [&](int i, int j) -> double& { return M[(size_t)j * msz + i]; };
     // one prepared program for every apply of this call (plans resolved once)
-    // the MPO-step fusion saves GPU time (a lone solve waits for its GPU) at
-    // the price of two plans' host time (a solver pool's threads are short of it)
-    static const bool fuse = std::getenv("ITG_NO_MPO_FUSION") == nullptr;  // diagnostics
-    auto prog = heff_prepare(ctx, op, phi.lay, prec, true, false, fuse && !fiber_active());
+    // unfused MPO steps: the same arithmetic whether the solve runs alone or in
+    // a solver pool (where the fusion's two extra plans cost more host time than
+    // the launch they save), so a solve's result does not depend on where it runs
+    auto prog = heff_prepare(ctx, op, phi.lay, prec, true, false, false);
     const int nproj = op.proj ? (int)op.proj->size() : 0;
     ITG_REQUIRE(nproj <= VecList::MAX, "davidson: too many projected states");
     std::vector<double const*> pptr(nproj);

@@ -72,8 +72,7 @@ std::shared_ptr<HeffProgram> heff_prepare(Ctx& ctx, LocalOp const& op, std::shar
     // not the Hubbard model's d = 4).
     // Site dimensions above 2 are ruled out before any plan is built (the
     // check below needs two extra plans); the caller turns fusion on
-    // (fuse_mpo: the prepared programs of the C-ABI, and Davidson outside a
-    // solver pool).
+    // (fuse_mpo: the prepared programs of the C-ABI).
     int dsite = 0;
     for (auto const& I : op.W1->inds())
         if (phi_layout->find_index(I) >= 0) dsite = std::max(dsite, (int)I.dim());
