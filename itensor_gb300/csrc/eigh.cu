@@ -348,6 +348,279 @@ __global__ void __launch_bounds__(EIG_THREADS) vapply_kernel(VJob const* __restr
     }
 }
 
+// Blocks of at most 16 rows (most density-matrix blocks of a chain): the
+// same cyclic Jacobi, laid out for the FP64 pipe of this part. One FP64 warp
+// instruction holds its SMSP's FP64 pipe for about 64 cycles whatever the
+// number of active lanes (measured: a dependent DFMA, DADD, DSETP or F2F
+// costs ~64 cycles from one warp; four warps on four SMSPs ~76 each), so a
+// round costs FP64 instructions per warp, not flops:
+//  - the rotation of each pair (lanes 0..7 of warp 0) is the critical path;
+//    its skip tests are integer compares of the bit patterns (|a_pq| against
+//    the absolute floor exactly; the relative test 1e-30 a_pp a_qq < a_pq^2
+//    on the exponent-and-top-mantissa words, a log2 approximation within
+//    0.09), and its FP32 seeds are converted with integer operations, so it
+//    holds 17 FP64 instructions (one subtraction, two Newton steps for t,
+//    two for 1/sqrt(1 + t^2), s = t c). The seed comes from the unscaled
+//    operands: every Newton iterate equals the power-of-two scaled form's
+//    while |a_pq| and |a_qq - a_pp| stay inside FP32's range (checked; else
+//    the IEEE formulas);
+//  - the 2x2 block updates: one lane per output element of the off-diagonal
+//    blocks k < l (warps 0-3, 4 lanes per block in one warp, operands read
+//    before a __syncwarp and written after it), row and column coefficients
+//    chosen by integer selects so the lanes of a warp take one path (6 FP64
+//    instructions), the diagonal blocks on warp 4;
+//  - V <- V J of round g on warps 5-7 (SMSPs 1-3) while warp 0 (SMSP 0)
+//    computes the rotations of round g + 1 (rotations double-buffered).
+// Results agree with jacobi_kernel to rounding (same rotations, same update
+// formulas; a pair whose coupling sits within the log approximation of the
+// relative threshold can be skipped by one and rotated by the other).
+constexpr int JS_THREADS = 256;
+constexpr int JS_MAXN = 16;
+constexpr long long JS_ABS_MASK = 0x7fffffffffffffffLL;
+constexpr long long JS_REL_LOG = 104501084LL;  // 99.66 * 2^20: -log2(1e-30) in units of (bits >> 32)
+
+__device__ __forceinline__ long long js_log2fix(double x) { return (__double_as_longlong(x) & JS_ABS_MASK) >> 32; }
+
+// double -> float by truncation (a seed), signed zero below FP32's normal range
+__device__ __forceinline__ float js_d2f(double x) {
+    const long long b = __double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7ff) - 1023 + 127;
+    const unsigned sign = hi & 0x80000000u;
+    if (e <= 0) return __uint_as_float(sign);
+    return __uint_as_float(sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+
+// float -> double, exact for normal floats (denormals give signed zero)
+__device__ __forceinline__ double js_f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    return __longlong_as_double(
+        (long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+__device__ __forceinline__ double js_neg(double x) { return __longlong_as_double(__double_as_longlong(x) ^ (1LL << 63)); }
+
+// jacobi_pivot with integer skip tests and unscaled seeds (see above)
+__device__ __forceinline__ bool js_pivot(double app, double aqq, double apq, long long floor_bits, double& c, double& s,
+                                         double& t) {
+    const long long b = __double_as_longlong(apq) & JS_ABS_MASK;
+    if (b <= floor_bits) return false;
+    if (2 * (b >> 32) <= js_log2fix(app) + js_log2fix(aqq) - JS_REL_LOG) return false;
+    const double d = aqq - app;
+    const int epq = (int)(b >> 52) - 1023;
+    const int ed = (int)((__double_as_longlong(d) & JS_ABS_MASK) >> 52) - 1023;
+    if (epq > -120 && epq < 120 && ed < 120) {
+        const float asf = js_d2f(apq), dsf = js_d2f(d);
+        const float tauf = __fdividef(dsf, 2.0f * asf);
+        const float t0 = copysignf(__fdividef(1.0f, fabsf(tauf) + sqrtf(fmaf(tauf, tauf, 1.0f))), tauf);
+        const double r = js_f2d(__fdividef(1.0f, fmaf(2.0f * asf, t0, dsf)));
+        double tt = js_f2d(t0);
+        double g = fma(fma(apq, tt, d), tt, -apq);
+        tt = fma(-g, r, tt);
+        g = fma(fma(apq, tt, d), tt, -apq);
+        tt = fma(-g, r, tt);
+        const double x = fma(tt, tt, 1.0);
+        double y = js_f2d(rsqrtf(js_d2f(x)));
+        double e = fma(-x * y, y, 1.0);
+        y = fma(0.5 * y, e, y);
+        e = fma(-x * y, y, 1.0);
+        y = fma(0.5 * y, e, y);
+        t = tt;
+        c = y;
+        s = tt * y;
+        return true;
+    }
+    const double tau = d / (2.0 * apq);
+    t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+    c = 1.0 / sqrt(1.0 + t * t);
+    s = t * c;
+    return true;
+}
+
+__global__ void __launch_bounds__(JS_THREADS) jacobi_small_kernel(EigJob const* __restrict__ jobs,
+                                                                  double const* __restrict__ src, double* __restrict__ vout,
+                                                                  double* __restrict__ wout, int* __restrict__ sweeps_out,
+                                                                  int* __restrict__ status) {
+    __shared__ double A[JS_MAXN * (JS_MAXN + 1)];
+    __shared__ double V[JS_MAXN * JS_MAXN];
+    __shared__ double cst[2][3 * JS_MAXN / 2];
+    __shared__ int pq[2][JS_MAXN];
+    __shared__ int rf[2][JS_MAXN / 2];
+    __shared__ int rank[JS_MAXN];
+    __shared__ int rot_sweep;
+    __shared__ double red[JS_THREADS / 32];
+    const EigJob it = jobs[blockIdx.x];
+    const int n = it.n, np = n + (n & 1), half = np / 2, lda = np + 1;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    double loc = 0;
+    for (int e = tid; e < n * n; e += JS_THREADS) {
+        const int i = e % n, j = e / n;
+        const double x = src[it.a_off + e];
+        A[j * lda + i] = x;
+        V[e] = (i == j) ? 1.0 : 0.0;
+        loc = fma(x, x, loc);
+    }
+    if (tid == 0) rot_sweep = 0;
+    for (int o = 16; o; o >>= 1) loc += __shfl_down_sync(0xffffffffu, loc, o);
+    if ((tid & 31) == 0) red[warp] = loc;
+    __syncthreads();
+    double norm2 = 0;
+    for (int w = 0; w < JS_THREADS / 32; ++w) norm2 += red[w];
+    const double normA = sqrt(norm2);
+    const long long floor_bits = __double_as_longlong(0x1p-52 * normA);
+    // this thread's update work: kind 1 = element (ei, ej) of off-diagonal
+    // block (bk, bl); kind 2 = diagonal entry ei of block bk
+    const int noff = half * (half - 1) / 2;
+    int kind = 0, bk = 0, bl = 0, ei = 0, ej = 0;
+    if (tid < 4 * noff) {
+        int b = tid >> 2, k = 0;
+        while (b >= half - 1 - k) {
+            b -= half - 1 - k;
+            ++k;
+        }
+        kind = 1;
+        bk = k;
+        bl = k + 1 + b;
+        ei = (tid >> 1) & 1;
+        ej = tid & 1;
+    } else if (tid >= 128 && tid - 128 < 2 * half) {
+        kind = 2;
+        bk = (tid - 128) >> 1;
+        ei = (tid - 128) & 1;
+    }
+    // V items (pair, row) on warps 5-7
+    const int vi0 = tid - 160, nvi = half * n;
+    auto v_update = [&](int buf) {
+        for (int e = vi0; e < nvi; e += 96) {
+            const int k = e / n, i = e % n;
+            if (!rf[buf][k]) continue;
+            const double c = cst[buf][3 * k], s = cst[buf][3 * k + 1];
+            const int p = pq[buf][2 * k], q = pq[buf][2 * k + 1];
+            const double a = V[p * n + i], b = V[q * n + i];
+            V[p * n + i] = c * a - s * b;
+            V[q * n + i] = s * a + c * b;
+        }
+    };
+    // rot_sweep holds the last sweep (1-based) that rotated; it only grows, so
+    // a thread reading it late in the next sweep still sees "not converged"
+    bool converged = (n <= 1);
+    int nsw = 0, g = 0;
+    for (int sweep = 0; sweep < EIG_MAX_SWEEPS && !converged; ++sweep) {
+        for (int r = 0; r < np - 1; ++r, ++g) {
+            const int bf = g & 1;
+            if (tid < half) {
+                const int k = tid;
+                int p, q;
+                round_pair(r, k, np, p, q);
+                double c = 1.0, s = 0.0, t = 0.0;
+                bool rot = false;
+                if (q < n) rot = js_pivot(A[p * lda + p], A[q * lda + q], A[q * lda + p], floor_bits, c, s, t);
+                if (rot) rot_sweep = sweep + 1;
+                cst[bf][3 * k] = c;
+                cst[bf][3 * k + 1] = s;
+                cst[bf][3 * k + 2] = t;
+                pq[bf][2 * k] = p;
+                pq[bf][2 * k + 1] = q;
+                rf[bf][k] = rot;
+            } else if (vi0 >= 0 && g > 0) {
+                v_update(bf ^ 1);
+            }
+            __syncthreads();
+            if (kind == 1) {
+                const int fk = rf[bf][bk], fl = rf[bf][bl];
+                const int p = pq[bf][2 * bk], q = pq[bf][2 * bk + 1], u = pq[bf][2 * bl], w = pq[bf][2 * bl + 1];
+                const bool qk = q < n, wl = w < n;  // dummy slots hold no row / column
+                const int oi = ei ? q : p, oj = ej ? w : u;
+                double out = 0;
+                if (fk | fl) {
+                    const double ck = cst[bf][3 * bk], sk = cst[bf][3 * bk + 1];
+                    const double cl = cst[bf][3 * bl], sl = cst[bf][3 * bl + 1];
+                    const double x = A[u * lda + p];
+                    const double y = wl ? A[w * lda + p] : 0.0;
+                    const double z = qk ? A[u * lda + q] : 0.0;
+                    const double v = (qk && wl) ? A[w * lda + q] : 0.0;
+                    // column oj by (cl, sl), then row oi by (ck, sk)
+                    const double m0 = ej ? sl : cl, m1 = ej ? cl : js_neg(sl);
+                    const double r0 = ei ? sk : ck, r1 = ei ? ck : js_neg(sk);
+                    const double a0 = fma(m0, x, m1 * y), a1 = fma(m0, z, m1 * v);
+                    out = fma(r0, a0, r1 * a1);
+                }
+                __syncwarp();
+                if ((fk | fl) && (ei == 0 || qk) && (ej == 0 || wl)) {
+                    A[oj * lda + oi] = out;
+                    A[oi * lda + oj] = out;
+                }
+            } else if (kind == 2) {
+                // pivot block: diagonalised exactly
+                const int fk = rf[bf][bk];
+                const int p = pq[bf][2 * bk], q = pq[bf][2 * bk + 1];
+                double apq = 0, d = 0;
+                if (fk) {
+                    apq = A[q * lda + p];
+                    d = ei ? A[q * lda + q] : A[p * lda + p];
+                }
+                __syncwarp();
+                if (fk) {
+                    const double t = cst[bf][3 * bk + 2];
+                    if (ei == 0) {
+                        A[p * lda + p] = d - t * apq;
+                        A[q * lda + p] = 0.0;
+                        A[p * lda + q] = 0.0;
+                    } else {
+                        A[q * lda + q] = d + t * apq;
+                    }
+                }
+            } else if (tid < 160) {
+                __syncwarp();
+            }
+            __syncthreads();
+        }
+        nsw = sweep + 1;
+        converged = rot_sweep < sweep + 1;
+    }
+    if (g > 0 && vi0 >= 0) v_update((g - 1) & 1);
+    __syncthreads();
+    // eigenvalues descending (ties by position); eigenvector columns follow
+    for (int i = tid; i < n; i += JS_THREADS) {
+        const double di = A[i * lda + i];
+        int rr = 0;
+        for (int j = 0; j < n; ++j) {
+            const double dj = A[j * lda + j];
+            rr += (dj > di) || (dj == di && j < i);
+        }
+        wout[it.w_off + rr] = di;
+        rank[i] = rr;
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += JS_THREADS) {
+        const int col = e / n, row = e % n;
+        vout[it.v_off + (size_t)rank[col] * n + row] = V[e];
+    }
+    if (tid == 0) sweeps_out[blockIdx.x] = nsw;
+    if (!converged) {
+        // sweep cap reached: accept when the remaining coupling is negligible
+        double mx = 0;
+        for (int e = tid; e < n * n; e += JS_THREADS) {
+            const int i = e % n, j = e / n;
+            if (i != j) mx = fmax(mx, fabs(A[j * lda + i]));
+        }
+        for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        __syncthreads();
+        if ((tid & 31) == 0) red[warp] = mx;
+        __syncthreads();
+        if (tid == 0) {
+            double m = 0;
+            for (int w = 0; w < JS_THREADS / 32; ++w) m = fmax(m, red[w]);
+            status[blockIdx.x] = (m <= 1e-13 * normA) ? 0 : 1;
+        }
+    } else if (tid == 0) {
+        status[blockIdx.x] = 0;
+    }
+}
+
 namespace {
 constexpr size_t EIG_SMEM_LIMIT = 227 * 1024;
 constexpr size_t EIG_LOG_LIMIT = size_t(512) << 20;   // bytes of rotation log per launch
@@ -437,7 +710,12 @@ static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const
     int* d_rank = reinterpret_cast<int*>(db + o_rank);
     double2* d_log = logv ? reinterpret_cast<double2*>(db + o_log) : nullptr;
     EigJob const* d_jobs = reinterpret_cast<EigJob const*>(db + o_jobs);
-    if (sa && sv) launch_eig<true, true>(ctx, nb, smem, d_jobs, src, vout, wout, scratch, d_log, d_rank, d_sw, d_stat);
+    static const bool ieee_rot = std::getenv("ITG_EIG_IEEE_ROT") != nullptr;
+    if (!logv && nmax <= JS_MAXN && !ieee_rot) {
+        jacobi_small_kernel<<<nb, JS_THREADS, 0, ctx.stream>>>(d_jobs, src, vout, wout, d_sw, d_stat);
+        ITG_CHECK_CUDA(cudaGetLastError());
+        ctx.kernel_launches++;
+    } else if (sa && sv) launch_eig<true, true>(ctx, nb, smem, d_jobs, src, vout, wout, scratch, d_log, d_rank, d_sw, d_stat);
     else if (sa) launch_eig<true, false>(ctx, nb, smem, d_jobs, src, vout, wout, scratch, d_log, d_rank, d_sw, d_stat);
     else launch_eig<false, false>(ctx, nb, smem, d_jobs, src, vout, wout, scratch, d_log, d_rank, d_sw, d_stat);
     if (logv && !vjobs.empty()) {
