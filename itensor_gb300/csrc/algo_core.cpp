@@ -409,12 +409,15 @@ static_assert(S_PZ + VecList::MAX <= Ctx::NSCALAR, "davidson: scalar slots");
 
 // The reductions stay on the device: dot products and norms land in scalar
 // slots that the next kernels read as coefficients, and the host reads them
-// only where the reference's control flow branches on them. A call with
-// niter 2 waits for its stream four times: <phi|H|phi> and the first
-// residual; the new vector's Gram-Schmidt norm with the projected matrix's
-// new column (twice); the second residual. The arithmetic is that of the
+// only where the reference's control flow branches on them. Each iteration
+// runs ahead of its convergence test (Gram-Schmidt, the next apply and the
+// projected matrix's new column are enqueued before the host reads the
+// residual), so a call with niter 2 waits for its stream twice: after
+// iteration 0 (<phi|H|phi>, the residual, the Gram-Schmidt norm, the new
+// column) and after iteration 1 (the same). The arithmetic is that of the
 // host-driven form (the same kernels, coefficients formed by the same
-// products), so the results are bit-identical to it.
+// products), so the results are bit-identical to it; work run ahead of a
+// stop is dropped.
 double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double errgoal, int miniter, int prec,
                 int* applies) {
     const double approx0 = 1e-12;
@@ -500,31 +503,12 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
     for (ii = 0; ii <= actual_maxiter; ++ii) {
         const int ni = ii + 1;
         Tensor q(phi.lay, ctx.stream);
-        double qnorm2 = 0;
         if (ii == 0) {
             // q = H V0 - lambda V0 and |q|^2, lambda = <V0|H|V0> from its slot
             VecList L;
             L.add(AV[0].data(), 1.0);
             L.add(V[0].data(), -1.0, S_E0);
             combo_async(ctx, q.data(), 0.0, L, n, S_Q);
-            ctx.sync();
-            if (!(scal[S_NRM] > 0.0)) {
-                // zero starting vector: the reference's random restart
-                // (itensor/iterativesolvers.h), which needs the host in the loop
-                phi = phi_in;
-                double nrm = tensor_norm(ctx, phi);
-                int guard = 0;
-                while (nrm == 0.0 && guard++ < 4) {
-                    launch_random(ctx, phi.data(), n, 0x5eed + guard);
-                    nrm = tensor_norm(ctx, phi);
-                }
-                ITG_REQUIRE(nrm > 0, "davidson: zero initial vector");
-                return davidson(ctx, op, phi, maxiter, errgoal, miniter, prec, applies);
-            }
-            initEn = scal[S_E0];
-            lambda = initEn;
-            Mat(0, 0) = lambda;
-            qnorm2 = scal[S_Q];
         } else {
             std::vector<double> Msub((size_t)(ii + 1) * (ii + 1));
             for (int j = 0; j <= ii; ++j) for (int i = 0; i <= ii; ++i) Msub[(size_t)j * (ii + 1) + i] = Mat(i, j);
@@ -544,25 +528,48 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
             // the last iteration stops whatever the residual: it is not needed
             if (ii == actual_maxiter) break;
             combo_async(ctx, q.data(), 0.0, Lq, n, S_Q);
-            ctx.sync();
-            qnorm2 = scal[S_Q];
         }
-        const double qnorm = std::sqrt(std::max(qnorm2, 0.0));
-        const bool converged = (qnorm < errgoal && std::abs(lambda - last_lambda) < errgoal) ||
-                               qnorm < std::max(approx0, errgoal * 1e-3);
-        last_lambda = lambda;
-        if (qnorm < 1e-20 || (converged && ii >= miniter) || ii == actual_maxiter) break;
-        // one Gram-Schmidt pass on the device, the next vector applied and its
-        // column of the projected matrix formed before the host looks at the norm
-        gs_device(q, ni);
-        V[ni] = q;
-        AV[ni] = apply(V[ni]);
-        {
+        // Ahead of the host's look at the residual: one Gram-Schmidt pass on
+        // the device, the next vector applied and its column of the projected
+        // matrix formed; one wait then returns all of it. When the residual
+        // ends the iteration that work is dropped (the results are those of the
+        // stop before it).
+        const bool ahead = ii < actual_maxiter;
+        if (ahead) {
+            gs_device(q, ni);
+            V[ni] = q;
+            AV[ni] = apply(V[ni]);
             VecList Lv;
             for (int k = 0; k <= ni; ++k) Lv.add(V[k].data(), 0.0);
             dots_async(ctx, Lv, AV[ni].data(), n, S_M);
         }
         ctx.sync();
+        if (ii == 0) {
+            if (!(scal[S_NRM] > 0.0)) {
+                // zero starting vector: the reference's random restart
+                // (itensor/iterativesolvers.h), which needs the host in the loop
+                phi = phi_in;
+                double nrm = tensor_norm(ctx, phi);
+                int guard = 0;
+                while (nrm == 0.0 && guard++ < 4) {
+                    launch_random(ctx, phi.data(), n, 0x5eed + guard);
+                    nrm = tensor_norm(ctx, phi);
+                }
+                ITG_REQUIRE(nrm > 0, "davidson: zero initial vector");
+                return davidson(ctx, op, phi, maxiter, errgoal, miniter, prec, applies);
+            }
+            initEn = scal[S_E0];
+            lambda = initEn;
+            Mat(0, 0) = lambda;
+        }
+        const double qnorm = std::sqrt(std::max(scal[S_Q], 0.0));
+        const bool converged = (qnorm < errgoal && std::abs(lambda - last_lambda) < errgoal) ||
+                               qnorm < std::max(approx0, errgoal * 1e-3);
+        last_lambda = lambda;
+        if (qnorm < 1e-20 || (converged && ii >= miniter) || ii == actual_maxiter) {
+            if (ahead) --napply;  // the apply made ahead is not part of the result
+            break;
+        }
         double qnrm = std::sqrt(std::max(scal[S_G], 0.0));
         if (qnrm < 1e-10) {
             // q depended on V: the pass above divided by a tiny norm. Redo it
@@ -692,11 +699,11 @@ SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor co
     // eigenvalues first; the eigenvectors of the large blocks only for the kept states
     EighPending eig = batched_eigh_begin(ctx, items, rho.data(), vbuf.as<double>(), wbuf.as<double>(),
                                          sbuf.as<double>());
-    if (eig.bad) throw Error(ERR_NOCONV, "denmat_decomp: eigensolver hit its sweep cap");
     std::vector<double> w(std::max<int64_t>(wtot, 1));
-    if (wtot) {
-        ctx.d2h(w.data(), wbuf.as<double>(), sizeof(double) * wtot);
-    }
+    // one wait: the eigenvalues, and the convergence statuses enqueued before them
+    if (wtot) ctx.d2h(w.data(), wbuf.as<double>(), sizeof(double) * wtot);
+    else if (eig.jac_pending) ctx.sync();
+    if (eigh_collect(ctx, eig)) throw Error(ERR_NOCONV, "denmat_decomp: eigensolver hit its sweep cap");
     std::vector<double> alleig(w.begin(), w.begin() + wtot);
     std::sort(alleig.begin(), alleig.end(), std::greater<double>());
     const long maxdim = args.maxdim > 0 ? args.maxdim : (long)ci.dim();
@@ -761,10 +768,8 @@ SplitResult denmat_decomp(Ctx& ctx, Tensor const& AA, Tensor const& A, Tensor co
     Tensor Ud = relabel(U, dag_all(U.inds()));
     Tensor new_orth = uncombine(ctx, Ud, cmb);
     Tensor new_oc = contract(ctx, U, AAc, prec);
-    if (args.normalize) {
-        double nr = tensor_norm(ctx, new_oc);
-        if (nr > 1e-16) launch_scale(ctx, new_oc.data(), new_oc.lay->size, 1.0 / nr);
-    }
+    // new_oc /= |new_oc| when |new_oc| > 1e-16, on the device (no wait)
+    if (args.normalize) normalize_async(ctx, new_oc.data(), new_oc.lay->size, 1e-16);
     SplitResult res;
     res.probs = tr.P;
     res.truncerr = tr.truncerr;

@@ -733,8 +733,12 @@ Ctx::~Ctx() {
     if (pin) cudaFreeHost(pin);
     if (stage) cudaFreeHost(stage);
     if (ring) cudaFreeHost(ring);
+    if (defer_host) cudaFreeHost(defer_host);
     for (int i = 0; i < 2; ++i)
         if (ring_ev[i]) cudaEventDestroy(ring_ev[i]);
+    if (std::getenv("ITG_WAIT_LOG"))
+        std::fprintf(stderr, "itg context: %llu host waits, %llu kernel launches\n", (unsigned long long)host_waits,
+                     (unsigned long long)kernel_launches);
     if (stream) {
         stream_unregister(stream);
         if (cache) cache->release();  // while the stream lives
@@ -755,6 +759,7 @@ void Ctx::ensure_pin(size_t bytes) {
 }
 
 void Ctx::sync() {
+    ++host_waits;
     if (fiber_active()) {
         ITG_CHECK_CUDA(cudaEventRecord(sync_event, stream));
         fiber_wait_event(sync_event);
@@ -770,6 +775,7 @@ void Ctx::sync() {
 }
 
 void Ctx::wait_event(cudaEvent_t ev) {
+    ++host_waits;
     if (fiber_active()) fiber_wait_event(ev);
     else ITG_CHECK_CUDA(cudaEventSynchronize(ev));
 }
@@ -854,6 +860,18 @@ void BlockCache::trim(size_t keep) {
         held -= it->first;
         free.erase(it);
     }
+}
+
+void* Ctx::ensure_defer(size_t bytes) {
+    if (defer_bytes < bytes) {
+        sync();
+        if (defer_host) cudaFreeHost(defer_host);
+        defer_host = nullptr;
+        const size_t nb = std::max<size_t>({bytes, size_t(4) << 10, 2 * defer_bytes});
+        ITG_CHECK_CUDA(cudaHostAlloc(&defer_host, nb, cudaHostAllocDefault));
+        defer_bytes = nb;
+    }
+    return defer_host;
 }
 
 void Ctx::ensure_stage(size_t bytes) {

@@ -649,8 +649,12 @@ void launch_eig(Ctx& ctx, int njobs, size_t smem, EigJob const* d_jobs, double c
 }
 }  // namespace
 
+// Returns the number of blocks known not to have converged. Without
+// ITG_EIG_LOG the statuses are not waited for: they are copied to
+// ctx.defer_host and *pending is set to their count (eigh_collect reads them).
 static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
-                       double* scratch) {
+                       double* scratch, int* pending) {
+    *pending = 0;
     if (items.empty()) return 0;
     const int nb = (int)items.size();
     int nmax = 0;
@@ -699,11 +703,12 @@ static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const
     const size_t o_log = a16(o_rank + sizeof(int) * (size_t)ntot);
     const size_t total = o_log + (logv ? sizeof(double2) * log_elems : 0);
     DevBuf buf(total, ctx.stream);
-    ctx.ensure_stage(up);
-    char* st = static_cast<char*>(ctx.stage);
+    // through the staging ring: this function returns without waiting for the
+    // stream, and the tridiagonal path refills the context's pinned buffer
+    char* st = ctx.stage_ring(up);
     std::memcpy(st + o_jobs, jobs.data(), sizeof(EigJob) * nb);
     if (!vjobs.empty()) std::memcpy(st + o_vj, vjobs.data(), sizeof(VJob) * vjobs.size());
-    ITG_CHECK_CUDA(cudaMemcpyAsync(buf.p, ctx.stage, up, cudaMemcpyHostToDevice, ctx.stream));
+    ITG_CHECK_CUDA(cudaMemcpyAsync(buf.p, st, up, cudaMemcpyHostToDevice, ctx.stream));
     char* db = buf.as<char>();
     int* d_stat = reinterpret_cast<int*>(db + o_stat);
     int* d_sw = reinterpret_cast<int*>(db + o_sw);
@@ -727,11 +732,17 @@ static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;
     }
+    if (!std::getenv("ITG_EIG_LOG")) {
+        void* hs = ctx.ensure_defer(sizeof(int) * nb);
+        ITG_CHECK_CUDA(cudaMemcpyAsync(hs, d_stat, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx.stream));
+        *pending = nb;
+        return 0;
+    }
     std::vector<int> stv(nb);
     ctx.d2h(stv.data(), d_stat, sizeof(int) * nb);
     int bad = 0;
     for (int s : stv) bad += s;
-    if (std::getenv("ITG_EIG_LOG")) {
+    {
         std::vector<int> swv(nb);
         ctx.d2h(swv.data(), d_sw, sizeof(int) * nb);
         std::fprintf(stderr, "itg eigh:");
@@ -760,10 +771,11 @@ EighPending batched_eigh_begin(Ctx& ctx, std::vector<EigItem> const& items, doub
     const bool timing = std::getenv("ITG_EIG_TIME") != nullptr;  // diagnostics: wall time of each path
     auto now = [&] { ctx.sync(); return std::chrono::steady_clock::now(); };
     auto t0 = timing ? now() : std::chrono::steady_clock::time_point{};
-    // Jacobi first: both paths stage uploads in the context's pinned buffer, and
-    // each is done with it when it returns
+    // Jacobi first: its uploads go through the staging ring (no wait), the
+    // tridiagonal path's through the context's pinned buffer, which it waits
+    // for before it returns
     EighPending p;
-    p.bad = jacobi_eigh(ctx, small, src, vout, wout, scratch);
+    p.bad = jacobi_eigh(ctx, small, src, vout, wout, scratch, &p.jac_pending);
     auto t1 = timing ? now() : t0;
     int bad_tri = 0;
     p.tri = tri_eigh_begin(ctx, large, large_ids, src, wout, scratch, &bad_tri);
@@ -780,6 +792,15 @@ EighPending batched_eigh_begin(Ctx& ctx, std::vector<EigItem> const& items, doub
     return p;
 }
 
+int eigh_collect(Ctx& ctx, EighPending& p) {
+    if (p.jac_pending) {
+        int const* st = static_cast<int const*>(ctx.defer_host);
+        for (int i = 0; i < p.jac_pending; ++i) p.bad += st[i];
+        p.jac_pending = 0;
+    }
+    return p.bad;
+}
+
 void batched_eigh_finish(Ctx& ctx, EighPending& p, std::vector<int> const& keep, double* vout, double* scratch) {
     if (p.tri) tri_eigh_finish(ctx, *p.tri, keep, vout, scratch);
 }
@@ -787,7 +808,8 @@ void batched_eigh_finish(Ctx& ctx, EighPending& p, std::vector<int> const& keep,
 int batched_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout, double* wout,
                  double* scratch) {
     EighPending p = batched_eigh_begin(ctx, items, src, vout, wout, scratch);
-    if (p.bad) return p.bad;
+    if (p.jac_pending) ctx.sync();
+    if (eigh_collect(ctx, p)) return p.bad;
     std::vector<int> all(items.size());
     for (size_t i = 0; i < items.size(); ++i) all[i] = items[i].n;
     batched_eigh_finish(ctx, p, all, vout, scratch);

@@ -33,8 +33,12 @@ void tri_eigh_finish(Ctx& ctx, TriPending& p, std::vector<int> const& keep, doub
 // large block i (the small blocks already have all of theirs).
 struct EighPending {
     TriPendingPtr tri;
-    int bad = 0;   // blocks whose iteration did not converge
+    int bad = 0;          // blocks whose iteration did not converge (known so far)
+    int jac_pending = 0;  // Jacobi statuses on their way to ctx.defer_host
 };
+// After a sync() that follows batched_eigh_begin: adds the Jacobi statuses to
+// p.bad and returns it.
+int eigh_collect(Ctx& ctx, EighPending& p);
 EighPending batched_eigh_begin(Ctx& ctx, std::vector<EigItem> const& items, double const* src, double* vout,
                                double* wout, double* scratch);
 void batched_eigh_finish(Ctx& ctx, EighPending& p, std::vector<int> const& keep, double* vout, double* scratch);

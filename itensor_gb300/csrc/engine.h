@@ -270,7 +270,14 @@ struct Ctx {
     cudaStream_t side_stream(int i);
     void fork();                 // side streams wait for the work enqueued on `stream` so far
     void join(int nused);        // `stream` waits for side streams 0..nused-1
+    // pinned host area for device -> host copies enqueued now and read after a
+    // later sync(), so that two reads share one wait (the eigensolver's
+    // convergence status rides on the eigenvalue read of the bond split)
+    void* defer_host = nullptr;
+    size_t defer_bytes = 0;
+    void* ensure_defer(size_t bytes);
     // counters
+    uint64_t host_waits = 0;
     uint64_t kernel_launches = 0;
     uint64_t plans_built = 0, plan_hits = 0;
     double flops_done = 0;
@@ -430,6 +437,10 @@ void combo_async(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, in
 void dots_async(Ctx& ctx, VecList const& V, double const* x, int64_t n, int slot);
 // x *= 1 / sqrt(max(s, 0)), s = scalar slot norm_slot (no wait).
 void scale_rnorm(Ctx& ctx, double* x, int64_t n, int norm_slot);
+// x /= |x| when |x| > min_norm, without waiting: |x|^2 in the last scalar
+// slot (Ctx::NSCALAR - 1, which Davidson does not use), then one scaling
+// kernel that reads it.
+void normalize_async(Ctx& ctx, double* x, int64_t n, double min_norm);
 // General block permute / gather: dst[dst_off[e]] = src[src_off[e]] described per
 // block by offset tables (see ops.cu). Used for combiner, uncombine and
 // layout changes.

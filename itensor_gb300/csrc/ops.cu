@@ -295,6 +295,29 @@ void scale_rnorm(Ctx& ctx, double* x, int64_t n, int norm_slot) {
     ctx.kernel_launches++;
 }
 
+__global__ void scale_rnorm_min_kernel(double* x, int64_t n, double const* __restrict__ s, double min_norm) {
+    __shared__ double a;
+    if (threadIdx.x == 0) {
+        const double nr = sqrt(fmax(*s, 0.0));
+        a = nr > min_norm ? 1.0 / nr : 1.0;
+    }
+    __syncthreads();
+    const double f = a;
+    if (f == 1.0) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] *= f;
+}
+
+void normalize_async(Ctx& ctx, double* x, int64_t n, double min_norm) {
+    if (n <= 0) return;
+    constexpr int slot = Ctx::NSCALAR - 1;
+    VecList V;
+    V.add(x, 1.0);
+    dots_async(ctx, V, x, n, slot);
+    scale_rnorm_min_kernel<<<grid_for(ctx, n), 256, 0, ctx.stream>>>(x, n, ctx.scal_dev->as<double>() + slot, min_norm);
+    ITG_CHECK_CUDA(cudaGetLastError());
+    ctx.kernel_launches++;
+}
+
 static bool uses_slots(VecList const& X) {
     for (int k = 0; k < X.n; ++k)
         if (X.cs[k] >= 0) {
