@@ -638,8 +638,7 @@ size_t eig_smem_bytes(int n, bool sa, bool sv) {
 template <bool SA, bool SV>
 void launch_eig(Ctx& ctx, int njobs, size_t smem, EigJob const* d_jobs, double const* src, double* vout, double* wout,
                 double* scratch, double2* rlog, int* ranks, int* sweeps, int* d_stat) {
-    if (smem > 48 * 1024)
-        ITG_CHECK_CUDA(cudaFuncSetAttribute(jacobi_kernel<SA, SV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    grow_smem_attr((void const*)jacobi_kernel<SA, SV>, smem);
     // ITG_EIG_IEEE_ROT: rotations by IEEE division and square root (diagnostics)
     static const int fast = std::getenv("ITG_EIG_IEEE_ROT") ? 0 : 1;
     jacobi_kernel<SA, SV><<<njobs, EIG_THREADS, smem, ctx.stream>>>(d_jobs, src, vout, wout, scratch, rlog, ranks, sweeps,
@@ -725,8 +724,7 @@ static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const
     else launch_eig<false, false>(ctx, nb, smem, d_jobs, src, vout, wout, scratch, d_log, d_rank, d_sw, d_stat);
     if (logv && !vjobs.empty()) {
         const size_t vsm = sizeof(double) * (size_t)rows * nmax;
-        if (vsm > 48 * 1024)
-            ITG_CHECK_CUDA(cudaFuncSetAttribute(vapply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsm));
+        grow_smem_attr((void const*)vapply_kernel, vsm);
         vapply_kernel<<<(int)vjobs.size(), EIG_THREADS, vsm, ctx.stream>>>(
             reinterpret_cast<VJob const*>(db + o_vj), d_log, d_rank, d_sw, vout);
         ITG_CHECK_CUDA(cudaGetLastError());

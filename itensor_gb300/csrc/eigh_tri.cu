@@ -527,10 +527,12 @@ TriPendingPtr tri_eigh_begin(Ctx& ctx, std::vector<EigItem> const& items_in, std
     //    so they run side by side on the context's side streams
     {
         const size_t smem = sizeof(double) * 2 * (size_t)P->nmax;
-        if (smem > 48 * 1024)
-            ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_reduce_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)smem));
-        ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_reduce_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        grow_smem_attr((void const*)tri_reduce_kernel, smem);
+        static const bool cluster16 = [] {
+            ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_reduce_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+            return true;
+        }();
+        (void)cluster16;
         int ngroups = 0;
         for (int b = 0; b < nj;) {
             int e = b;
@@ -728,8 +730,7 @@ void tri_eigh_finish(Ctx& ctx, TriPending& P, std::vector<int> const& keep, doub
     // 1. kept eigenvectors of the tridiagonal matrices (reversed rotations on unit vectors)
     {
         const size_t smem = sizeof(double) * (size_t)R * P.nmax;
-        if (smem > 48 * 1024)
-            ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_rot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        grow_smem_attr((void const*)tri_rot_kernel, smem);
         tri_rot_kernel<<<(int)rjobs.size(), TRI_ROT_WARPS * 32, smem, ctx.stream>>>(
             d_rj, d_jobs, scratch, reinterpret_cast<QlOut const*>(blob.as<char>()), blob.as<char>(), R);
         ITG_CHECK_CUDA(cudaGetLastError());
@@ -740,9 +741,7 @@ void tri_eigh_finish(Ctx& ctx, TriPending& P, std::vector<int> const& keep, doub
     // 2. back to the block's basis: the Householder reflectors applied to each kept column
     {
         const size_t smem = sizeof(double) * TRI_APPLYQ_WARPS * (size_t)P.nmax;
-        if (smem > 48 * 1024)
-            ITG_CHECK_CUDA(cudaFuncSetAttribute(tri_applyq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)smem));
+        grow_smem_attr((void const*)tri_applyq_kernel, smem);
         tri_applyq_kernel<<<(int)cjobs.size(), TRI_APPLYQ_WARPS * 32, smem, ctx.stream>>>(d_cj, d_jobs, scratch, d_aux,
                                                                                         vout, P.nmax);
         ITG_CHECK_CUDA(cudaGetLastError());

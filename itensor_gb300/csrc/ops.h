@@ -1,8 +1,25 @@
 // Gather plans and the batched eigensolver interface (kernels in ops.cu).
 #pragma once
 #include "engine.h"
+#include <mutex>
+#include <unordered_map>
 
 namespace itg {
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) for kernel f only when
+// `bytes` exceeds what was set for it before (the attribute lasts for the
+// process; it only grows, so a concurrent launch with less never sees it
+// shrink). Saves a driver call on most launches of the eigensolver kernels.
+inline void grow_smem_attr(void const* f, size_t bytes) {
+    if (bytes <= 48 * 1024) return;
+    static std::mutex mu;
+    static std::unordered_map<void const*, size_t> set;
+    std::lock_guard<std::mutex> g(mu);
+    size_t& cur = set[f];
+    if (bytes <= cur) return;
+    ITG_CHECK_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+}
 
 struct GatherItem {
     int64_t soff, doff;
