@@ -414,7 +414,9 @@ static_assert(S_PZ + VecList::MAX <= Ctx::NSCALAR, "davidson: scalar slots");
 // projected matrix's new column are enqueued before the host reads the
 // residual), so a call with niter 2 waits for its stream twice: after
 // iteration 0 (<phi|H|phi>, the residual, the Gram-Schmidt norm, the new
-// column) and after iteration 1 (the same). The arithmetic is that of the
+// column) and after iteration 1 (the same). After a call that stopped on its
+// residual, the next one waits for each residual first (four waits), so
+// converged sweeps do not pay for extensions they drop. The arithmetic is that of the
 // host-driven form (the same kernels, coefficients formed by the same
 // products), so the results are bit-identical to it; work run ahead of a
 // stop is dropped.
@@ -497,6 +499,8 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
         dots_async(ctx, L, AV[0].data(), n, S_E0);
     }
     double initEn = 0, last_lambda = 1000.0, lambda = 0;
+    const bool run_ahead = !ctx.dav_stopped_early;
+    bool stopped_early = false;
     Tensor phi_t = phi;
     std::vector<double> D, U;
     int ii = 0;
@@ -529,20 +533,23 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
             if (ii == actual_maxiter) break;
             combo_async(ctx, q.data(), 0.0, Lq, n, S_Q);
         }
-        // Ahead of the host's look at the residual: one Gram-Schmidt pass on
-        // the device, the next vector applied and its column of the projected
-        // matrix formed; one wait then returns all of it. When the residual
-        // ends the iteration that work is dropped (the results are those of the
-        // stop before it).
-        const bool ahead = ii < actual_maxiter;
-        if (ahead) {
+        // one Gram-Schmidt pass on the device, the next vector applied and its
+        // column of the projected matrix formed
+        auto extend = [&] {
             gs_device(q, ni);
             V[ni] = q;
             AV[ni] = apply(V[ni]);
             VecList Lv;
             for (int k = 0; k <= ni; ++k) Lv.add(V[k].data(), 0.0);
             dots_async(ctx, Lv, AV[ni].data(), n, S_M);
-        }
+        };
+        // Ahead of the host's look at the residual, unless the last call
+        // stopped on its residual (then this one likely does too): one wait
+        // returns the residual and the extension. When the residual ends the
+        // iteration the extension is dropped (the results are those of the
+        // stop before it).
+        const bool ahead = run_ahead && ii < actual_maxiter;
+        if (ahead) extend();
         ctx.sync();
         if (ii == 0) {
             if (!(scal[S_NRM] > 0.0)) {
@@ -568,7 +575,12 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
         last_lambda = lambda;
         if (qnorm < 1e-20 || (converged && ii >= miniter) || ii == actual_maxiter) {
             if (ahead) --napply;  // the apply made ahead is not part of the result
+            stopped_early = ii < actual_maxiter;
             break;
+        }
+        if (!ahead) {
+            extend();
+            ctx.sync();
         }
         double qnrm = std::sqrt(std::max(scal[S_G], 0.0));
         if (qnrm < 1e-10) {
@@ -607,6 +619,7 @@ double davidson(Ctx& ctx, LocalOp const& op, Tensor& phi, int maxiter, double er
         for (int k = 0; k <= ni; ++k) { Mat(k, ni) = scal[S_M + k]; Mat(ni, k) = scal[S_M + k]; }
     }
     phi = phi_t;
+    ctx.dav_stopped_early = stopped_early;
     if (applies) *applies += napply;
     return lambda;
 }

@@ -689,9 +689,14 @@ Ctx::Ctx(int dev) : device(dev) {
     uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
     ITG_CHECK_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
     ITG_CHECK_CUDA(cudaEventCreateWithFlags(&sync_event, cudaEventDisableTiming));
-    ITG_CHECK_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&err_host), 64, cudaHostAllocMapped));
+    // one pinned allocation: the status word, then the first deferred-read area
+    // (pinning host memory takes the driver's lock; solver-pool contexts are
+    // created while other solves launch)
+    ITG_CHECK_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&err_host), 64 + DEFER0, cudaHostAllocMapped));
     ITG_CHECK_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&err_dev), err_host, 0));
     err_host[0] = 0;
+    defer_host = reinterpret_cast<char*>(err_host) + 64;
+    defer_bytes = DEFER0;
 }
 
 cudaStream_t Ctx::side_stream(int i) {
@@ -733,7 +738,7 @@ Ctx::~Ctx() {
     if (pin) cudaFreeHost(pin);
     if (stage) cudaFreeHost(stage);
     if (ring) cudaFreeHost(ring);
-    if (defer_host) cudaFreeHost(defer_host);
+    if (defer_own) cudaFreeHost(defer_host);
     for (int i = 0; i < 2; ++i)
         if (ring_ev[i]) cudaEventDestroy(ring_ev[i]);
     if (std::getenv("ITG_WAIT_LOG"))
@@ -865,8 +870,9 @@ void BlockCache::trim(size_t keep) {
 void* Ctx::ensure_defer(size_t bytes) {
     if (defer_bytes < bytes) {
         sync();
-        if (defer_host) cudaFreeHost(defer_host);
+        if (defer_own) cudaFreeHost(defer_host);
         defer_host = nullptr;
+        defer_own = true;
         const size_t nb = std::max<size_t>({bytes, size_t(4) << 10, 2 * defer_bytes});
         ITG_CHECK_CUDA(cudaHostAlloc(&defer_host, nb, cudaHostAllocDefault));
         defer_bytes = nb;

@@ -273,9 +273,15 @@ struct Ctx {
     // pinned host area for device -> host copies enqueued now and read after a
     // later sync(), so that two reads share one wait (the eigensolver's
     // convergence status rides on the eigenvalue read of the bond split)
+    static constexpr size_t DEFER0 = 16 << 10;  // carved from the status word's allocation
     void* defer_host = nullptr;
     size_t defer_bytes = 0;
+    bool defer_own = false;  // grown past DEFER0: an allocation of its own
     void* ensure_defer(size_t bytes);
+    // Davidson: the last call stopped on its convergence test before its last
+    // iteration, so the next call waits for each residual before enqueuing
+    // the next vector (a timing hint only: results are the same either way)
+    bool dav_stopped_early = false;
     // counters
     uint64_t host_waits = 0;
     uint64_t kernel_launches = 0;
