@@ -326,6 +326,45 @@ def _big_split_problem(seed=3):
     return AA, A, B
 
 
+def _small_split_problem(seed=5):
+    """A two-site tensor whose density-matrix blocks have 1, 2, 3, 15, 16 and 3
+    rows from the left (combined l, s1 sectors) and several sizes from the right."""
+    from oracle.blocksparse import BSTensor, Index, QN, OUT, IN
+    rng = np.random.default_rng(seed)
+    q = lambda v: QN(("Sz", v, 1))
+    l = Index([(q(-4), 1), (q(-2), 1), (q(0), 2), (q(2), 13), (q(4), 3)], dir=IN, tags="l")
+    s1 = Index([(q(1), 1), (q(-1), 1)], dir=OUT, tags="s1")
+    s2 = Index([(q(1), 1), (q(-1), 1)], dir=OUT, tags="s2")
+    r = Index([(q(-2), 5), (q(0), 9), (q(2), 7)], dir=OUT, tags="r")
+    a = Index([(q(0), 2), (q(2), 2), (q(-2), 2)], dir=OUT, tags="a")
+    AA = BSTensor.random([l, s1, s2, r], QN(("Sz", 0, 1)), rng)
+    A = BSTensor.random([l, s1, a], QN(("Sz", 0, 1)), rng)
+    B = BSTensor.random([a.dag(), s2, r], QN(("Sz", 0, 1)), rng)
+    return AA, A, B
+
+
+def test_denmat_small_blocks(ctx, monkeypatch):
+    """Density-matrix blocks of 1 to 16 rows through the small-block Jacobi
+    (the tridiagonal threshold raised past 16, so a 16-row block takes it too)
+    against the oracle's eigh: every eigenvalue, the truncation error, and the
+    kept weight of A' B'."""
+    from oracle.decomp import denmat_decomp as odenmat
+    from helpers import to_gpu
+    monkeypatch.setenv("ITG_EIG_TRI_MIN", "17")
+    AA, A, B = _small_split_problem()
+    names = ["Sz"]
+    for fromleft in (True, False):
+        _, _, probs, te = odenmat(AA, A, B, fromleft, 100, 1, 1e-14, normalize=False)
+        gA, gB, eigs, gte = ctx.denmat_decomp(to_gpu(ctx, AA, names), to_gpu(ctx, A, names), to_gpu(ctx, B, names),
+                                              fromleft, 1e-14, 100, 1, normalize=False)
+        assert len(eigs) == len(probs), fromleft
+        assert np.max(np.abs(eigs - probs)) < 1e-13 * probs[0], fromleft
+        assert abs(gte - te) < 1e-13, fromleft
+        AB = ctx.contract(gA, gB)
+        nrm2 = float(np.sum(AB.numpy() ** 2))
+        assert abs(nrm2 - np.sum(probs)) < 1e-12 * np.sum(probs)
+
+
 @pytest.mark.parametrize("tri_min", ["64", "300", "100000"])
 def test_denmat_large_blocks(ctx, tri_min, monkeypatch):
     """Density-matrix blocks of 90..460 rows through the tridiagonal eigensolver
