@@ -77,22 +77,37 @@ __device__ __forceinline__ void oz_digit_vals(double x, int emax, int (&dig)[S])
 // + 4 (l mod 2) ..+3) and writes their digits as one 8-byte store per plane,
 // so a warp writes 256 contiguous bytes per plane. Rows past the block's end
 // get zero digits.
+// The column offsets of a chunk of PREP_KCHUNK contracted positions are looked
+// up once per CTA into shared memory (a table lookup can take an integer
+// division), then read by both passes.
+constexpr int PREP_KCHUNK = 1024;
+
 template <int S>
 __device__ __forceinline__ void prep_item(PrepItem const& pi, const OpBlockRec* __restrict__ ops,
                                           const int32_t* __restrict__ tab, const double* __restrict__ A,
                                           const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
                                           int64_t plane, int32_t* __restrict__ exps) {
     __shared__ int rexp[8];
+    __shared__ int32_t coff[PREP_KCHUNK];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const OpBlockRec ob = ops[pi.op];
     const double* __restrict__ base = (pi.which ? B : A) + ob.src;
+    auto load_offsets = [&](int kc) {
+        const int kn = min(PREP_KCHUNK, ob.K - kc);
+        __syncthreads();  // the previous chunk's readers are done
+        for (int j = threadIdx.x; j < kn; j += blockDim.x) coff[j] = tab_at(tab, ob.tcol, kc + j);
+        __syncthreads();
+        return kn;
+    };
     // row exponents: warp w takes row r0 + w
     {
         const int r = pi.r0 + warp;
+        const int32_t ro = r < pi.r1 ? tab_at(tab, ob.trow, r) : 0;
         int emax = 0;
-        if (r < pi.r1) {
-            const int32_t ro = tab_at(tab, ob.trow, r);
-            for (int k = lane; k < ob.K; k += 32) emax = max(emax, exp_field(base[ro + tab_at(tab, ob.tcol, k)]));
+        for (int kc = 0; kc < ob.K; kc += PREP_KCHUNK) {
+            const int kn = load_offsets(kc);
+            if (r < pi.r1)
+                for (int j = lane; j < kn; j += 32) emax = max(emax, exp_field(base[ro + coff[j]]));
         }
         emax = __reduce_max_sync(0xffffffffu, emax);
         if (lane == 0) {
@@ -109,22 +124,31 @@ __device__ __forceinline__ void prep_item(PrepItem const& pi, const OpBlockRec* 
     const int32_t ro = rrv ? tab_at(tab, ob.trow, rr) : 0;
     const int nrg = panel_row_groups(ob.rows);
     __nv_bfloat16* dst0 = panels + ob.panel + (int64_t)(pi.r0 >> 3) * 128 + lane * 4;
-    for (int ks = warp; ks < ob.Kp / 16; ks += 8) {
-        int dig[4][S];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int k = ks * 16 + kq + i;
-            oz_digit_vals<S>((rrv && k < ob.K) ? base[ro + tab_at(tab, ob.tcol, k)] : 0.0, er, dig[i]);
+    int kc = 0;  // first position of the chunk of offsets in shared memory
+    for (int kb = 0; kb < ob.Kp; kb += PREP_KCHUNK) {
+        // k-steps of this chunk: [kb, kb + PREP_KCHUNK) (a multiple of 16)
+        if (kb < ob.K) {
+            kc = kb;
+            load_offsets(kc);
         }
-        __nv_bfloat16* dst = dst0 + (int64_t)ks * nrg * 128;
+        const int ks_end = min(ob.Kp, kb + PREP_KCHUNK) / 16;
+        for (int ks = kb / 16 + warp; ks < ks_end; ks += 8) {
+            int dig[4][S];
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-            __nv_bfloat162 lo = __floats2bfloat162_rn((float)dig[0][s], (float)dig[1][s]);
-            __nv_bfloat162 hi = __floats2bfloat162_rn((float)dig[2][s], (float)dig[3][s]);
-            uint2 v;
-            v.x = *reinterpret_cast<uint32_t*>(&lo);
-            v.y = *reinterpret_cast<uint32_t*>(&hi);
-            *reinterpret_cast<uint2*>(dst + s * plane) = v;
+            for (int i = 0; i < 4; ++i) {
+                const int k = ks * 16 + kq + i;
+                oz_digit_vals<S>((rrv && k < ob.K) ? base[ro + coff[k - kc]] : 0.0, er, dig[i]);
+            }
+            __nv_bfloat16* dst = dst0 + (int64_t)ks * nrg * 128;
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                __nv_bfloat162 lo = __floats2bfloat162_rn((float)dig[0][s], (float)dig[1][s]);
+                __nv_bfloat162 hi = __floats2bfloat162_rn((float)dig[2][s], (float)dig[3][s]);
+                uint2 v;
+                v.x = *reinterpret_cast<uint32_t*>(&lo);
+                v.y = *reinterpret_cast<uint32_t*>(&hi);
+                *reinterpret_cast<uint2*>(dst + s * plane) = v;
+            }
         }
     }
 }
