@@ -144,6 +144,38 @@ double norm(Ctx& ctx, double const* a, int64_t n) {
     return std::sqrt(std::max(r, 0.0));
 }
 
+// Sum of the CTAs' partials by the last CTA: a loop of one thread over the
+// partials when there are few of them, else one partial per thread added as
+// a tree (lanes by shuffles, then the warps' sums in warp 0). Every FP64 add
+// is a warp instruction that holds its SMSP's FP64 pipe for about 64 cycles,
+// so a loop over 196 partials alone took about 11 us of a 17 us launch
+// (n = 50,000; the tree form: 6 us). Deterministic either way (the grid size
+// decides the form). The result is valid in thread 0. Called by every thread
+// of the CTA.
+constexpr int TREE_MIN_PARTS = 32;
+__device__ double sum_partials(double const* __restrict__ part, int nparts, double* sh) {
+    if (nparts <= TREE_MIN_PARTS) {
+        double t = 0;
+        if (threadIdx.x == 0)
+            for (int b = 0; b < nparts; ++b) t += __ldcg(part + b);
+        return t;
+    }
+    double v = 0;
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) v += __ldcg(part + b);
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();  // a previous use of sh has been read
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0;
+    const int nw = (int)(blockDim.x >> 5);
+    if (threadIdx.x < 32) {
+        t = (int)threadIdx.x < nw ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o; o >>= 1)
+            if (o < nw) t += __shfl_down_sync(0xffffffffu, t, o);
+    }
+    return t;
+}
+
 // ------------------------------------------------------------------ fused combinations
 // y = a0 y + sum_k c_k X_k (y not read when a0 == 0), the terms added in k
 // order with one FMA each (the same rounding as a chain of axpy calls), and
@@ -185,10 +217,9 @@ __global__ void combo_kernel(double* __restrict__ y, double a0, VecList X, int64
     }
     __syncthreads();
     if (!last) return;
+    __threadfence();
+    const double t = sum_partials(part, (int)gridDim.x, sh);
     if (threadIdx.x == 0) {
-        __threadfence();
-        double t = 0;
-        for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(part + b);
         *out = t;
         if (out2) *out2 = t;
         *counter = 0;  // ready for the next launch on this stream
@@ -224,11 +255,22 @@ __global__ void dots_fused_kernel(VecList V, double const* __restrict__ x, int64
     __syncthreads();
     if (!last) return;
     __threadfence();
-    for (int v = threadIdx.x; v < V.n; v += blockDim.x) {
-        double t = 0;
-        for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(part + (size_t)v * gridDim.x + b);
-        out[v] = t;
-        if (out2) out2[v] = t;
+    if ((int)gridDim.x <= TREE_MIN_PARTS) {
+        // few partials: one thread per vector, in CTA order
+        for (int v = threadIdx.x; v < V.n; v += blockDim.x) {
+            double t = 0;
+            for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(part + (size_t)v * gridDim.x + b);
+            out[v] = t;
+            if (out2) out2[v] = t;
+        }
+    } else {
+        for (int v = 0; v < V.n; ++v) {
+            const double t = sum_partials(part + (size_t)v * gridDim.x, (int)gridDim.x, sh);
+            if (threadIdx.x == 0) {
+                out[v] = t;
+                if (out2) out2[v] = t;
+            }
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) *counter = 0;  // ready for the next launch on this stream
