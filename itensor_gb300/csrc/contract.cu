@@ -327,6 +327,7 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const ItemRec* __restrict
                                                        const double* __restrict__ A,
                                                        const double* __restrict__ B,
                                                        double* __restrict__ C) {
+    pdl_wait();
     f64_tile(items[blockIdx.x], pairs, cblk, tab, A, B, C);
 }
 
@@ -491,6 +492,7 @@ __global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_direct_kernel(
                                                                                 const double* __restrict__ A,
                                                                                 const double* __restrict__ B,
                                                                                 double* __restrict__ C) {
+    pdl_wait();
     const ItemRec it = items[blockIdx.x];
     const CBlockRec cb = cblk[it.c];
     switch (cb.N) {
@@ -513,6 +515,7 @@ __global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_kernel(const I
                                                                          const double* __restrict__ A,
                                                                          const double* __restrict__ B,
                                                                          double* __restrict__ C) {
+    pdl_wait();
     __shared__ double Bs[SKINNY_K][SKINNY_N];
     const ItemRec it = items[blockIdx.x];
     const CBlockRec cb = cblk[it.c];
@@ -583,6 +586,7 @@ __global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_wide_kernel(co
                                                                               const double* __restrict__ A,
                                                                               const double* __restrict__ B,
                                                                               double* __restrict__ C) {
+    pdl_wait();
     __shared__ double part[WIDE_WARPS][WIDE_ROWS][SKINNY_N];
     const ItemRec it = items[blockIdx.x];
     const CBlockRec cb = cblk[it.c];
@@ -601,22 +605,22 @@ __global__ void __launch_bounds__(SKINNY_THREADS) gemm_f64_skinny_wide_kernel(co
 // Launches the skinny kernel with the plan's rows per thread.
 static void launch_skinny(Ctx& ctx, Plan const& p, double const* A, double const* B, double* C) {
     if (p.skinny_wide) {
-        gemm_f64_skinny_wide_kernel<<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk,
+        launch_pdl(ctx, p.nitems, SKINNY_THREADS, 0, gemm_f64_skinny_wide_kernel, p.d_items, p.d_pairs, p.d_cblk,
                                                                                  p.d_tab, A, B, C);
         return;
     }
     if (p.max_pair_K <= SKINNY_K) {
         switch (p.skinny_r) {
             case 1:
-                gemm_f64_skinny_direct_kernel<1><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk,
+                launch_pdl(ctx, p.nitems, SKINNY_THREADS, 0, gemm_f64_skinny_direct_kernel<1>, p.d_items, p.d_pairs, p.d_cblk,
                                                                                                p.d_tab, A, B, C);
                 break;
             case 2:
-                gemm_f64_skinny_direct_kernel<2><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk,
+                launch_pdl(ctx, p.nitems, SKINNY_THREADS, 0, gemm_f64_skinny_direct_kernel<2>, p.d_items, p.d_pairs, p.d_cblk,
                                                                                                p.d_tab, A, B, C);
                 break;
             default:
-                gemm_f64_skinny_direct_kernel<4><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk,
+                launch_pdl(ctx, p.nitems, SKINNY_THREADS, 0, gemm_f64_skinny_direct_kernel<4>, p.d_items, p.d_pairs, p.d_cblk,
                                                                                                p.d_tab, A, B, C);
                 break;
         }
@@ -624,13 +628,13 @@ static void launch_skinny(Ctx& ctx, Plan const& p, double const* A, double const
     }
     switch (p.skinny_r) {
         case 1:
-            gemm_f64_skinny_kernel<1><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+            launch_pdl(ctx, p.nitems, SKINNY_THREADS, 0, gemm_f64_skinny_kernel<1>, p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
             break;
         case 2:
-            gemm_f64_skinny_kernel<2><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+            launch_pdl(ctx, p.nitems, SKINNY_THREADS, 0, gemm_f64_skinny_kernel<2>, p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
             break;
         default:
-            gemm_f64_skinny_kernel<4><<<p.nitems, SKINNY_THREADS, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+            launch_pdl(ctx, p.nitems, SKINNY_THREADS, 0, gemm_f64_skinny_kernel<4>, p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
             break;
     }
 }
@@ -1582,7 +1586,7 @@ void exec_plan(Ctx& ctx, Plan const& p, double const* A, double const* B, double
     } else if (prec == PREC_F64 || prec == PREC_OZAKI_BF16) {
         // in a solver-pool fiber that groups launches: one launch with the other solves' contractions
         if (ctx.profiling || !fiber_group_contract(ctx, p, A, B, C, 0, nullptr, nullptr, false))
-            gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+            launch_pdl(ctx, p.nitems, 256, 0, gemm_f64_kernel, p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
         else
             ctx.kernel_launches -= 1;  // flush() counted the group's launch
     } else {
@@ -1602,7 +1606,7 @@ void exec_plan_f64_only(Ctx& ctx, Plan const& p, double const* A, double const* 
     if (p.skinny)
         launch_skinny(ctx, p, A, B, C);
     else
-        gemm_f64_kernel<<<p.nitems, 256, 0, ctx.stream>>>(p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
+        launch_pdl(ctx, p.nitems, 256, 0, gemm_f64_kernel, p.d_items, p.d_pairs, p.d_cblk, p.d_tab, A, B, C);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
     ctx.flops_done += p.flops;

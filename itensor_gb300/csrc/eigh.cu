@@ -444,6 +444,7 @@ __global__ void __launch_bounds__(JS_THREADS) jacobi_small_kernel(EigJob const* 
                                                                   double const* __restrict__ src, double* __restrict__ vout,
                                                                   double* __restrict__ wout, int* __restrict__ sweeps_out,
                                                                   int* __restrict__ status) {
+    pdl_wait();
     __shared__ double A[JS_MAXN * (JS_MAXN + 1)];
     __shared__ double V[JS_MAXN * JS_MAXN];
     __shared__ double cst[2][3 * JS_MAXN / 2];
@@ -720,7 +721,7 @@ static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const
     EigJob const* d_jobs = reinterpret_cast<EigJob const*>(db + o_jobs);
     static const bool ieee_rot = std::getenv("ITG_EIG_IEEE_ROT") != nullptr;
     if (!logv && nmax <= JS_MAXN && !ieee_rot) {
-        jacobi_small_kernel<<<nb, JS_THREADS, 0, ctx.stream>>>(d_jobs, src, vout, wout, d_sw, d_stat);
+        launch_pdl(ctx, nb, JS_THREADS, 0, jacobi_small_kernel, d_jobs, src, vout, wout, d_sw, d_stat);
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;
     } else if (sa && sv) launch_eig<true, true>(ctx, nb, smem, d_jobs, src, vout, wout, scratch, d_log, d_rank, d_sw, d_stat);

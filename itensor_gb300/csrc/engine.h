@@ -14,6 +14,7 @@
 #pragma once
 #include "tensor.h"
 #include <atomic>
+#include <utility>
 #include <mutex>
 #include <shared_mutex>
 
@@ -291,6 +292,9 @@ struct Ctx {
     int ozaki_slices = 6;
     int gemm_variant = -1;           // split-precision GEMM variant override (-1: autotuned per plan)
     int sm_count = 152;
+    // set while heff_program captures its launches into a graph: launch_pdl
+    // then launches without the programmatic-dependency attribute
+    bool capturing = false;
 
     explicit Ctx(int dev);
     ~Ctx();
@@ -452,5 +456,33 @@ void normalize_async(Ctx& ctx, double* x, int64_t n, double min_norm);
 // layout changes.
 struct GatherPlan;
 void launch_gather(Ctx& ctx, GatherPlan const& g, double const* src, double* dst);
+
+
+#ifdef __CUDACC__
+// Programmatic dependent launch. A kernel launched by launch_pdl may begin
+// while the previous kernel on its stream is still running, so its launch
+// latency hides behind that kernel (back to back on this part: an empty kernel
+// 2.06 -> 1.39 us per launch, a small dot-product kernel 4.10 -> 1.8 us).
+// Such a kernel calls pdl_wait() before it touches global memory:
+// griddepcontrol.wait returns once the previous grid has completed and its
+// writes are visible, so stream order holds; in a kernel launched without the
+// attribute it returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(Ctx& ctx, dim3 grid, dim3 block, size_t smem, void (*kernel)(KArgs...), Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = ctx.capturing ? 0 : 1;
+    ITG_CHECK_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
+#endif
 
 }  // namespace itg

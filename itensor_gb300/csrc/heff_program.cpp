@@ -197,7 +197,14 @@ void HeffProgram::run(Ctx& ctx, double const* in_ptr, double* out_ptr, bool host
             const double f0 = ctx.flops_done;
             cudaGraph_t g;
             ITG_CHECK_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
-            launch_steps(ctx);
+            ctx.capturing = true;
+            try {
+                launch_steps(ctx);
+            } catch (...) {
+                ctx.capturing = false;
+                throw;
+            }
+            ctx.capturing = false;
             ITG_CHECK_CUDA(cudaStreamEndCapture(ctx.stream, &g));
             launches_per_run = (int)(ctx.kernel_launches - l0);
             ctx.kernel_launches = l0;

@@ -14,9 +14,11 @@ namespace itg {
 
 // ------------------------------------------------------------------ vector kernels
 __global__ void fill_kernel(double* x, int64_t n, double v) {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] = v;
 }
 __global__ void scale_kernel(double* x, int64_t n, double a) {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] *= a;
 }
 // y = a x + b y. With b == 0, y is not read: it may be fresh pool memory whose
@@ -42,13 +44,13 @@ static int grid_for(Ctx& ctx, int64_t n) {
 
 void launch_fill(Ctx& ctx, double* x, int64_t n, double v) {
     if (n <= 0) return;
-    fill_kernel<<<grid_for(ctx, n), 256, 0, ctx.stream>>>(x, n, v);
+    launch_pdl(ctx, grid_for(ctx, n), 256, 0, fill_kernel, x, n, v);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
 void launch_scale(Ctx& ctx, double* x, int64_t n, double a) {
     if (n <= 0) return;
-    scale_kernel<<<grid_for(ctx, n), 256, 0, ctx.stream>>>(x, n, a);
+    launch_pdl(ctx, grid_for(ctx, n), 256, 0, scale_kernel, x, n, a);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
@@ -187,6 +189,7 @@ __device__ double sum_partials(double const* __restrict__ part, int nparts, doub
 __global__ void combo_kernel(double* __restrict__ y, double a0, VecList X, int64_t n, int want_norm,
                              double* __restrict__ part, unsigned int* __restrict__ counter, double* __restrict__ out,
                              double* __restrict__ out2, double const* __restrict__ sd) {
+    pdl_wait();
     __shared__ double sh[32];
     __shared__ double cf[VecList::MAX];
     __shared__ bool last;
@@ -231,6 +234,7 @@ __global__ void combo_kernel(double* __restrict__ y, double a0, VecList X, int64
 __global__ void dots_fused_kernel(VecList V, double const* __restrict__ x, int64_t n, double* __restrict__ part,
                                   unsigned int* __restrict__ counter, double* __restrict__ out,
                                   double* __restrict__ out2) {
+    pdl_wait();
     __shared__ double sh[32];
     __shared__ bool last;
     for (int v = 0; v < V.n; ++v) {
@@ -292,7 +296,7 @@ void dots_fused(Ctx& ctx, VecList const& V, double const* x, int64_t n, double* 
     double* part = ctx.reduce_buf->as<double>();
     unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
-    dots_fused_kernel<<<nb, 256, 0, ctx.stream>>>(V, x, n, part, counter, static_cast<double*>(ctx.pin_dev), nullptr);
+    launch_pdl(ctx, nb, 256, 0, dots_fused_kernel, V, x, n, part, counter, static_cast<double*>(ctx.pin_dev), nullptr);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
     ctx.sync();
@@ -314,13 +318,14 @@ void dots_async(Ctx& ctx, VecList const& V, double const* x, int64_t n, int slot
     double* part = ctx.reduce_buf->as<double>();
     unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
-    dots_fused_kernel<<<nb, 256, 0, ctx.stream>>>(V, x, n, part, counter, ctx.scal_map + slot,
+    launch_pdl(ctx, nb, 256, 0, dots_fused_kernel, V, x, n, part, counter, ctx.scal_map + slot,
                                                   ctx.scal_dev->as<double>() + slot);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
 
 __global__ void scale_rnorm_kernel(double* x, int64_t n, double const* __restrict__ s) {
+    pdl_wait();
     __shared__ double a;
     if (threadIdx.x == 0) a = 1.0 / sqrt(fmax(*s, 0.0));
     __syncthreads();
@@ -332,12 +337,13 @@ void scale_rnorm(Ctx& ctx, double* x, int64_t n, int norm_slot) {
     ITG_REQUIRE(norm_slot >= 0 && norm_slot < Ctx::NSCALAR, "scale_rnorm: scalar slot out of range");
     if (n <= 0) return;
     ctx.ensure_scalars();
-    scale_rnorm_kernel<<<grid_for(ctx, n), 256, 0, ctx.stream>>>(x, n, ctx.scal_dev->as<double>() + norm_slot);
+    launch_pdl(ctx, grid_for(ctx, n), 256, 0, scale_rnorm_kernel, x, n, ctx.scal_dev->as<double>() + norm_slot);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
 
 __global__ void scale_rnorm_min_kernel(double* x, int64_t n, double const* __restrict__ s, double min_norm) {
+    pdl_wait();
     __shared__ double a;
     if (threadIdx.x == 0) {
         const double nr = sqrt(fmax(*s, 0.0));
@@ -355,7 +361,7 @@ void normalize_async(Ctx& ctx, double* x, int64_t n, double min_norm) {
     VecList V;
     V.add(x, 1.0);
     dots_async(ctx, V, x, n, slot);
-    scale_rnorm_min_kernel<<<grid_for(ctx, n), 256, 0, ctx.stream>>>(x, n, ctx.scal_dev->as<double>() + slot, min_norm);
+    launch_pdl(ctx, grid_for(ctx, n), 256, 0, scale_rnorm_min_kernel, x, n, ctx.scal_dev->as<double>() + slot, min_norm);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
@@ -378,7 +384,7 @@ double combo(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, bool w
     double* part = ctx.reduce_buf->as<double>();
     unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
-    combo_kernel<<<nb, 256, 0, ctx.stream>>>(y, a0, X, n, want_norm ? 1 : 0, part, counter,
+    launch_pdl(ctx, nb, 256, 0, combo_kernel, y, a0, X, n, want_norm ? 1 : 0, part, counter,
                                              static_cast<double*>(ctx.pin_dev), nullptr,
                                              ctx.scal_dev ? ctx.scal_dev->as<double>() : nullptr);
     ITG_CHECK_CUDA(cudaGetLastError());
@@ -399,7 +405,7 @@ void combo_async(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, in
     unsigned int* counter = reinterpret_cast<unsigned int*>(part + REDUCE_DOUBLES - 2);
     const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(DOT_CTAS, (n + 255) / 256));
     double* sd = ctx.scal_dev->as<double>();
-    combo_kernel<<<nb, 256, 0, ctx.stream>>>(y, a0, X, n, norm_slot >= 0 ? 1 : 0, part, counter,
+    launch_pdl(ctx, nb, 256, 0, combo_kernel, y, a0, X, n, norm_slot >= 0 ? 1 : 0, part, counter,
                                              norm_slot >= 0 ? ctx.scal_map + norm_slot : nullptr,
                                              norm_slot >= 0 ? sd + norm_slot : nullptr, sd);
     ITG_CHECK_CUDA(cudaGetLastError());
@@ -410,6 +416,7 @@ void combo_async(Ctx& ctx, double* y, double a0, VecList const& X, int64_t n, in
 // dst[doff + d1[i] + d2[j]] = src[soff + s1[i] + s2[j]], i < n1 (fastest), j < n2
 __global__ void gather_kernel(GatherItem const* __restrict__ items, int32_t const* __restrict__ tab,
                               double const* __restrict__ src, double* __restrict__ dst) {
+    pdl_wait();
     const GatherItem it = items[blockIdx.x];
     const int64_t n = (int64_t)it.n1 * it.n2;
     for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
@@ -433,7 +440,7 @@ void GatherPlan::upload(Ctx& ctx) {
 
 void launch_gather(Ctx& ctx, GatherPlan const& g, double const* src, double* dst) {
     if (g.nitems == 0) return;
-    gather_kernel<<<g.nitems, 256, 0, ctx.stream>>>(g.d_items, g.d_tab, src, dst);
+    launch_pdl(ctx, g.nitems, 256, 0, gather_kernel, g.d_items, g.d_tab, src, dst);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
