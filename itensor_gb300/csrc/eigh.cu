@@ -217,6 +217,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(EigJob const* __res
                                                              double* __restrict__ scratch, double2* __restrict__ rlog,
                                                              int* __restrict__ ranks, int* __restrict__ sweeps_out,
                                                              int* __restrict__ status, int fast) {
+    pdl_wait();
     extern __shared__ __align__(16) unsigned char eig_smem[];
     __shared__ int rotated;
     __shared__ double red[32];
@@ -313,6 +314,7 @@ struct VJob {
 __global__ void __launch_bounds__(EIG_THREADS) vapply_kernel(VJob const* __restrict__ jobs, double2 const* __restrict__ rlog,
                                                              int const* __restrict__ ranks, int const* __restrict__ sweeps,
                                                              double* __restrict__ vout) {
+    pdl_wait();
     extern __shared__ __align__(16) unsigned char va_smem[];
     double* vr = reinterpret_cast<double*>(va_smem);  // rows x n, row-major
     const VJob j = jobs[blockIdx.x];
@@ -642,7 +644,7 @@ void launch_eig(Ctx& ctx, int njobs, size_t smem, EigJob const* d_jobs, double c
     grow_smem_attr((void const*)jacobi_kernel<SA, SV>, smem);
     // ITG_EIG_IEEE_ROT: rotations by IEEE division and square root (diagnostics)
     static const int fast = std::getenv("ITG_EIG_IEEE_ROT") ? 0 : 1;
-    jacobi_kernel<SA, SV><<<njobs, EIG_THREADS, smem, ctx.stream>>>(d_jobs, src, vout, wout, scratch, rlog, ranks, sweeps,
+    launch_pdl(ctx, njobs, EIG_THREADS, smem, jacobi_kernel<SA, SV>, d_jobs, src, vout, wout, scratch, rlog, ranks, sweeps,
                                                                     d_stat, fast);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
@@ -730,7 +732,7 @@ static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const
     if (logv && !vjobs.empty()) {
         const size_t vsm = sizeof(double) * (size_t)rows * nmax;
         grow_smem_attr((void const*)vapply_kernel, vsm);
-        vapply_kernel<<<(int)vjobs.size(), EIG_THREADS, vsm, ctx.stream>>>(
+        launch_pdl(ctx, (int)vjobs.size(), EIG_THREADS, vsm, vapply_kernel, 
             reinterpret_cast<VJob const*>(db + o_vj), d_log, d_rank, d_sw, vout);
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;

@@ -245,6 +245,7 @@ __global__ void __launch_bounds__(TRI_APPLYQ_WARPS * 32) tri_applyq_kernel(ColJo
                                                                           double const* __restrict__ scratch,
                                                                           double const* __restrict__ aux,
                                                                           double* __restrict__ vout, int nmax) {
+    pdl_wait();
     extern __shared__ double sm[];
     const ColJob cj = cjobs[blockIdx.x];
     const TriJob jb = jobs[cj.job];
@@ -297,6 +298,7 @@ __global__ void __launch_bounds__(TRI_ROT_WARPS * 32) tri_rot_kernel(RowJob cons
                                                                      double* __restrict__ scratch,
                                                                      QlOut const* __restrict__ qo,
                                                                      char const* __restrict__ blob, int R) {
+    pdl_wait();
     extern __shared__ double tile[];
     const RowJob rj = rjobs[blockIdx.x];
     const TriJob jb = jobs[rj.job];
@@ -359,6 +361,7 @@ __global__ void __launch_bounds__(TRI_ROT_WARPS * 32) tri_rot_kernel(RowJob cons
 // Sorted eigenvalues of every block to wout (one CTA per block).
 __global__ void tri_wout_kernel(TriJob const* __restrict__ jobs, double const* __restrict__ sorted,
                                 int64_t const* __restrict__ soff, double* __restrict__ wout) {
+    pdl_wait();
     const TriJob jb = jobs[blockIdx.x];
     const int64_t o = soff[blockIdx.x];
     for (int i = threadIdx.x; i < jb.n; i += blockDim.x) wout[jb.w_off + i] = sorted[o + i];
@@ -606,7 +609,7 @@ TriPendingPtr tri_eigh_begin(Ctx& ctx, std::vector<EigItem> const& items_in, std
             std::memcpy(st + o_s + sizeof(double) * soff[b], sorted[b].data(), sizeof(double) * items[b].n);
         DevBuf wb(bytes, ctx.stream);
         ITG_CHECK_CUDA(cudaMemcpyAsync(wb.p, st, bytes, cudaMemcpyHostToDevice, ctx.stream));
-        tri_wout_kernel<<<nj, 128, 0, ctx.stream>>>(d_jobs, reinterpret_cast<double const*>(wb.as<char>() + o_s),
+        launch_pdl(ctx, nj, 128, 0, tri_wout_kernel, d_jobs, reinterpret_cast<double const*>(wb.as<char>() + o_s),
                                                      wb.as<int64_t>(), wout);
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;
@@ -731,7 +734,7 @@ void tri_eigh_finish(Ctx& ctx, TriPending& P, std::vector<int> const& keep, doub
     {
         const size_t smem = sizeof(double) * (size_t)R * P.nmax;
         grow_smem_attr((void const*)tri_rot_kernel, smem);
-        tri_rot_kernel<<<(int)rjobs.size(), TRI_ROT_WARPS * 32, smem, ctx.stream>>>(
+        launch_pdl(ctx, (int)rjobs.size(), TRI_ROT_WARPS * 32, smem, tri_rot_kernel, 
             d_rj, d_jobs, scratch, reinterpret_cast<QlOut const*>(blob.as<char>()), blob.as<char>(), R);
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;
@@ -742,7 +745,7 @@ void tri_eigh_finish(Ctx& ctx, TriPending& P, std::vector<int> const& keep, doub
     {
         const size_t smem = sizeof(double) * TRI_APPLYQ_WARPS * (size_t)P.nmax;
         grow_smem_attr((void const*)tri_applyq_kernel, smem);
-        tri_applyq_kernel<<<(int)cjobs.size(), TRI_APPLYQ_WARPS * 32, smem, ctx.stream>>>(d_cj, d_jobs, scratch, d_aux,
+        launch_pdl(ctx, (int)cjobs.size(), TRI_APPLYQ_WARPS * 32, smem, tri_applyq_kernel, d_cj, d_jobs, scratch, d_aux,
                                                                                         vout, P.nmax);
         ITG_CHECK_CUDA(cudaGetLastError());
         ctx.kernel_launches++;

@@ -480,6 +480,9 @@ inline void launch_pdl(Ctx& ctx, dim3 grid, dim3 block, size_t smem, void (*kern
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
+    // not under graph capture: a graph replay already starts its kernels back
+    // to back (measured: the m = 1024 apply's replay time did not change with
+    // the attribute captured)
     cfg.numAttrs = ctx.capturing ? 0 : 1;
     ITG_CHECK_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
 }

@@ -24,6 +24,7 @@ __global__ void scale_kernel(double* x, int64_t n, double a) {
 // y = a x + b y. With b == 0, y is not read: it may be fresh pool memory whose
 // bits (old digit panels, integers) need not be finite doubles, and 0 * NaN = NaN.
 __global__ void axpby_kernel(double* y, double const* x, int64_t n, double a, double b) {
+    pdl_wait();
     if (b == 0.0) {
         for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
             y[i] = a * x[i];
@@ -33,6 +34,7 @@ __global__ void axpby_kernel(double* y, double const* x, int64_t n, double a, do
         y[i] = fma(a, x[i], b * y[i]);
 }
 __global__ void axpy_kernel(double* y, double const* x, int64_t n, double a) {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         y[i] = fma(a, x[i], y[i]);
 }
@@ -56,13 +58,13 @@ void launch_scale(Ctx& ctx, double* x, int64_t n, double a) {
 }
 void launch_axpy(Ctx& ctx, double* y, double const* x, int64_t n, double a) {
     if (n <= 0) return;
-    axpy_kernel<<<grid_for(ctx, n), 256, 0, ctx.stream>>>(y, x, n, a);
+    launch_pdl(ctx, grid_for(ctx, n), 256, 0, axpy_kernel, y, x, n, a);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
 void launch_axpby(Ctx& ctx, double* y, double const* x, int64_t n, double a, double b) {
     if (n <= 0) return;
-    axpby_kernel<<<grid_for(ctx, n), 256, 0, ctx.stream>>>(y, x, n, a, b);
+    launch_pdl(ctx, grid_for(ctx, n), 256, 0, axpby_kernel, y, x, n, a, b);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
@@ -452,6 +454,7 @@ void launch_gather(Ctx& ctx, GatherPlan const& g, double const* src, double* dst
 // element is read and written by the same thread.
 __global__ void noisy_rho_kernel(NoiseBlock const* __restrict__ blocks, double const* rho,
                                  double const* __restrict__ d, double* out, double half_noise) {
+    pdl_wait();
     const NoiseBlock bk = blocks[blockIdx.x];
     const int64_t n = bk.n;
     for (int64_t e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -467,6 +470,7 @@ __global__ void noisy_rho_kernel(NoiseBlock const* __restrict__ blocks, double c
 constexpr int TRACE_THREADS = 256;
 __global__ void block_trace_kernel(NoiseBlock const* __restrict__ blocks, int nb, double const* __restrict__ out,
                                    double* __restrict__ tr) {
+    pdl_wait();
     __shared__ double part[TRACE_THREADS];
     double s = 0.0;
     for (int b = 0; b < nb; ++b) {
@@ -482,6 +486,7 @@ __global__ void block_trace_kernel(NoiseBlock const* __restrict__ blocks, int nb
     if (threadIdx.x == 0) *tr = part[0];
 }
 __global__ void trace_normalise_kernel(double* __restrict__ x, int64_t n, double const* __restrict__ tr) {
+    pdl_wait();
     const double t = *tr;
     if (!(t > 1e-16)) return;
     const double inv = 1.0 / t;
@@ -505,13 +510,13 @@ void launch_noisy_rho(Ctx& ctx, std::vector<std::vector<NoiseBlock>> const& pass
     // pass 0: out = rho + noise (D_0 + D_0^T)/2; pass k: out += noise (D_k + D_k^T)/2 (in place)
     for (size_t k = 0; k < passes.size(); ++k) {
         NoiseBlock const* dblocks = reinterpret_cast<NoiseBlock const*>(tab.as<char>() + k * pbytes);
-        noisy_rho_kernel<<<(int)nb, 256, 0, ctx.stream>>>(dblocks, k == 0 ? rho : out, ds[k], out, 0.5 * noise);
+        launch_pdl(ctx, (int)nb, 256, 0, noisy_rho_kernel, dblocks, k == 0 ? rho : out, ds[k], out, 0.5 * noise);
         ITG_CHECK_CUDA(cudaGetLastError());
     }
     NoiseBlock const* dblocks0 = reinterpret_cast<NoiseBlock const*>(tab.as<char>());
-    block_trace_kernel<<<1, TRACE_THREADS, 0, ctx.stream>>>(dblocks0, (int)nb, out, dtr);
+    launch_pdl(ctx, 1, TRACE_THREADS, 0, block_trace_kernel, dblocks0, (int)nb, out, dtr);
     ITG_CHECK_CUDA(cudaGetLastError());
-    trace_normalise_kernel<<<grid_for(ctx, out_size), 256, 0, ctx.stream>>>(out, out_size, dtr);
+    launch_pdl(ctx, grid_for(ctx, out_size), 256, 0, trace_normalise_kernel, out, out_size, dtr);
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches += passes.size() + 2;
 }

@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(256) ozaki_prep_kernel(const PrepItem* __restr
                                                          const int32_t* __restrict__ tab, const double* __restrict__ A,
                                                          const double* __restrict__ B, __nv_bfloat16* __restrict__ panels,
                                                          int64_t plane, int32_t* __restrict__ exps) {
+    pdl_wait();
     prep_item<S>(items[blockIdx.x], ops, tab, A, B, panels, plane, exps);
 }
 
@@ -361,6 +362,7 @@ gemm_ozaki_kernel(const ItemRec* __restrict__ items, int nitems, const PairRec* 
                   const CBlockRec* __restrict__ cblk, const OpBlockRec* __restrict__ ops, const int32_t* __restrict__ tab,
                   const __nv_bfloat16* __restrict__ panels, int64_t plane, const int32_t* __restrict__ exps,
                   double* __restrict__ C) {
+    pdl_wait();
     extern __shared__ __align__(16) unsigned char oz_smem[];
     if (PERSIST) {
         for (int i = blockIdx.x; i < nitems; i += gridDim.x)
@@ -446,7 +448,7 @@ void launch_gemm(Ctx& ctx, Plan const& p, double* C, __nv_bfloat16 const* panels
     if (nitems == 0) return;
     const int resident = oz_resident<S, WM, PERSIST>();
     const int grid = PERSIST ? std::min(nitems, ctx.sm_count * resident) : nitems;
-    gemm_ozaki_kernel<S, WM, PERSIST><<<grid, 64 * WM, oz_smem_bytes<S, WM>(), ctx.stream>>>(
+    launch_pdl(ctx, grid, 64 * WM, oz_smem_bytes<S, WM>(), gemm_ozaki_kernel<S, WM, PERSIST>,
         items, nitems, p.d_pairs, p.d_cblk, p.d_ops, p.d_tab, panels, plane, exps, C);
 }
 
@@ -475,9 +477,8 @@ void launch_tc(Ctx& ctx, Plan const& p, double* C, __nv_bfloat16 const* panels, 
     // arrives at, so the bounded wait runs out (tests of the ERR_TIMEOUT path)
     static const int stuck = std::getenv("ITG_TC_TEST_STUCK_WAIT") ? 1 : 0;
     const int grid = std::min(p.nitems_tc, ctx.sm_count);  // persistent: one CTA per SM
-    gemm_ozaki_tc_kernel<S, TC_TILE_N><<<grid, SH::THREADS, SH::SMEM, ctx.stream>>>(
-        p.d_items_tc, p.nitems_tc, p.d_pairs_tc, p.d_tab, panels, plane, exps, C, ctx.err_dev, tc_wait_limit(),
-        stuck);
+    launch_pdl(ctx, grid, SH::THREADS, SH::SMEM, gemm_ozaki_tc_kernel<S, TC_TILE_N>, p.d_items_tc, p.nitems_tc,
+               p.d_pairs_tc, p.d_tab, panels, plane, exps, C, ctx.err_dev, tc_wait_limit(), stuck);
 }
 
 template <int S>
@@ -499,7 +500,7 @@ void launch_s(Ctx& ctx, Plan const& p, double const* A, double const* B, double*
     // A items come first: without prep_b only A is sliced (B's panels are already in place)
     const int nprep = prep_b ? p.nprep : p.nprepA;
     if (nprep > 0)
-        ozaki_prep_kernel<S><<<nprep, 256, 0, ctx.stream>>>(p.d_prep, nprep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
+        launch_pdl(ctx, nprep, 256, 0, ozaki_prep_kernel<S>, p.d_prep, nprep, p.d_ops, p.d_tab, A, B, panels, plane, exps);
     launch_variant<S>(ctx, p, variant, C, panels, plane, exps);
 }
 }  // namespace

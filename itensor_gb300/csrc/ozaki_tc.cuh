@@ -143,6 +143,7 @@ gemm_ozaki_tc_kernel(const TcTile* __restrict__ tiles, int ntiles, const TcPair*
                      const int32_t* __restrict__ tab, const __nv_bfloat16* __restrict__ panels, int64_t plane,
                      const int32_t* __restrict__ exps, double* __restrict__ C, int* __restrict__ status,
                      long long wait_limit, int stuck_test) {
+    pdl_wait();
     using SH = TcShape<S, TN>;
     static_assert(2 * S * TN <= 512, "two accumulator sets must fit in TMEM");
     static_assert(TN % 32 == 0, "the column-wise store gives each lane one column per 32");
