@@ -54,8 +54,7 @@ std::vector<Index> noprime_all(std::vector<Index> inds) {
 
 Tensor copy_tensor(Ctx& ctx, Tensor const& t) {
     Tensor r(t.lay, ctx.stream);
-    if (t.lay->size > 0)
-        ITG_CHECK_CUDA(cudaMemcpyAsync(r.data(), t.data(), sizeof(double) * t.lay->size, cudaMemcpyDeviceToDevice, ctx.stream));
+    launch_copy(ctx, r.data(), t.data(), t.lay->size);
     r.scalar = t.scalar;
     return r;
 }

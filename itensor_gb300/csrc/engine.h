@@ -420,6 +420,8 @@ void measure_peaks(Ctx& ctx, double* tflops);
 // ---- kernels launched from other translation units (ops.cu)
 void launch_fill(Ctx& ctx, double* x, int64_t n, double v);
 void launch_scale(Ctx& ctx, double* x, int64_t n, double a);
+// dst = src (n doubles, device memory), as a kernel on the context's stream
+void launch_copy(Ctx& ctx, double* dst, double const* src, int64_t n);
 void launch_axpy(Ctx& ctx, double* y, double const* x, int64_t n, double a);          // y += a x
 void launch_axpby(Ctx& ctx, double* y, double const* x, int64_t n, double a, double b); // y = a x + b y
 // dot products of x with each of nv vectors V[k] (device pointers); result to host

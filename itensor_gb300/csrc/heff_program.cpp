@@ -185,9 +185,12 @@ void HeffProgram::launch_steps(Ctx& ctx) {
 }
 
 void HeffProgram::run(Ctx& ctx, double const* in_ptr, double* out_ptr, bool host) {
-    if (in_size > 0)
-        ITG_CHECK_CUDA(cudaMemcpyAsync(in->p, in_ptr, sizeof(double) * in_size,
-                                       host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, ctx.stream));
+    if (in_size > 0) {
+        if (host)
+            ITG_CHECK_CUDA(cudaMemcpyAsync(in->p, in_ptr, sizeof(double) * in_size, cudaMemcpyHostToDevice, ctx.stream));
+        else
+            launch_copy(ctx, static_cast<double*>(in->p), in_ptr, in_size);
+    }
     if (use_graph) {
         if (!graph) {
             launch_steps(ctx);  // first run outside capture: allocates the split-precision scratch
@@ -219,9 +222,12 @@ void HeffProgram::run(Ctx& ctx, double const* in_ptr, double* out_ptr, bool host
     } else {
         launch_steps(ctx);
     }
-    if (out_size > 0)
-        ITG_CHECK_CUDA(cudaMemcpyAsync(out_ptr, out->p, sizeof(double) * out_size,
-                                       host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, ctx.stream));
+    if (out_size > 0) {
+        if (host)
+            ITG_CHECK_CUDA(cudaMemcpyAsync(out_ptr, out->p, sizeof(double) * out_size, cudaMemcpyDeviceToHost, ctx.stream));
+        else
+            launch_copy(ctx, out_ptr, static_cast<double const*>(out->p), out_size);
+    }
     if (host) ctx.sync();
 }
 

@@ -50,6 +50,20 @@ void launch_fill(Ctx& ctx, double* x, int64_t n, double v) {
     ITG_CHECK_CUDA(cudaGetLastError());
     ctx.kernel_launches++;
 }
+// Device-to-device copy on the SMs, launched like the other small kernels
+// (programmatic dependent launch): a copy-engine transfer between two kernels
+// would break their launch overlap.
+__global__ void copy_kernel(double* __restrict__ dst, double const* __restrict__ src, int64_t n) {
+    pdl_wait();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+void launch_copy(Ctx& ctx, double* dst, double const* src, int64_t n) {
+    if (n <= 0) return;
+    launch_pdl(ctx, grid_for(ctx, n), 256, 0, copy_kernel, dst, src, n);
+    ctx.kernel_launches++;
+}
+
 void launch_scale(Ctx& ctx, double* x, int64_t n, double a) {
     if (n <= 0) return;
     launch_pdl(ctx, grid_for(ctx, n), 256, 0, scale_kernel, x, n, a);
