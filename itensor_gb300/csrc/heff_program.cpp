@@ -184,12 +184,30 @@ void HeffProgram::launch_steps(Ctx& ctx) {
     }
 }
 
+// The device address of a page-locked host buffer (null for pageable memory,
+// which only a copy-engine transfer may read).
+static void* pinned_device_ptr(void const* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 void HeffProgram::run(Ctx& ctx, double const* in_ptr, double* out_ptr, bool host) {
+    // Host buffers that are page-locked are read and written by the copy
+    // kernel through their device addresses (no copy-engine transfer between
+    // the kernels); pageable ones go through cudaMemcpyAsync.
+    void* in_dev = host && in_size > 0 ? pinned_device_ptr(in_ptr) : nullptr;
+    void* out_dev = host && out_size > 0 ? pinned_device_ptr(out_ptr) : nullptr;
     if (in_size > 0) {
-        if (host)
-            ITG_CHECK_CUDA(cudaMemcpyAsync(in->p, in_ptr, sizeof(double) * in_size, cudaMemcpyHostToDevice, ctx.stream));
-        else
+        if (!host)
             launch_copy(ctx, static_cast<double*>(in->p), in_ptr, in_size);
+        else if (in_dev)
+            launch_copy(ctx, static_cast<double*>(in->p), static_cast<double const*>(in_dev), in_size);
+        else
+            ITG_CHECK_CUDA(cudaMemcpyAsync(in->p, in_ptr, sizeof(double) * in_size, cudaMemcpyHostToDevice, ctx.stream));
     }
     if (use_graph) {
         if (!graph) {
@@ -223,10 +241,12 @@ void HeffProgram::run(Ctx& ctx, double const* in_ptr, double* out_ptr, bool host
         launch_steps(ctx);
     }
     if (out_size > 0) {
-        if (host)
-            ITG_CHECK_CUDA(cudaMemcpyAsync(out_ptr, out->p, sizeof(double) * out_size, cudaMemcpyDeviceToHost, ctx.stream));
-        else
+        if (!host)
             launch_copy(ctx, out_ptr, static_cast<double const*>(out->p), out_size);
+        else if (out_dev)
+            launch_copy(ctx, static_cast<double*>(out_dev), static_cast<double const*>(out->p), out_size);
+        else
+            ITG_CHECK_CUDA(cudaMemcpyAsync(out_ptr, out->p, sizeof(double) * out_size, cudaMemcpyDeviceToHost, ctx.stream));
     }
     if (host) ctx.sync();
 }

@@ -74,6 +74,32 @@ def test_prepared_apply_matches_the_plain_call(ctx, prec):
         assert _relerr(out.cpu().numpy(), ref) <= (1e-12 if prec == 0 else 1e-11), graph
 
 
+def test_prepared_apply_host_buffers(ctx):
+    """itg_heff_run with host buffers: page-locked ones (read and written by the
+    copy kernel through their device addresses) and pageable ones (copy-engine
+    transfers) give the device-pointer run's output, bit for bit."""
+    import ctypes as C
+    import torch
+    import itensor_gb300 as itg
+    from itensor_gb300 import workloads
+    wl = workloads.heff_workload(256, 11, 4.0, 7)
+    dev = {k: workloads.to_device(ctx, wl[k]) for k in ("psi", "L", "W1", "W2", "R")}
+    h = ctx.heff_prepare(dev["L"], dev["W1"], dev["W2"], dev["R"], dev["psi"], precision=0, use_graph=True)
+    out = torch.empty(h.out_size, dtype=torch.float64, device="cuda")
+    h.run(dev["psi"].device_ptr(), out.data_ptr())
+    ctx.sync()
+    want = out.cpu().numpy()
+    psi_host = dev["psi"].numpy()
+    pin_in = torch.from_numpy(psi_host.copy()).pin_memory()
+    pin_out = torch.full((h.out_size,), float("nan"), dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        ctx._ok(itg.lib().itg_heff_run(ctx.h, h.h, C.c_void_p(pin_in.data_ptr()), C.c_void_p(pin_out.data_ptr()), 1),
+                ctx.h)
+        assert np.array_equal(pin_out.numpy(), want)
+    got = h.run_host(psi_host)
+    assert np.array_equal(got, want)
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_heff_benchmark_layout_matches_the_reference(ctx, golden, prec):
     d = golden("heff_config")
