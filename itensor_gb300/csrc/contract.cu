@@ -797,7 +797,8 @@ char* Ctx::stage_ring(size_t n) {
         if (ring) cudaFreeHost(ring);
         ring = nullptr;
         ring_half = std::max<size_t>({n, size_t(256) << 10, 2 * ring_half});
-        ITG_CHECK_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ring), 2 * ring_half, cudaHostAllocDefault));
+        ITG_CHECK_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ring), 2 * ring_half, cudaHostAllocMapped));
+        ITG_CHECK_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&ring_dev), ring, 0));
         for (int i = 0; i < 2; ++i) {
             if (!ring_ev[i]) ITG_CHECK_CUDA(cudaEventCreateWithFlags(&ring_ev[i], cudaEventDisableTiming));
             ring_pending[i] = false;
@@ -825,7 +826,27 @@ void Ctx::upload(void* dst, void const* src, size_t n) {
     if (!n) return;
     char* p = stage_ring(n);
     std::memcpy(p, src, n);
-    ITG_CHECK_CUDA(cudaMemcpyAsync(dst, p, n, cudaMemcpyHostToDevice, stream));
+    ring_copy(dst, p, n);
+}
+
+__global__ void ring_copy_kernel(char* __restrict__ dst, char const* __restrict__ src, size_t n) {
+    pdl_wait();
+    const size_t i0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x, step = (size_t)gridDim.x * blockDim.x;
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) | n) & 15) == 0) {
+        for (size_t i = i0; i < n / 16; i += step) reinterpret_cast<int4*>(dst)[i] = reinterpret_cast<int4 const*>(src)[i];
+    } else {
+        for (size_t i = i0; i < n; i += step) dst[i] = src[i];
+    }
+}
+
+void Ctx::ring_copy(void* dst, char const* st, size_t n) {
+    if (!n) return;
+    ITG_REQUIRE(ring && st >= ring && st + n <= ring + 2 * ring_half, "ring_copy: source outside the staging ring");
+    const char* src = ring_dev + (st - ring);
+    const size_t units = (n + 15) / 16;
+    const int grid = (int)std::max<size_t>(1, std::min<size_t>((units + 255) / 256, (size_t)2 * sm_count));
+    launch_pdl(*this, grid, 256, 0, ring_copy_kernel, static_cast<char*>(dst), src, n);
+    kernel_launches++;
 }
 
 void Ctx::d2h(void* dst, void const* src, size_t bytes) {
@@ -1040,7 +1061,7 @@ void ensure_variant_tables(Ctx& ctx, Plan const& p) {
     if (!items64.empty()) std::memcpy(st + t_i64, items64.data(), sizeof(ItemRec) * items64.size());
     if (!items_tc.empty()) std::memcpy(st + t_itc, items_tc.data(), sizeof(TcTile) * items_tc.size());
     if (!pairs_tc.empty()) std::memcpy(st + t_ptc, pairs_tc.data(), sizeof(TcPair) * pairs_tc.size());
-    ITG_CHECK_CUDA(cudaMemcpyAsync(dev->p, st, bytes, cudaMemcpyHostToDevice, ctx.stream));
+    ctx.ring_copy(dev->p, st, bytes);
     ctx.sync();  // resident before any stream launches with them
     char* db = dev->as<char>();
     p.d_items64 = reinterpret_cast<ItemRec*>(db + t_i64);
@@ -1488,7 +1509,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         plan->max_rows = max_rows;
         plan->dev = dev_alloc(tbytes, ctx.stream);
         char* db = plan->dev->as<char>();
-        ITG_CHECK_CUDA(cudaMemcpyAsync(db, st, tbytes, cudaMemcpyHostToDevice, ctx.stream));
+        ctx.ring_copy(db, st, tbytes);
         plan->d_items = reinterpret_cast<ItemRec*>(db + t_items);
         plan->d_pairs = reinterpret_cast<PairRec*>(db + t_pairs);
         plan->d_cblk = reinterpret_cast<CBlockRec*>(db + t_cblk);
@@ -1541,7 +1562,7 @@ std::shared_ptr<Plan> get_plan(Ctx& ctx, Layout const& A, Layout const& B, Match
         if (!tab.empty()) std::memcpy(st + t_tab, tab.data(), sizeof(int32_t) * tab.size());
         plan->dev = dev_alloc(tbytes, ctx.stream);
         char* db = plan->dev->as<char>();
-        ITG_CHECK_CUDA(cudaMemcpyAsync(db, st, tbytes, cudaMemcpyHostToDevice, ctx.stream));
+        ctx.ring_copy(db, st, tbytes);
         plan->d_items = reinterpret_cast<ItemRec*>(db + t_items);
         plan->d_pairs = nullptr;
         plan->d_cblk = reinterpret_cast<CBlockRec*>(db + t_cblk);

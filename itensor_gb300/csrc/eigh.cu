@@ -714,7 +714,7 @@ static int jacobi_eigh(Ctx& ctx, std::vector<EigItem> const& items, double const
     char* st = ctx.stage_ring(up);
     std::memcpy(st + o_jobs, jobs.data(), sizeof(EigJob) * nb);
     if (!vjobs.empty()) std::memcpy(st + o_vj, vjobs.data(), sizeof(VJob) * vjobs.size());
-    ITG_CHECK_CUDA(cudaMemcpyAsync(buf.p, st, up, cudaMemcpyHostToDevice, ctx.stream));
+    ctx.ring_copy(buf.p, st, up);
     char* db = buf.as<char>();
     int* d_stat = reinterpret_cast<int*>(db + o_stat);
     int* d_sw = reinterpret_cast<int*>(db + o_sw);

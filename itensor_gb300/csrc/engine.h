@@ -234,6 +234,7 @@ struct Ctx {
     // Pinned staging ring for uploads that do not wait for the stream: two
     // halves, a half reused only after the copies enqueued from it completed.
     char* ring = nullptr;
+    char* ring_dev = nullptr;  // the ring's device address (mapped, page-locked)
     size_t ring_half = 0, ring_off = 0;
     int ring_cur = 0;
     cudaEvent_t ring_ev[2] = {};
@@ -305,6 +306,10 @@ struct Ctx {
     char* stage_ring(size_t n);
     // host -> device copy through the ring, without waiting
     void upload(void* dst, void const* src, size_t n);
+    // dst <- n bytes staged at st (a stage_ring pointer), by a copy kernel that
+    // reads the ring through its device address (launched like the other small
+    // kernels, so a table upload does not break their launch overlap)
+    void ring_copy(void* dst, char const* st, size_t n);
     // waits for an event recorded on this context's streams (yields in a fiber)
     void wait_event(cudaEvent_t ev);
     // Waits for the stream. Inside a solver-pool fiber the wait yields to the

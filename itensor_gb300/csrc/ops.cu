@@ -448,7 +448,7 @@ void GatherPlan::upload(Ctx& ctx) {
     if (!items.empty()) std::memcpy(st + o_items, items.data(), sizeof(GatherItem) * items.size());
     if (!tab.empty()) std::memcpy(st + o_tab, tab.data(), sizeof(int32_t) * tab.size());
     dev = dev_alloc(bytes, ctx.stream);
-    ITG_CHECK_CUDA(cudaMemcpyAsync(dev->as<char>(), st, bytes, cudaMemcpyHostToDevice, ctx.stream));
+    ctx.ring_copy(dev->as<char>(), st, bytes);
     d_items = reinterpret_cast<GatherItem*>(dev->as<char>() + o_items);
     d_tab = reinterpret_cast<int32_t*>(dev->as<char>() + o_tab);
     nitems = (int)items.size();
@@ -519,7 +519,7 @@ void launch_noisy_rho(Ctx& ctx, std::vector<std::vector<NoiseBlock>> const& pass
         std::memcpy(st + k * pbytes, passes[k].data(), pbytes);
     }
     DevBuf tab(bytes + 16, ctx.stream);
-    ITG_CHECK_CUDA(cudaMemcpyAsync(tab.as<char>(), st, bytes, cudaMemcpyHostToDevice, ctx.stream));
+    ctx.ring_copy(tab.as<char>(), st, bytes);
     double* dtr = reinterpret_cast<double*>(tab.as<char>() + bytes);
     // pass 0: out = rho + noise (D_0 + D_0^T)/2; pass k: out += noise (D_k + D_k^T)/2 (in place)
     for (size_t k = 0; k < passes.size(); ++k) {
